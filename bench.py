@@ -1,0 +1,340 @@
+"""Benchmark of the GB300 bake-off operator apply.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (the headline configuration): BK5 collocated Laplacian, plain FP64,
+p = 7 (P = Q = 8 GLL points), E = 262144 elements = 134,217,728 DoFs on a
+64^3 grid of spacing h = 1/64 whose vertices are jittered by U[-0.15h, 0.15h]
+(seeded), G = w detJ J^-1 J^-T with 6 symmetric factors in BK5.cpp's
+interleaved layout, D the 8 x 8 GLL derivative, u ~ U[-1, 1] (seeded).  All
+inputs are synthetic (the reference names no dataset); the inputs (8.6 GB per
+apply) are 65x the 129 MB L2, so no flush is needed between steps.
+
+One step = one apply v = D^T G D u.  `value` is GDoF/s with u, G, v resident
+in HBM (CUDA events on the launching stream, K steps); `e2e` is the same
+apply through the C ABI from pinned host memory: every step copies u to the
+device and v back (G, the operator, stays resident, as the reference's
+`omp target data` region keeps it mapped, openmp/BK5.cpp:133).  The plain FP64
+form uses the float-float engine (FP64 storage, FP64-accurate arithmetic on
+the FP32 pipes: the GB300's FP64 pipe runs at 1/64 rate); the native-DFMA
+engine and the FP32-storage mixed form are timed beside it ("forms").
+
+`--impl reference` times the reference's algorithm on the host cores: the
+oracle's C restatement of bk::SumFactorization<double, 8> (openmp/BK5.cpp:
+19-103) with OpenMP over all cores, on a bounded sample of the same workload.
+Multi-GPU (torchrun): replicas only (the apply has no exchange step); every
+rank applies the operator to its own elements, value = all DoFs / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "GDOF/s per apply on 1 GB300: plain FP64 vs mixed/batched at stated error"
+UNIT = "GDoF/s"
+P_ORDER = 7
+NX = 64
+E_FULL = NX ** 3
+SEED_U, SEED_G = 1, 2
+H = 1.0 / NX
+JITTER = 0.15
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--elements", type=int, default=E_FULL, help="override E (profiling a smaller case)")
+    ap.add_argument("--engine", default="ff", choices=["ff", "dfma"])
+    ap.add_argument("--no-forms", action="store_true", help="skip the side-by-side forms")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+# ---- distributed plumbing -------------------------------------------------------
+
+def dist_setup(n):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl")
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---- clocks -----------------------------------------------------------------------
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---- workload -----------------------------------------------------------------------
+
+def make_inputs(bk, E, torch):
+    """Device inputs of the headline workload (FP64), built on the GPU."""
+    D, x, w = bk.bk5_matrices(P_ORDER)
+    Q = P_ORDER + 1
+    n = E * Q ** 3
+    u = torch.empty(n, dtype=torch.float64, device="cuda")
+    G = torch.empty(6 * n, dtype=torch.float64, device="cuda")
+    bk.fill_uniform(u, SEED_U, -1.0, 1.0)
+    bk.geom_trilinear(Q, E, NX, NX, x, w, SEED_G, H, JITTER, G=G, layout=bk.LAYOUT_INTERLEAVED)
+    torch.cuda.synchronize()
+    return D, u, G
+
+
+def time_loop(fn, steps, warmup, world, stream, torch):
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for _ in range(steps):
+        fn()
+    t1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    torch.cuda.synchronize()
+    return t0.elapsed_time(t1) / 1e3 / steps   # seconds per step
+
+
+def cpu_baseline_run(sample_E, reps):
+    """The oracle's restatement of the reference's BK5 kernel in double, OpenMP
+    over the host cores, on `sample_E` elements of the workload; min time over
+    `reps` (bk::time_min, include/bk_common.h:182-192)."""
+    import numpy as np
+
+    import oracle
+    Q = P_ORDER + 1
+    rng = np.random.default_rng(0)
+    D = np.asarray(__import__("omp_bk_gb300").bk5_matrices(P_ORDER)[0])
+    u = rng.uniform(-1, 1, sample_E * Q ** 3)
+    G = rng.uniform(0.5, 1.5, sample_E * 6 * Q ** 3)
+    oracle.lib(fast=True)
+    best = float("inf")
+    for _ in range(reps):
+        t = time.perf_counter()
+        oracle.bk5(Q, sample_E, D, G, u, fast=True)
+        best = min(best, time.perf_counter() - t)
+    cores = os.cpu_count()
+    return {"value": sample_E * Q ** 3 / best / 1e9, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"BK5 p=7 FP64, {sample_E} of the {E_FULL} elements (random u, G), min of {reps} applies, "
+                      f"OMP over {cores} host threads (oracle/bk_oracle.c, -O3)"}
+
+
+def traffic_from_profiles():
+    """DRAM bytes per launch of the headline kernel from the committed ncu
+    summary (profiles/bk5_p7_fp64.json), scaled to the full workload."""
+    path = os.path.join(ROOT, "profiles", "bk5_p7_fp64.json")
+    try:
+        d = json.load(open(path))
+        return d.get("dram_bytes_per_launch_full")
+    except (OSError, ValueError):
+        return None
+
+
+def measured_peak():
+    try:
+        d = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, ValueError, KeyError):
+        return 6800.0, "fallback"
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    reps = max(1, min(args.steps, 5))
+    cb = cpu_baseline_run(32768, reps)
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
+            "steps": reps, "warmup": 0, "ms_per_step": 32768 * 512 / cb["value"] / 1e6, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "BK5 p=7 FP64 apply, E=262144 (134M DoFs), CPU sample of 32768 elements",
+                       "p": P_ORDER, "elements": E_FULL},
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import torch
+
+    import omp_bk_gb300 as bk
+    rank, world, local = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    stream = torch.cuda.current_stream()
+    E = args.elements
+    Q = P_ORDER + 1
+    dofs = E * Q ** 3
+    D, u, G = make_inputs(bk, E, torch)
+    v = torch.empty_like(u)
+    engine = bk.ENGINE_FF if args.engine == "ff" else bk.ENGINE_DFMA
+
+    def apply():
+        bk.bk5_apply(P_ORDER, E, D, G, u, v, prec=bk.PREC_FP64, engine=engine, stream=stream)
+
+    steps, warmup = args.steps, max(args.warmup, 3)
+    with ClockSampler(local) as clk:
+        t = time_loop(apply, steps, warmup, world, stream, torch)
+    t = max_over_ranks(t, world)
+    value = world * dofs / t / 1e9
+    bytes_per_apply = 8 * (2 + 6) * dofs
+    peak, peak_kind = measured_peak()
+    achieved = bytes_per_apply / t / 1e9
+    traffic = traffic_from_profiles() if E == E_FULL else None
+
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps, "warmup": warmup,
+           "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f64", "data": "synthetic",
+           "config": {"workload": f"BK5 collocated Laplacian p={P_ORDER} (P=Q=8 GLL) FP64 apply, E={E} "
+                                  f"({dofs} DoFs), jittered trilinear mesh, G6 interleaved",
+                      "p": P_ORDER, "elements": E, "engine": args.engine, "l2": "inputs 8.6 GB >> 129 MB L2, no flush",
+                      "parallelism": f"replicas x{world}"},
+           "gpu_launches": steps,
+           "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                        "frac": achieved / peak, "traffic": traffic,
+                        "note": f"peak = {peak_kind} copy bandwidth (MEASURED_PEAKS.json hbm_gbs); algorithmic "
+                                f"bytes = 8 B x (u + v + 6 G) per DoF"},
+           "clocks": clk.summary()}
+
+    # end to end through the C ABI: pinned host u -> device, apply, v -> pinned host
+    if not args.no_e2e:
+        uh = torch.empty(u.numel(), dtype=torch.float64, pin_memory=True)
+        vh = torch.empty_like(uh)
+        uh.copy_(u)
+
+        def e2e():
+            u.copy_(uh, non_blocking=True)
+            apply()
+            vh.copy_(v, non_blocking=True)
+
+        te = max_over_ranks(time_loop(e2e, max(3, steps // 10), 2, world, stream, torch), world)
+        out["e2e"] = {"value": world * dofs / te / 1e9, "unit": UNIT, "h2d_bytes_per_step": 8 * dofs,
+                      "d2h_bytes_per_step": 8 * dofs, "ms_per_step": te * 1e3,
+                      "note": "G (6.4 GB) resident on the device; u in, v out every step"}
+
+    # the forms side by side, with their error against the FP64 result
+    if not args.no_forms and rank == 0:
+        forms = {}
+        ref = v.clone()
+        forms["fp64_ff"] = {"gdofs": value / world, "rel_err_vs_fp64": 0.0}
+        vd = torch.empty_like(v)
+        td = time_loop(lambda: bk.bk5_apply(P_ORDER, E, D, G, u, vd, engine=bk.ENGINE_DFMA, stream=stream),
+                       max(3, steps // 20), 2, 1, stream, torch)
+        forms["fp64_dfma"] = {"gdofs": dofs / td / 1e9,
+                              "rel_err_vs_fp64": float((vd - ref).abs().max() / ref.abs().max())}
+        del vd
+        u32, G32 = u.float(), G.float()
+        v32 = torch.empty_like(u32)
+        for name, prec in (("mixed_fp32_storage", bk.PREC_MIXED), ("fp32", bk.PREC_FP32)):
+            tm = time_loop(lambda: bk.bk5_apply(P_ORDER, E, D, G32, u32, v32, prec=prec, stream=stream),
+                           max(3, steps // 4), 3, 1, stream, torch)
+            err = float((v32.double() - ref).abs().max() / ref.abs().max())
+            forms[name] = {"gdofs": dofs / tm / 1e9, "rel_err_vs_fp64": err,
+                           "hbm_frac": 4 * 8 * dofs / tm / 1e9 / peak}
+        out["forms"] = forms
+        del u32, G32, v32
+
+    if rank == 0 and world == 1 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline_run(32768, 3)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

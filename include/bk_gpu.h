@@ -1,0 +1,176 @@
+/* bk_gpu.h -- C ABI of the GB300 bake-off operator apply (BK1 mass, BK3
+ * Poisson, BK5 collocated Laplacian) on element-major hexahedral E-vectors.
+ *
+ * The reference (ivan-pi/omp_bk) has no library and no FFI: its "interface"
+ * is the kernel template
+ *     template <typename T, int nq> void bk::SumFactorization(
+ *         std::size_t nelmt, const T* basis, const T* JxW|G, const T* in, T* out)
+ * (openmp/bk1_sumfact.h:16-22, openmp/bk3_sumfact.h:17-24 with basis and
+ * dbasis, openmp/BK5.cpp:18-24 with dbasis), called by the drivers through the
+ * function-pointer type sumfact_kernel<T> (openmp/bk1_sumfact.h:161-163) and
+ * the variant tables of the GPU harnesses.  Each entry point below replaces one
+ * of those templates for every order p = 1..8 at once (run-time p dispatched to
+ * a compile-time nq, as bk::with_order does, include/bk_common.h:148-178).
+ *
+ * Conventions (all entry points):
+ *   - p is the polynomial order; BK1/BK3 use P = p + 1 nodes and Q = p + 2
+ *     points per direction (openmp/BK1.cpp:41), BK5 uses Q = p + 1
+ *     (openmp/BK5.cpp:153).  E is the number of elements (0 is a no-op).
+ *   - The 1-D matrices (B, D) are HOST pointers to row-major doubles in the
+ *     reference's convention: B(i,p) = B[i*Q + p] (P x Q, node-major,
+ *     bk1_sumfact.h:39); BK3's D(n,p) = D[n*Q + p] (bk3_sumfact.h:41); BK5's
+ *     D(i,n) = D[i*Q + n] (BK5.cpp:290).  They are at most 10 x 10 and are
+ *     passed by value into the launch (constant bank): no device copy, no
+ *     allocation, safe to capture in a CUDA graph.
+ *   - All other arrays are DEVICE pointers, 16-byte aligned, element-major with
+ *     the last index fastest, in the storage type of `prec`: double for
+ *     BK_PREC_FP64, float for BK_PREC_FP32 and BK_PREC_MIXED.
+ *   - The call is asynchronous on `stream` (0: the legacy default stream),
+ *     allocates nothing and synchronizes nothing.  Calls on distinct streams
+ *     may run concurrently.
+ *   - Return value: BK_OK or one of the BK_ERR_* codes below.  Argument errors
+ *     are detected on the host before any launch.  Errors that only the GPU
+ *     can see (a bounded wait that gave up) are recorded in a device status
+ *     word read by bk_device_status().
+ */
+#ifndef BK_GPU_H
+#define BK_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* A CUDA stream (cudaStream_t); declared here so that callers need no CUDA
+ * header. */
+typedef struct CUstream_st* bk_stream_t;
+
+/* ---- status codes --------------------------------------------------------- */
+enum bk_status {
+    BK_OK = 0,
+    BK_ERR_ORDER = 1,    /* p outside 1..8: the reference's with_order prints
+                            "unsupported polynomial order p" (bk_common.h:170-177) */
+    BK_ERR_SIZE = 2,     /* E < 0, or an index would overflow 64 bits */
+    BK_ERR_ALIGN = 3,    /* a device pointer is not 16-byte aligned */
+    BK_ERR_NULL = 4,     /* a required pointer is NULL (E > 0) */
+    BK_ERR_PREC = 5,     /* unknown precision, engine, layout or factor count */
+    BK_ERR_CUDA = 6,     /* a CUDA launch or copy failed */
+    BK_ERR_TIMEOUT = 7,  /* a device-side wait gave up (device status only) */
+    BK_ERR_ARG = 8       /* another invalid argument */
+};
+
+/* ---- precision forms ------------------------------------------------------ */
+enum bk_prec {
+    BK_PREC_FP64 = 0,   /* FP64 storage, FP64-accurate arithmetic (engine below) */
+    BK_PREC_FP32 = 1,   /* FP32 storage and arithmetic: the reference drivers'
+                           T = float (openmp/BK1.cpp:41, BK3.cpp:60, BK5.cpp:153) */
+    BK_PREC_MIXED = 2   /* FP32 storage and FP32 FMA contractions, the final
+                           sum of the three directional terms compensated
+                           (float-float); used inside FP64-refined solvers */
+};
+
+/* ---- FP64 arithmetic engines (BK_PREC_FP64 only) -------------------------- */
+enum bk_engine {
+    BK_ENGINE_AUTO = 0, /* the fastest engine that meets 1e-12 (float-float) */
+    BK_ENGINE_DFMA = 1, /* native FP64 FMA */
+    BK_ENGINE_FF = 2    /* float-float on the FP32 pipes: values split into
+                           two floats (~48 significant bits) as they are
+                           loaded, joined back to double as they are stored
+                           (the technique of openmp/float_float.h) */
+};
+
+/* BK5 geometric-factor layouts (make_bk5_G, include/bk_harness.h:217-219). */
+enum bk_layout {
+    BK_LAYOUT_FACTOR = 0,      /* G(e, f, i, j, k) */
+    BK_LAYOUT_INTERLEAVED = 1, /* G(e, i, j, f, k): BK5.cpp's layout (:42, :296) */
+    BK_LAYOUT_COLUMN = 2       /* G(e, f, k, i, j) */
+};
+
+/* Options of the extended entry points; a NULL bk_options* means defaults. */
+typedef struct bk_options {
+    int prec;      /* bk_prec */
+    int engine;    /* bk_engine (FP64 only) */
+    int layout;    /* BK5: bk_layout; BK3 reads G factor-major (bk3_sumfact.h:53) */
+    int nfactors;  /* BK5: 6 (symmetric rr rs rt ss st tt) or 9 (full 3x3,
+                      row-major; bk5_offload.cpp "F") */
+    int elems_per_block; /* elements per thread block; 0: the tuned default */
+} bk_options;
+
+/* bk_options with the defaults: prec FP64, engine AUTO, BK5 layout
+ * INTERLEAVED with 6 factors, elems_per_block 0. */
+bk_options bk_default_options(void);
+
+/* ---- operator apply ------------------------------------------------------- */
+
+/* BK1 mass operator v = B^T diag(qdata) B u per element
+ * (replaces bk::SumFactorization<T, nq>, openmp/bk1_sumfact.h:16-159).
+ *   B      host, P x Q doubles, B(i,p) = B[i*Q+p]
+ *   qdata  device, E x Q^3 (quadrature weight x detJ, "JxW" in the reference)
+ *   u, v   device, E x P^3 */
+int bk1_apply(int p, int64_t E, const double* B, const void* qdata, const void* u, void* v,
+              int prec, bk_stream_t stream);
+
+/* BK3 Poisson operator v = B^T D^T G D B u per element
+ * (replaces bk::SumFactorization<T, nq>, openmp/bk3_sumfact.h:17-187).
+ *   B      host, P x Q doubles; D host, Q x Q doubles, D(n,p) = D[n*Q+p]
+ *   G      device, E x 6 x Q^3, factor-major (rr rs rt ss st tt)
+ *   u, v   device, E x P^3 */
+int bk3_apply(int p, int64_t E, const double* B, const double* D, const void* G, const void* u,
+              void* v, int prec, bk_stream_t stream);
+
+/* BK5 collocated Laplacian v = D^T G D u per element
+ * (replaces bk::SumFactorization<T, nq>, openmp/BK5.cpp:18-103).
+ *   D      host, Q x Q doubles, D(i,n) = D[i*Q+n]
+ *   G      device, E x 6 x Q^3 interleaved G(e,i,j,f,k) (BK5.cpp:296)
+ *   u, v   device, E x Q^3 */
+int bk5_apply(int p, int64_t E, const double* D, const void* G, const void* u, void* v, int prec,
+              bk_stream_t stream);
+
+/* The same with options (engine, BK5 layout and factor count, block shape):
+ * the variants of the reference's kernel harnesses (bk5_offload.cpp:7-28,
+ * variant table :716-772) behind one entry point.  opt may be NULL. */
+int bk1_apply_opt(int p, int64_t E, const double* B, const void* qdata, const void* u, void* v,
+                  const bk_options* opt, bk_stream_t stream);
+int bk3_apply_opt(int p, int64_t E, const double* B, const double* D, const void* G,
+                  const void* u, void* v, const bk_options* opt, bk_stream_t stream);
+int bk5_apply_opt(int p, int64_t E, const double* D, const void* G, const void* u, void* v,
+                  const bk_options* opt, bk_stream_t stream);
+
+/* BK5 plus a diagonal term: v = D^T G D u + lambda * mass .* u (the
+ * Helmholtz operator with the collocated GLL mass, no reference counterpart).
+ * mass: device, E x Q^3 in the storage type, or NULL for plain BK5. */
+int bk5_apply_ex(int p, int64_t E, const double* D, const void* G, const void* u, const void* mass,
+                 double lambda, void* v, const bk_options* opt, bk_stream_t stream);
+
+/* BK3 with a coefficient at the quadrature points: the fluxes are
+ * k(x) G(x) grad u(x) (no reference counterpart; the forward operator of the
+ * adjoint below).  k: device, E x Q^3, or NULL for plain BK3. */
+int bk3_apply_k(int p, int64_t E, const double* B, const double* D, const void* G, const void* k,
+                const void* u, void* v, const bk_options* opt, bk_stream_t stream);
+
+/* ---- device status -------------------------------------------------------- */
+
+/* Reads (and, if reset != 0, clears) the status word of the current device:
+ * BK_OK or the first device-side error (BK_ERR_TIMEOUT) recorded since the
+ * last reset.  Synchronizes `stream`. */
+int bk_device_status(int* status, int reset, bk_stream_t stream);
+
+/* Test hook: the cycle limit of every bounded device-side wait on the current
+ * device (default 4e9, about two seconds).  0 restores the default. */
+int bk_set_wait_limit(long long cycles);
+
+/* Test hook: launches one block that waits on a barrier nothing arrives on,
+ * with the current wait limit; the wait gives up, records BK_ERR_TIMEOUT in
+ * the status word and the kernel returns normally. */
+int bk_test_wait_timeout(bk_stream_t stream);
+
+/* Library version string. */
+const char* bk_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BK_GPU_H */

@@ -1,0 +1,314 @@
+"""omp_bk_gb300 -- GB300 (sm_103a) bake-off operator apply: BK1 mass, BK3
+Poisson, BK5 collocated Laplacian on element-major hexahedral E-vectors.
+
+The compute path is the CUDA library ``_lib/libbk_gb300.so`` behind the C ABI
+of ``include/bk_gpu.h`` (built by ``omp_bk_gb300.build``).  This module is a
+thin ctypes layer over it, mirroring the reference's operator interface
+``bk::SumFactorization<T, nq>(nelmt, basis, JxW|G, in, out)``
+(openmp/bk1_sumfact.h:16-22, openmp/bk3_sumfact.h:17-24, openmp/BK5.cpp:18-24):
+the same argument order and meaning, the order p dispatched at run time as
+``bk::with_order`` does (include/bk_common.h:148-178), and an unsupported
+order reported as ``unsupported polynomial order p = <p>``.  Device arrays are
+torch CUDA tensors (torch is used for device memory and streams only).
+
+There is no CPU fallback: without the built library every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "_lib", "libbk_gb300.so")
+
+# status codes (bk_gpu.h)
+BK_OK, BK_ERR_ORDER, BK_ERR_SIZE, BK_ERR_ALIGN, BK_ERR_NULL, BK_ERR_PREC, BK_ERR_CUDA, BK_ERR_TIMEOUT, BK_ERR_ARG = range(9)
+STATUS_NAMES = {0: "ok", 1: "unsupported polynomial order p", 2: "bad element count", 3: "misaligned pointer",
+                4: "null pointer", 5: "unsupported precision/engine/layout", 6: "CUDA error",
+                7: "device wait timed out", 8: "invalid argument"}
+# precisions, engines, layouts
+PREC_FP64, PREC_FP32, PREC_MIXED = 0, 1, 2
+ENGINE_AUTO, ENGINE_DFMA, ENGINE_FF = 0, 1, 2
+LAYOUT_FACTOR, LAYOUT_INTERLEAVED, LAYOUT_COLUMN = 0, 1, 2
+
+# every symbol the C headers declare (checked by the CPU tests)
+EXPORTS = [
+    "bk_default_options", "bk1_apply", "bk3_apply", "bk5_apply", "bk1_apply_opt", "bk3_apply_opt",
+    "bk5_apply_opt", "bk5_apply_ex", "bk3_apply_k", "bk_device_status", "bk_set_wait_limit",
+    "bk_test_wait_timeout", "bk_version",
+    "bk_gauss_points", "bk_gll_points", "bk_lagrange_interp", "bk_lagrange_deriv", "bk_fill_uniform",
+    "bk_fill_lognormal", "bk_geom_affine", "bk_coords_affine", "bk_geom_trilinear", "bk_convert",
+]
+
+
+class BKError(RuntimeError):
+    """A non-zero status of the C ABI."""
+
+    def __init__(self, code: int, what: str = ""):
+        self.code = code
+        super().__init__(f"{what}: {STATUS_NAMES.get(code, 'error')} (status {code})")
+
+
+class Options(C.Structure):
+    _fields_ = [("prec", C.c_int), ("engine", C.c_int), ("layout", C.c_int), ("nfactors", C.c_int),
+                ("elems_per_block", C.c_int)]
+
+
+_lib = None
+_vp = C.c_void_p
+_dp = C.POINTER(C.c_double)
+_i64 = C.c_int64
+
+
+def lib():
+    """The loaded CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -m omp_bk_gb300.build` "
+                           "(there is no CPU fallback)")
+    L = C.CDLL(LIB_PATH)
+    sig = {
+        "bk1_apply": [C.c_int, _i64, _dp, _vp, _vp, _vp, C.c_int, _vp],
+        "bk3_apply": [C.c_int, _i64, _dp, _dp, _vp, _vp, _vp, C.c_int, _vp],
+        "bk5_apply": [C.c_int, _i64, _dp, _vp, _vp, _vp, C.c_int, _vp],
+        "bk1_apply_opt": [C.c_int, _i64, _dp, _vp, _vp, _vp, C.POINTER(Options), _vp],
+        "bk3_apply_opt": [C.c_int, _i64, _dp, _dp, _vp, _vp, _vp, C.POINTER(Options), _vp],
+        "bk5_apply_opt": [C.c_int, _i64, _dp, _vp, _vp, _vp, C.POINTER(Options), _vp],
+        "bk5_apply_ex": [C.c_int, _i64, _dp, _vp, _vp, _vp, C.c_double, _vp, C.POINTER(Options), _vp],
+        "bk3_apply_k": [C.c_int, _i64, _dp, _dp, _vp, _vp, _vp, _vp, C.POINTER(Options), _vp],
+        "bk_device_status": [C.POINTER(C.c_int), C.c_int, _vp],
+        "bk_set_wait_limit": [C.c_longlong],
+        "bk_test_wait_timeout": [_vp],
+        "bk_gauss_points": [C.c_int, _dp, _dp],
+        "bk_gll_points": [C.c_int, _dp, _dp],
+        "bk_lagrange_interp": [C.c_int, _dp, C.c_int, _dp, _dp],
+        "bk_lagrange_deriv": [C.c_int, _dp, _dp],
+        "bk_fill_uniform": [_vp, C.c_longlong, C.c_ulonglong, C.c_double, C.c_double, C.c_int, _vp],
+        "bk_fill_lognormal": [_vp, C.c_longlong, C.c_ulonglong, C.c_double, C.c_int, _vp],
+        "bk_geom_affine": [C.c_int, C.c_longlong, _dp, _dp, C.c_ulonglong, C.c_double, C.c_double, _vp, _vp,
+                           C.c_int, _vp],
+        "bk_coords_affine": [C.c_int, C.c_longlong, C.c_int, C.c_int, _dp, C.c_ulonglong, C.c_double,
+                             C.c_double, _vp, _vp],
+        "bk_geom_trilinear": [C.c_int, C.c_longlong, C.c_int, C.c_int, _dp, _dp, C.c_ulonglong, C.c_double,
+                              C.c_double, _vp, C.c_int, _vp, _vp, _vp],
+        "bk_convert": [_vp, _vp, C.c_longlong, C.c_int, _vp],
+    }
+    for name, args in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = C.c_int
+    L.bk_version.restype = C.c_char_p
+    L.bk_default_options.restype = Options
+    _lib = L
+    return L
+
+
+def check(rc: int, what: str) -> None:
+    if rc != BK_OK:
+        raise BKError(rc, what)
+
+
+# ---- helpers -------------------------------------------------------------------
+
+def _host(a) -> tuple:
+    """A C double* to a contiguous float64 copy of `a` (kept alive by the
+    returned tuple)."""
+    arr = np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+    return arr, arr.ctypes.data_as(_dp)
+
+
+def _ptr(t) -> int | None:
+    if t is None:
+        return None
+    return t.data_ptr()
+
+
+def _order(p: int, what: str) -> None:
+    """bk::with_order (include/bk_common.h:162-178): orders 1..8."""
+    if not 1 <= int(p) <= 8:
+        raise BKError(BK_ERR_ORDER, f"{what}: p = {p}")
+
+
+def _stream(stream):
+    if stream is None:
+        import torch
+        return torch.cuda.current_stream().cuda_stream
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream
+
+
+def order_q(bk: int, p: int) -> int:
+    """Points per direction: p + 2 for BK1/BK3 (openmp/BK1.cpp:41), p + 1 for
+    BK5 (openmp/BK5.cpp:153)."""
+    return p + 1 if bk == 5 else p + 2
+
+
+@dataclass
+class ApplyOptions:
+    prec: int = PREC_FP64
+    engine: int = ENGINE_AUTO
+    layout: int = LAYOUT_INTERLEAVED
+    nfactors: int = 6
+    elems_per_block: int = 0
+
+    def c(self) -> Options:
+        return Options(self.prec, self.engine, self.layout, self.nfactors, self.elems_per_block)
+
+
+# ---- operator apply (device tensors) -------------------------------------------
+
+def bk1_apply(p, E, B, qdata, u, v, prec=PREC_FP64, engine=ENGINE_AUTO, stream=None):
+    """v = B^T diag(qdata) B u per element (openmp/bk1_sumfact.h:16-159)."""
+    _order(p, "bk1_apply")
+    Bh, Bp = _host(B)
+    o = ApplyOptions(prec=prec, engine=engine).c()
+    check(lib().bk1_apply_opt(p, E, Bp, _ptr(qdata), _ptr(u), _ptr(v), C.byref(o), _stream(stream)), "bk1_apply")
+
+
+def bk3_apply(p, E, B, D, G, u, v, k=None, prec=PREC_FP64, engine=ENGINE_AUTO, stream=None):
+    """v = B^T D^T (k) G D B u per element (openmp/bk3_sumfact.h:17-187); G
+    factor-major, k an optional coefficient at the quadrature points."""
+    _order(p, "bk3_apply")
+    Bh, Bp = _host(B)
+    Dh, Dp = _host(D)
+    o = ApplyOptions(prec=prec, engine=engine).c()
+    check(lib().bk3_apply_k(p, E, Bp, Dp, _ptr(G), _ptr(k), _ptr(u), _ptr(v), C.byref(o), _stream(stream)),
+          "bk3_apply")
+
+
+def bk5_apply(p, E, D, G, u, v, prec=PREC_FP64, engine=ENGINE_AUTO, layout=LAYOUT_INTERLEAVED, nfactors=6,
+              mass=None, lam=0.0, stream=None):
+    """v = D^T G D u (+ lam * mass * u) per element (openmp/BK5.cpp:18-103)."""
+    _order(p, "bk5_apply")
+    Dh, Dp = _host(D)
+    o = ApplyOptions(prec=prec, engine=engine, layout=layout, nfactors=nfactors).c()
+    check(lib().bk5_apply_ex(p, E, Dp, _ptr(G), _ptr(u), _ptr(mass), float(lam), _ptr(v), C.byref(o),
+                             _stream(stream)), "bk5_apply")
+
+
+def sum_factorization(bk: int, p: int, nelmt: int, *args, prec=PREC_FP64, **kw):
+    """The reference's kernel interface: SumFactorization(nelmt, basis, JxW, in,
+    out) for BK1, (nelmt, basis, dbasis, G, in, out) for BK3 and (nelmt,
+    dbasis, G, in, out) for BK5, with the order p as a run-time argument."""
+    if bk == 1:
+        basis, jxw, inp, out = args
+        return bk1_apply(p, nelmt, basis, jxw, inp, out, prec=prec, **kw)
+    if bk == 3:
+        basis, dbasis, G, inp, out = args
+        return bk3_apply(p, nelmt, basis, dbasis, G, inp, out, prec=prec, **kw)
+    if bk == 5:
+        dbasis, G, inp, out = args
+        return bk5_apply(p, nelmt, dbasis, G, inp, out, prec=prec, **kw)
+    raise ValueError(f"unknown operator BK{bk}")
+
+
+def device_status(reset: bool = True, stream=None) -> int:
+    s = C.c_int(0)
+    check(lib().bk_device_status(C.byref(s), 1 if reset else 0, _stream(stream)), "bk_device_status")
+    return s.value
+
+
+def version() -> str:
+    return lib().bk_version().decode()
+
+
+# ---- 1-D rules and matrices (host) ---------------------------------------------
+
+def gauss(n: int):
+    x = np.empty(n)
+    w = np.empty(n)
+    check(lib().bk_gauss_points(n, x.ctypes.data_as(_dp), w.ctypes.data_as(_dp)), "bk_gauss_points")
+    return x, w
+
+
+def gll(n: int):
+    x = np.empty(n)
+    w = np.empty(n)
+    check(lib().bk_gll_points(n, x.ctypes.data_as(_dp), w.ctypes.data_as(_dp)), "bk_gll_points")
+    return x, w
+
+
+def lagrange_interp(nodes, pts):
+    nodes = np.ascontiguousarray(nodes, dtype=np.float64)
+    pts = np.ascontiguousarray(pts, dtype=np.float64)
+    B = np.empty(nodes.size * pts.size)
+    check(lib().bk_lagrange_interp(nodes.size, nodes.ctypes.data_as(_dp), pts.size, pts.ctypes.data_as(_dp),
+                                   B.ctypes.data_as(_dp)), "bk_lagrange_interp")
+    return B
+
+
+def lagrange_deriv(x):
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    D = np.empty(x.size * x.size)
+    check(lib().bk_lagrange_deriv(x.size, x.ctypes.data_as(_dp), D.ctypes.data_as(_dp)), "bk_lagrange_deriv")
+    return D
+
+
+def bk1_bk3_matrices(p: int):
+    """(B, D_bk3, gauss x, gauss w, gll x) for BK1/BK3 at order p: P = p + 1
+    GLL nodes, Q = p + 2 Gauss points; B(i, q) = l_i(x_q) (P x Q) and the BK3
+    derivative D(n, q) = l_n'(x_q) on the Gauss points."""
+    P, Q = p + 1, p + 2
+    xn, _ = gll(P)
+    xq, wq = gauss(Q)
+    B = lagrange_interp(xn, xq)
+    D = lagrange_deriv(xq).reshape(Q, Q).T.copy().ravel()
+    return B, D, xq, wq, xn
+
+
+def bk5_matrices(p: int):
+    """(D, gll x, gll w) for BK5 at order p: Q = p + 1 GLL points, D(i, n) =
+    l_n'(x_i)."""
+    Q = p + 1
+    x, w = gll(Q)
+    return lagrange_deriv(x), x, w
+
+
+# ---- seeded device inputs ------------------------------------------------------
+
+def fill_uniform(t, seed: int, lo: float = -1.0, hi: float = 1.0, stream=None):
+    import torch
+    check(lib().bk_fill_uniform(_ptr(t), t.numel(), seed, lo, hi, int(t.dtype == torch.float64), _stream(stream)),
+          "bk_fill_uniform")
+    return t
+
+
+def fill_lognormal(t, seed: int, sigma: float, stream=None):
+    import torch
+    check(lib().bk_fill_lognormal(_ptr(t), t.numel(), seed, sigma, int(t.dtype == torch.float64), _stream(stream)),
+          "bk_fill_lognormal")
+    return t
+
+
+def geom_affine(Q, E, x, w, seed, h, pert, qdata=None, G=None, layout=LAYOUT_FACTOR, stream=None):
+    xh, xp = _host(x)
+    wh, wp = _host(w)
+    check(lib().bk_geom_affine(Q, E, xp, wp, seed, h, pert, _ptr(qdata), _ptr(G), layout, _stream(stream)),
+          "bk_geom_affine")
+
+
+def coords_affine(Q, E, nx, ny, x, seed, h, pert, coords, stream=None):
+    xh, xp = _host(x)
+    check(lib().bk_coords_affine(Q, E, nx, ny, xp, seed, h, pert, _ptr(coords), _stream(stream)), "bk_coords_affine")
+
+
+def geom_trilinear(Q, E, nx, ny, x, w, seed, h, jit, G=None, layout=LAYOUT_INTERLEAVED, mass=None, coords=None,
+                   stream=None):
+    xh, xp = _host(x)
+    wh, wp = _host(w)
+    check(lib().bk_geom_trilinear(Q, E, nx, ny, xp, wp, seed, h, jit, _ptr(G), layout, _ptr(mass), _ptr(coords),
+                                  _stream(stream)), "bk_geom_trilinear")
+
+
+def convert(src, dst, stream=None):
+    import torch
+    assert src.numel() == dst.numel()
+    check(lib().bk_convert(_ptr(src), _ptr(dst), src.numel(), int(dst.dtype == torch.float32), _stream(stream)),
+          "bk_convert")
+    return dst

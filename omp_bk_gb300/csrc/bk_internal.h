@@ -1,0 +1,32 @@
+// bk_internal.h -- declarations shared by the translation units of the
+// library (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "bk_gpu.h"
+
+namespace bkg {
+
+struct DevCtx;
+
+constexpr int kMaxDevices = 64;
+
+int current_device();          // cudaGetDevice, or -1
+int sm_count();                // SMs of the current device
+DevCtx dev_ctx();              // status word and wait limit of the current device
+
+#define BK_DECLARE_ENGINE(sfx)                                                                                    \
+    int launch_bk5_##sfx(int p, long long E, const double* D, const void* G, const void* u, const void* mass,    \
+                         double lambda, void* v, int F, int layout, int eb, cudaStream_t s);                     \
+    int launch_bk1_##sfx(int p, long long E, const double* B, const void* jxw, const void* u, void* v, int eb,   \
+                         cudaStream_t s);                                                                        \
+    int launch_bk3_##sfx(int p, long long E, const double* B, const double* D, const void* G, const void* k,     \
+                         const void* u, void* v, int eb, cudaStream_t s);
+
+BK_DECLARE_ENGINE(dfma)
+BK_DECLARE_ENGINE(ff)
+BK_DECLARE_ENGINE(f32)
+BK_DECLARE_ENGINE(mixed)
+
+}  // namespace bkg

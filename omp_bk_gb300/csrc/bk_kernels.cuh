@@ -1,0 +1,604 @@
+// bk_kernels.cuh -- the BK1 / BK3 / BK5 operator kernels for sm_103a.
+//
+// One thread block processes a batch of EB elements at a time (grid-stride
+// over the batches).  Per batch:
+//   1. stage: the batch's slices of u and of the geometric data (qdata or G)
+//      are contiguous in HBM (element-major E-vectors); each is copied into
+//      shared memory by one 1-D TMA bulk copy (cp.async.bulk, completion on an
+//      mbarrier with a bounded wait).  The copy starts at the first 16-byte
+//      boundary of the slice; the few values before it and after the last
+//      boundary are loaded by threads, so any element count and any odd
+//      extent is staged without an alignment condition on the batch.
+//   2. load pass: u is converted to the working type (float-float split for
+//      the FP64 engine) into a padded work box.
+//   3. sweeps: every 1-D contraction (interpolation with B, derivative with
+//      D, and their transposes) is a "sweep" of one direction: one thread per
+//      line of the box loads the line into registers, forms all outputs of the
+//      line and writes them back.  The 1-D matrices are kernel parameters
+//      (__grid_constant__), so every coefficient is an operand of the FMA
+//      straight from the constant bank.
+//   4. pointwise: qdata (BK1) or G (BK3, BK5, with the optional coefficient k
+//      of BK3) at every quadrature point.
+//   5. the result is assembled densely in shared memory and written to HBM
+//      with coalesced stores.
+// Work boxes are padded (row stride ZP, plane stride PS) so that the
+// thread-per-line accesses of all three directions spread over the 32 banks.
+#pragma once
+
+#include <cstdint>
+
+#include "bk_device.cuh"
+#include "bk_engine.cuh"
+
+namespace bkg {
+
+constexpr int kMaxQ = 10;
+
+// ---- padded work boxes ---------------------------------------------------------
+
+// Row and plane strides of a Q x Q x Q work box of `vbytes`-byte values.
+// Rows of odd length in 8-byte words (or in 4-byte words) keep the
+// contiguous lines of direction 2 on distinct banks; the plane stride is
+// chosen so that the lines of direction 1 (which differ in the plane index)
+// split evenly across the banks.
+constexpr int box_zp(int q) { return (q % 2 == 0) ? q + 1 : q; }
+constexpr int box_ps(int q, int vbytes)
+{
+    // plane stride in words of the value: for 8-byte values aim at PS = 8
+    // (mod 16), for 4-byte values at PS = 8 (mod 32) or 16 (mod 32)
+    return (vbytes == 8) ? ((q * box_zp(q)) % 16 == 8 ? q * box_zp(q) : q * box_zp(q) + ((24 - (q * box_zp(q)) % 16) % 16))
+                         : ((q * box_zp(q)) % 32 == 8 ? q * box_zp(q) : q * box_zp(q) + ((40 - (q * box_zp(q)) % 32) % 32));
+}
+
+template <int Q, class V>
+struct WBox {
+    static constexpr int ZP = box_zp(Q);
+    static constexpr int PS = box_ps(Q, int(sizeof(V)));
+    static constexpr int size = Q * PS;   // values per element (padded)
+    __device__ static __forceinline__ int at(int i, int j, int k) { return i * PS + j * ZP + k; }
+};
+
+// ---- staging -------------------------------------------------------------------
+
+// Shared-memory footprint (bytes) of a staged slice of n values of type S:
+// 16 bytes of slack for the alignment of the slice's first value.
+template <class S>
+constexpr int stage_bytes(int n)
+{
+    return ((n * int(sizeof(S)) + 15) / 16) * 16 + 16;
+}
+
+// Issues the copy of src[0, n) (global) into the shared buffer `buf`
+// (16-byte aligned, stage_bytes(n) long).  Returns where src[0] lands.
+// Thread 0 issues the TMA part and adds its bytes to *tx; the head and the
+// tail (fewer than 16 bytes each) are loaded by the threads of the block.
+template <class S>
+__device__ __forceinline__ S* stage_issue(void* buf, const S* src, int n, uint64_t* bar, uint32_t& tx,
+                                          int tid, int nt)
+{
+    const uintptr_t a = reinterpret_cast<uintptr_t>(src);
+    const uintptr_t b = a + uintptr_t(n) * sizeof(S);
+    const uintptr_t a_up = (a + 15) & ~uintptr_t(15);
+    const uintptr_t b_dn = b & ~uintptr_t(15);
+    // place src[0] at offset (a mod 16) so that a_up lands on a 16-byte boundary
+    char* dst0 = static_cast<char*>(buf) + (a & 15);
+    S* dst = reinterpret_cast<S*>(dst0);
+    if (a_up < b_dn) {
+        if (tid == 0) {
+            tma_load_1d(dst0 + (a_up - a), reinterpret_cast<const void*>(a_up), uint32_t(b_dn - a_up), bar);
+        }
+        tx += uint32_t(b_dn - a_up);
+        const int head = int((a_up - a) / sizeof(S));
+        const int tail0 = int((b_dn - a) / sizeof(S));
+        for (int i = tid; i < head; i += nt) dst[i] = src[i];
+        for (int i = tail0 + tid; i < n; i += nt) dst[i] = src[i];
+    } else {
+        for (int i = tid; i < n; i += nt) dst[i] = src[i];
+    }
+    return dst;
+}
+
+// ---- sweeps --------------------------------------------------------------------
+
+// Coefficient M(o, n) of a 1-D matrix stored row-major with leading dimension
+// LD, optionally transposed.  `m` points into the kernel's parameter space.
+template <class C, int LD, bool T>
+struct Mat {
+    const C* m;
+    __device__ __forceinline__ C operator()(int o, int n) const { return T ? m[n * LD + o] : m[o * LD + n]; }
+};
+
+// Contract direction DIR of the box with extents (X, Y, Z) in `in` into `out`
+// (extent NO along DIR): out(.., o, ..) = sum_n M(o, n) in(.., n, ..).  Boxes
+// use the padded strides of WB whatever their extents; in == out is allowed
+// (each line is read completely before it is written).  Lines of all `ne`
+// elements are spread over the block's threads.
+template <class Eng, class WB, int DIR, int X, int Y, int Z, int NO, class M>
+__device__ __forceinline__ void sweep(const typename Eng::V* in, typename Eng::V* out, int ne, const M& mat,
+                                      int tid, int nt)
+{
+    using V = typename Eng::V;
+    using A = typename Eng::A;
+    constexpr int NI = DIR == 0 ? X : (DIR == 1 ? Y : Z);
+    constexpr int LB = DIR == 2 ? Y : Z;
+    constexpr int L = (X * Y * Z) / NI;
+    constexpr int SD = DIR == 0 ? WB::PS : (DIR == 1 ? WB::ZP : 1);
+    for (int w = tid; w < ne * L; w += nt) {
+        const int e = w / L;
+        const int l = w - e * L;
+        const int a = l / LB;
+        const int b = l - a * LB;
+        int base = (DIR == 0) ? a * WB::ZP + b : (DIR == 1 ? a * WB::PS + b : a * WB::PS + b * WB::ZP);
+        base += e * WB::size;
+        V x[NI];
+#pragma unroll
+        for (int n = 0; n < NI; ++n) x[n] = in[base + n * SD];
+#pragma unroll
+        for (int o = 0; o < NO; ++o) {
+            A acc = Eng::zero();
+#pragma unroll
+            for (int n = 0; n < NI; ++n) Eng::madd(acc, mat(o, n), x[n]);
+            out[base + o * SD] = Eng::result(acc);
+        }
+    }
+}
+
+// Dense (X, Y, Z) slice of S values of `ne` elements (element stride estride)
+// -> padded work box, converted to the working type.
+template <class Eng, class WB, int X, int Y, int Z>
+__device__ __forceinline__ void load_box(const typename Eng::S* src, int estride, typename Eng::V* dst, int ne,
+                                         int tid, int nt)
+{
+    constexpr int N = X * Y * Z;
+    for (int w = tid; w < ne * N; w += nt) {
+        const int e = w / N;
+        const int x = w - e * N;
+        const int i = x / (Y * Z);
+        const int r = x - i * (Y * Z);
+        const int j = r / Z;
+        const int k = r - j * Z;
+        dst[e * WB::size + WB::at(i, j, k)] = Eng::load(src[e * estride + x]);
+    }
+}
+
+// Padded work box -> dense (X, Y, Z) S values.
+template <class Eng, class WB, int X, int Y, int Z>
+__device__ __forceinline__ void store_box(const typename Eng::V* src, typename Eng::S* dst, int estride, int ne,
+                                          int tid, int nt)
+{
+    constexpr int N = X * Y * Z;
+    for (int w = tid; w < ne * N; w += nt) {
+        const int e = w / N;
+        const int x = w - e * N;
+        const int i = x / (Y * Z);
+        const int r = x - i * (Y * Z);
+        const int j = r / Z;
+        const int k = r - j * Z;
+        dst[e * estride + x] = Eng::store(src[e * WB::size + WB::at(i, j, k)]);
+    }
+}
+
+template <class S>
+__device__ __forceinline__ void store_out(const S* src, S* dst, int n, int tid, int nt)
+{
+    for (int i = tid; i < n; i += nt) dst[i] = src[i];
+}
+
+// Waits (bounded) for the batch's staged copies; the block agrees on the
+// outcome with one barrier.  On a timeout the status word records
+// BK_ERR_TIMEOUT, every thread waits once more (bounded) so that copies still
+// in flight land before the block leaves, and true is returned: the caller
+// returns without touching the batch.
+__device__ __forceinline__ bool batch_wait_failed(uint64_t* bar, uint32_t phase, const DevCtx& ctx, int tid)
+{
+    const bool ok = mbar_wait_bounded(bar, phase, ctx.wait_limit);
+    if (__syncthreads_or(ok ? 0 : 1)) {
+        if (tid == 0) set_status(ctx, BK_ERR_TIMEOUT);
+        if (!ok) mbar_wait_bounded(bar, phase, ctx.wait_limit);
+        return true;
+    }
+    return false;
+}
+
+// ---- kernel parameters ---------------------------------------------------------
+
+template <class C, int Q>
+struct P5 {
+    C D[Q * Q];   // D(i, n) = D[i*Q + n]
+};
+
+template <class C, int Q>
+struct P13 {
+    C B[(Q - 1) * Q];   // B(i, p) = B[i*Q + p]
+    C D[Q * Q];         // BK3: D(n, p) = D[n*Q + p]
+};
+
+// ---- BK5 -----------------------------------------------------------------------
+
+template <class Eng, int Q, int F, int LAYOUT>
+__device__ __forceinline__ int g_index(int i, int j, int f, int k)
+{
+    if (LAYOUT == 0) return ((f * Q + i) * Q + j) * Q + k;
+    if (LAYOUT == 1) return ((i * Q + j) * F + f) * Q + k;
+    return ((f * Q + k) * Q + i) * Q + j;
+}
+
+template <class Eng, int Q, int EB, int F, int LAYOUT>
+struct BK5Cfg {
+    using S = typename Eng::S;
+    using V = typename Eng::V;
+    using WB = WBox<Q, V>;
+    static constexpr int Q3 = Q * Q * Q;
+    static constexpr int NT = ((EB * Q * Q + 31) / 32) * 32 < 64 ? 64 : ((EB * Q * Q + 31) / 32) * 32;
+    static constexpr int U_BYTES = stage_bytes<S>(EB * Q3);
+    static constexpr int G_BYTES = stage_bytes<S>(EB * F * Q3);
+    static constexpr int W_BYTES = 3 * EB * WB::size * int(sizeof(V));
+    static constexpr int SMEM = U_BYTES + G_BYTES + W_BYTES + 16;
+};
+
+template <class Eng, int Q, int EB, int F, int LAYOUT>
+__global__ void __launch_bounds__(BK5Cfg<Eng, Q, EB, F, LAYOUT>::NT)
+    bk5_kernel(const __grid_constant__ P5<typename Eng::C, Q> prm, const long long E,
+               const typename Eng::S* __restrict__ u, const typename Eng::S* __restrict__ G,
+               const typename Eng::S* __restrict__ mass, const double lambda, typename Eng::S* __restrict__ v,
+               const DevCtx ctx)
+{
+    using Cfg = BK5Cfg<Eng, Q, EB, F, LAYOUT>;
+    using S = typename Eng::S;
+    using V = typename Eng::V;
+    using A = typename Eng::A;
+    using WB = typename Cfg::WB;
+    constexpr int Q3 = Cfg::Q3;
+    extern __shared__ __align__(16) unsigned char smem[];
+    unsigned char* ustage = smem;
+    unsigned char* gstage = ustage + Cfg::U_BYTES;
+    V* W0 = reinterpret_cast<V*>(gstage + Cfg::G_BYTES);
+    V* W1 = W0 + EB * WB::size;
+    V* W2 = W1 + EB * WB::size;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(reinterpret_cast<unsigned char*>(W2 + EB * WB::size));
+    const int tid = threadIdx.x;
+    const int nt = Cfg::NT;
+    const Mat<typename Eng::C, Q, false> Dm{prm.D};   // D(i, n)
+    const Mat<typename Eng::C, Q, true> Dt{prm.D};    // D(n, i)
+
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    uint32_t phase = 0;
+    const long long nbatch = (E + EB - 1) / EB;
+    for (long long bt = blockIdx.x; bt < nbatch; bt += gridDim.x, phase ^= 1u) {
+        const long long e0 = bt * EB;
+        const int ne = int((E - e0) < EB ? (E - e0) : EB);
+        // 1. stage u and G of the batch
+        uint32_t tx = 0;
+        if (tid == 0) fence_proxy_async();
+        const S* us = stage_issue<S>(ustage, u + e0 * Q3, ne * Q3, bar, tx, tid, nt);
+        const S* gs = stage_issue<S>(gstage, G + e0 * F * Q3, ne * F * Q3, bar, tx, tid, nt);
+        if (tid == 0) mbar_arrive_expect_tx(bar, tx);
+        if (batch_wait_failed(bar, phase, ctx, tid)) return;
+        // 2. u -> W2 (working type, padded)
+        load_box<Eng, WB, Q, Q, Q>(us, Q3, W2, ne, tid, nt);
+        __syncthreads();
+        // 3. gradient: qr -> W0 (along i), qs -> W1 (along j); qt along k
+        //    in place into W2 after the other two have read it
+        sweep<Eng, WB, 0, Q, Q, Q, Q>(W2, W0, ne, Dm, tid, nt);
+        sweep<Eng, WB, 1, Q, Q, Q, Q>(W2, W1, ne, Dm, tid, nt);
+        __syncthreads();
+        sweep<Eng, WB, 2, Q, Q, Q, Q>(W2, W2, ne, Dm, tid, nt);
+        __syncthreads();
+        // 4. fluxes with the symmetric (F = 6) or full (F = 9) factors
+        for (int w = tid; w < ne * Q3; w += nt) {
+            const int e = w / Q3;
+            const int x = w - e * Q3;
+            int i, j, k;
+            if (LAYOUT == 2) {   // walk points in G's (k, i, j) order
+                k = x / (Q * Q);
+                i = (x / Q) % Q;
+                j = x % Q;
+            } else {
+                i = x / (Q * Q);
+                j = (x / Q) % Q;
+                k = x % Q;
+            }
+            const int wi = e * WB::size + WB::at(i, j, k);
+            const V qr = W0[wi], qs = W1[wi], qt = W2[wi];
+            const S* ge = gs + e * F * Q3;
+            auto g = [&](int f) { return Eng::load(ge[g_index<Eng, Q, F, LAYOUT>(i, j, f, k)]); };
+            A r0 = Eng::zero(), r1 = Eng::zero(), r2 = Eng::zero();
+            if (F == 6) {
+                const V g0 = g(0), g1 = g(1), g2 = g(2), g3 = g(3), g4 = g(4), g5 = g(5);
+                Eng::vmadd(r0, g0, qr); Eng::vmadd(r0, g1, qs); Eng::vmadd(r0, g2, qt);
+                Eng::vmadd(r1, g1, qr); Eng::vmadd(r1, g3, qs); Eng::vmadd(r1, g4, qt);
+                Eng::vmadd(r2, g2, qr); Eng::vmadd(r2, g4, qs); Eng::vmadd(r2, g5, qt);
+            } else {
+                Eng::vmadd(r0, g(0), qr); Eng::vmadd(r0, g(1), qs); Eng::vmadd(r0, g(2), qt);
+                Eng::vmadd(r1, g(3), qr); Eng::vmadd(r1, g(4), qs); Eng::vmadd(r1, g(5), qt);
+                Eng::vmadd(r2, g(6), qr); Eng::vmadd(r2, g(7), qs); Eng::vmadd(r2, g(8), qt);
+            }
+            W0[wi] = Eng::result(r0);
+            W1[wi] = Eng::result(r1);
+            W2[wi] = Eng::result(r2);
+        }
+        __syncthreads();
+        // 5. transposed derivatives: along i in place on W0, along j on W1
+        sweep<Eng, WB, 0, Q, Q, Q, Q>(W0, W0, ne, Dt, tid, nt);
+        sweep<Eng, WB, 1, Q, Q, Q, Q>(W1, W1, ne, Dt, tid, nt);
+        __syncthreads();
+        // 6. along k on W2, plus the other two terms (and the Helmholtz mass
+        //    term), written densely into the u staging area
+        S* vs = const_cast<S*>(us);
+        {
+            constexpr int L = Q * Q;
+            for (int w = tid; w < ne * L; w += nt) {
+                const int e = w / L;
+                const int l = w - e * L;
+                const int i = l / Q;
+                const int j = l - i * Q;
+                const int base = e * WB::size + WB::at(i, j, 0);
+                V x[Q];
+#pragma unroll
+                for (int n = 0; n < Q; ++n) x[n] = W2[base + n];
+#pragma unroll
+                for (int o = 0; o < Q; ++o) {
+                    A acc = Eng::zero();
+#pragma unroll
+                    for (int n = 0; n < Q; ++n) Eng::madd(acc, Dt(o, n), x[n]);
+                    V res;
+                    if constexpr (HasSum3<Eng>::value) {
+                        res = Eng::sum3(Eng::result(acc), W0[base + o], W1[base + o]);
+                    } else {
+                        Eng::add(acc, W0[base + o]);
+                        Eng::add(acc, W1[base + o]);
+                        res = Eng::result(acc);
+                    }
+                    const int xo = e * Q3 + (i * Q + j) * Q + o;
+                    S out = Eng::store(res);
+                    if (mass != nullptr) {
+                        // lambda * mass * u at the point, in the storage type's
+                        // arithmetic (double for the FP64 engines)
+                        out += S(lambda) * mass[(e0 + e) * Q3 + (i * Q + j) * Q + o] * us[xo];
+                    }
+                    vs[xo] = out;
+                }
+            }
+        }
+        __syncthreads();
+        store_out<S>(vs, v + e0 * Q3, ne * Q3, tid, nt);
+        __syncthreads();
+    }
+}
+
+// ---- BK1 -----------------------------------------------------------------------
+
+template <class Eng, int Q, int EB>
+struct BK1Cfg {
+    using S = typename Eng::S;
+    using V = typename Eng::V;
+    using WB = WBox<Q, V>;
+    static constexpr int P = Q - 1;
+    static constexpr int Q3 = Q * Q * Q;
+    static constexpr int P3 = P * P * P;
+    static constexpr int NT = ((EB * Q * Q + 31) / 32) * 32 < 64 ? 64 : ((EB * Q * Q + 31) / 32) * 32;
+    static constexpr int U_BYTES = stage_bytes<S>(EB * Q3);   // also holds the P^3 output
+    static constexpr int J_BYTES = stage_bytes<S>(EB * Q3);
+    static constexpr int W_BYTES = 2 * EB * WB::size * int(sizeof(V));
+    static constexpr int SMEM = U_BYTES + J_BYTES + W_BYTES + 16;
+};
+
+template <class Eng, int Q, int EB>
+__global__ void __launch_bounds__(BK1Cfg<Eng, Q, EB>::NT)
+    bk1_kernel(const __grid_constant__ P13<typename Eng::C, Q> prm, const long long E,
+               const typename Eng::S* __restrict__ u, const typename Eng::S* __restrict__ jxw,
+               typename Eng::S* __restrict__ v, const DevCtx ctx)
+{
+    using Cfg = BK1Cfg<Eng, Q, EB>;
+    using S = typename Eng::S;
+    using V = typename Eng::V;
+    using WB = typename Cfg::WB;
+    constexpr int P = Cfg::P, Q3 = Cfg::Q3, P3 = Cfg::P3;
+    extern __shared__ __align__(16) unsigned char smem[];
+    unsigned char* ustage = smem;
+    unsigned char* jstage = ustage + Cfg::U_BYTES;
+    V* W0 = reinterpret_cast<V*>(jstage + Cfg::J_BYTES);
+    V* W1 = W0 + EB * WB::size;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(reinterpret_cast<unsigned char*>(W1 + EB * WB::size));
+    const int tid = threadIdx.x;
+    const int nt = Cfg::NT;
+    // interpolation out(p) = sum_i in(i) B(i, p): M(o=p, n=i) = B[i*Q + p]
+    const Mat<typename Eng::C, Q, true> Bi{prm.B};
+    // back: out(i) = sum_p in(p) B(i, p): M(o=i, n=p) = B[i*Q + p]
+    const Mat<typename Eng::C, Q, false> Bb{prm.B};
+
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    uint32_t phase = 0;
+    const long long nbatch = (E + EB - 1) / EB;
+    for (long long bt = blockIdx.x; bt < nbatch; bt += gridDim.x, phase ^= 1u) {
+        const long long e0 = bt * EB;
+        const int ne = int((E - e0) < EB ? (E - e0) : EB);
+        uint32_t tx = 0;
+        if (tid == 0) fence_proxy_async();
+        const S* us = stage_issue<S>(ustage, u + e0 * P3, ne * P3, bar, tx, tid, nt);
+        const S* js = stage_issue<S>(jstage, jxw + e0 * Q3, ne * Q3, bar, tx, tid, nt);
+        if (tid == 0) mbar_arrive_expect_tx(bar, tx);
+        if (batch_wait_failed(bar, phase, ctx, tid)) return;
+        load_box<Eng, WB, P, P, P>(us, P3, W0, ne, tid, nt);
+        __syncthreads();
+        sweep<Eng, WB, 0, P, P, P, Q>(W0, W1, ne, Bi, tid, nt);   // (Q,P,P)
+        __syncthreads();
+        sweep<Eng, WB, 1, Q, P, P, Q>(W1, W0, ne, Bi, tid, nt);   // (Q,Q,P)
+        __syncthreads();
+        sweep<Eng, WB, 2, Q, Q, P, Q>(W0, W1, ne, Bi, tid, nt);   // (Q,Q,Q)
+        __syncthreads();
+        for (int w = tid; w < ne * Q3; w += nt) {
+            const int e = w / Q3;
+            const int x = w - e * Q3;
+            const int i = x / (Q * Q), j = (x / Q) % Q, k = x % Q;
+            const int wi = e * WB::size + WB::at(i, j, k);
+            W1[wi] = Eng::mul(W1[wi], Eng::load(js[e * Q3 + x]));
+        }
+        __syncthreads();
+        sweep<Eng, WB, 2, Q, Q, Q, P>(W1, W0, ne, Bb, tid, nt);   // (Q,Q,P)
+        __syncthreads();
+        sweep<Eng, WB, 1, Q, Q, P, P>(W0, W1, ne, Bb, tid, nt);   // (Q,P,P)
+        __syncthreads();
+        sweep<Eng, WB, 0, Q, P, P, P>(W1, W0, ne, Bb, tid, nt);   // (P,P,P)
+        __syncthreads();
+        S* vs = const_cast<S*>(us);
+        store_box<Eng, WB, P, P, P>(W0, vs, P3, ne, tid, nt);
+        __syncthreads();
+        store_out<S>(vs, v + e0 * P3, ne * P3, tid, nt);
+        __syncthreads();
+    }
+}
+
+// ---- BK3 -----------------------------------------------------------------------
+
+template <class Eng, int Q, int EB>
+struct BK3Cfg {
+    using S = typename Eng::S;
+    using V = typename Eng::V;
+    using WB = WBox<Q, V>;
+    static constexpr int P = Q - 1;
+    static constexpr int Q3 = Q * Q * Q;
+    static constexpr int P3 = P * P * P;
+    static constexpr int NT = ((EB * Q * Q + 31) / 32) * 32 < 64 ? 64 : ((EB * Q * Q + 31) / 32) * 32;
+    static constexpr int U_BYTES = stage_bytes<S>(EB * P3);
+    static constexpr int G_BYTES = stage_bytes<S>(EB * 6 * Q3);
+    static constexpr int K_BYTES = stage_bytes<S>(EB * Q3);
+    static constexpr int W_BYTES = 4 * EB * WB::size * int(sizeof(V));
+    static constexpr int SMEM = U_BYTES + G_BYTES + K_BYTES + W_BYTES + 16;
+};
+
+template <class Eng, int Q, int EB>
+__global__ void __launch_bounds__(BK3Cfg<Eng, Q, EB>::NT)
+    bk3_kernel(const __grid_constant__ P13<typename Eng::C, Q> prm, const long long E,
+               const typename Eng::S* __restrict__ u, const typename Eng::S* __restrict__ G,
+               const typename Eng::S* __restrict__ kq, typename Eng::S* __restrict__ v, const DevCtx ctx)
+{
+    using Cfg = BK3Cfg<Eng, Q, EB>;
+    using S = typename Eng::S;
+    using V = typename Eng::V;
+    using A = typename Eng::A;
+    using WB = typename Cfg::WB;
+    constexpr int P = Cfg::P, Q3 = Cfg::Q3, P3 = Cfg::P3;
+    extern __shared__ __align__(16) unsigned char smem[];
+    unsigned char* ustage = smem;
+    unsigned char* gstage = ustage + Cfg::U_BYTES;
+    unsigned char* kstage = gstage + Cfg::G_BYTES;
+    V* W0 = reinterpret_cast<V*>(kstage + Cfg::K_BYTES);
+    V* W1 = W0 + EB * WB::size;
+    V* W2 = W1 + EB * WB::size;
+    V* W3 = W2 + EB * WB::size;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(reinterpret_cast<unsigned char*>(W3 + EB * WB::size));
+    const int tid = threadIdx.x;
+    const int nt = Cfg::NT;
+    const Mat<typename Eng::C, Q, true> Bi{prm.B};    // M(p, i) = B[i*Q + p]
+    const Mat<typename Eng::C, Q, false> Bb{prm.B};   // M(i, p) = B[i*Q + p]
+    const Mat<typename Eng::C, Q, true> Dg{prm.D};    // q(p) = sum_n u(n) D(n, p)
+    const Mat<typename Eng::C, Q, false> Dtr{prm.D};  // sum_n f(n) D(p, n)
+
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    uint32_t phase = 0;
+    const long long nbatch = (E + EB - 1) / EB;
+    for (long long bt = blockIdx.x; bt < nbatch; bt += gridDim.x, phase ^= 1u) {
+        const long long e0 = bt * EB;
+        const int ne = int((E - e0) < EB ? (E - e0) : EB);
+        uint32_t tx = 0;
+        if (tid == 0) fence_proxy_async();
+        const S* us = stage_issue<S>(ustage, u + e0 * P3, ne * P3, bar, tx, tid, nt);
+        const S* gs = stage_issue<S>(gstage, G + e0 * 6 * Q3, ne * 6 * Q3, bar, tx, tid, nt);
+        const S* ks = (kq != nullptr) ? stage_issue<S>(kstage, kq + e0 * Q3, ne * Q3, bar, tx, tid, nt) : nullptr;
+        if (tid == 0) mbar_arrive_expect_tx(bar, tx);
+        if (batch_wait_failed(bar, phase, ctx, tid)) return;
+        load_box<Eng, WB, P, P, P>(us, P3, W0, ne, tid, nt);
+        __syncthreads();
+        sweep<Eng, WB, 0, P, P, P, Q>(W0, W1, ne, Bi, tid, nt);   // (Q,P,P)
+        __syncthreads();
+        sweep<Eng, WB, 1, Q, P, P, Q>(W1, W0, ne, Bi, tid, nt);   // (Q,Q,P)
+        __syncthreads();
+        sweep<Eng, WB, 2, Q, Q, P, Q>(W0, W2, ne, Bi, tid, nt);   // u at the points: W2
+        __syncthreads();
+        sweep<Eng, WB, 0, Q, Q, Q, Q>(W2, W0, ne, Dg, tid, nt);   // qr
+        sweep<Eng, WB, 1, Q, Q, Q, Q>(W2, W1, ne, Dg, tid, nt);   // qs
+        sweep<Eng, WB, 2, Q, Q, Q, Q>(W2, W3, ne, Dg, tid, nt);   // qt
+        __syncthreads();
+        for (int w = tid; w < ne * Q3; w += nt) {
+            const int e = w / Q3;
+            const int x = w - e * Q3;
+            const int i = x / (Q * Q), j = (x / Q) % Q, k = x % Q;
+            const int wi = e * WB::size + WB::at(i, j, k);
+            V qr = W0[wi], qs = W1[wi], qt = W3[wi];
+            if (ks != nullptr) {
+                const V kk = Eng::load(ks[e * Q3 + x]);
+                qr = Eng::mul(kk, qr);
+                qs = Eng::mul(kk, qs);
+                qt = Eng::mul(kk, qt);
+            }
+            const S* ge = gs + e * 6 * Q3 + x;   // factor-major
+            const V g0 = Eng::load(ge[0]), g1 = Eng::load(ge[Q3]), g2 = Eng::load(ge[2 * Q3]);
+            const V g3 = Eng::load(ge[3 * Q3]), g4 = Eng::load(ge[4 * Q3]), g5 = Eng::load(ge[5 * Q3]);
+            A r0 = Eng::zero(), r1 = Eng::zero(), r2 = Eng::zero();
+            Eng::vmadd(r0, g0, qr); Eng::vmadd(r0, g1, qs); Eng::vmadd(r0, g2, qt);
+            Eng::vmadd(r1, g1, qr); Eng::vmadd(r1, g3, qs); Eng::vmadd(r1, g4, qt);
+            Eng::vmadd(r2, g2, qr); Eng::vmadd(r2, g4, qs); Eng::vmadd(r2, g5, qt);
+            W0[wi] = Eng::result(r0);
+            W1[wi] = Eng::result(r1);
+            W3[wi] = Eng::result(r2);
+        }
+        __syncthreads();
+        sweep<Eng, WB, 0, Q, Q, Q, Q>(W0, W0, ne, Dtr, tid, nt);
+        sweep<Eng, WB, 1, Q, Q, Q, Q>(W1, W1, ne, Dtr, tid, nt);
+        __syncthreads();
+        // along r on W3, plus the two other terms -> W2
+        {
+            constexpr int L = Q * Q;
+            for (int w = tid; w < ne * L; w += nt) {
+                const int e = w / L;
+                const int l = w - e * L;
+                const int i = l / Q;
+                const int j = l - i * Q;
+                const int base = e * WB::size + WB::at(i, j, 0);
+                V x[Q];
+#pragma unroll
+                for (int n = 0; n < Q; ++n) x[n] = W3[base + n];
+#pragma unroll
+                for (int o = 0; o < Q; ++o) {
+                    A acc = Eng::zero();
+#pragma unroll
+                    for (int n = 0; n < Q; ++n) Eng::madd(acc, Dtr(o, n), x[n]);
+                    if constexpr (HasSum3<Eng>::value) {
+                        W2[base + o] = Eng::sum3(Eng::result(acc), W0[base + o], W1[base + o]);
+                    } else {
+                        Eng::add(acc, W0[base + o]);
+                        Eng::add(acc, W1[base + o]);
+                        W2[base + o] = Eng::result(acc);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        sweep<Eng, WB, 2, Q, Q, Q, P>(W2, W0, ne, Bb, tid, nt);   // (Q,Q,P)
+        __syncthreads();
+        sweep<Eng, WB, 1, Q, Q, P, P>(W0, W1, ne, Bb, tid, nt);   // (Q,P,P)
+        __syncthreads();
+        sweep<Eng, WB, 0, Q, P, P, P>(W1, W0, ne, Bb, tid, nt);   // (P,P,P)
+        __syncthreads();
+        S* vs = const_cast<S*>(us);
+        store_box<Eng, WB, P, P, P>(W0, vs, P3, ne, tid, nt);
+        __syncthreads();
+        store_out<S>(vs, v + e0 * P3, ne * P3, tid, nt);
+        __syncthreads();
+    }
+}
+
+}  // namespace bkg

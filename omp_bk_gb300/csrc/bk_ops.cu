@@ -1,0 +1,187 @@
+// bk_ops.cu -- launchers of the BK1 / BK3 / BK5 kernels for ONE arithmetic
+// engine, chosen at compile time by BK_ENGINE_TU (0 dfma, 1 float-float,
+// 2 fp32, 3 mixed): the build compiles this file once per engine so that the
+// translation units build in parallel.  Run-time order p -> compile-time Q
+// (the role of bk::with_order, include/bk_common.h:148-178).
+#include <cuda_runtime.h>
+
+#include "bk_internal.h"
+#include "bk_kernels.cuh"
+
+#ifndef BK_ENGINE_TU
+#error "BK_ENGINE_TU must be 0 (dfma), 1 (ff), 2 (fp32) or 3 (mixed)"
+#endif
+
+namespace bkg {
+
+#if BK_ENGINE_TU == 0
+using Eng = EngDfma;
+#define BK_SFX dfma
+#elif BK_ENGINE_TU == 1
+using Eng = EngFF;
+#define BK_SFX ff
+#elif BK_ENGINE_TU == 2
+using Eng = EngF32;
+#define BK_SFX f32
+#else
+using Eng = EngMixed;
+#define BK_SFX mixed
+#endif
+
+#define BK_CAT2(a, b) a##_##b
+#define BK_CAT(a, b) BK_CAT2(a, b)
+
+namespace {
+
+// Elements per block: about 128 lines per sweep (Q^2 lines per element).
+constexpr int default_eb(int q) { return (q * q >= 100) ? 1 : ((q * q >= 64) ? 2 : (128 + q * q - 1) / (q * q)); }
+
+// Sets the dynamic shared-memory size of a kernel on the current device once
+// and returns its resident blocks per SM (0 if it cannot run).
+template <class K>
+int prepare(K kern, int smem, int nt)
+{
+    static int occ[kMaxDevices] = {0};
+    const int dev = current_device();
+    if (dev < 0 || dev >= kMaxDevices) return 0;
+    if (occ[dev] == 0) {
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess) return 0;
+        int n = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, nt, smem) != cudaSuccess) return 0;
+        occ[dev] = n;
+    }
+    return occ[dev];
+}
+
+int grid_for(long long nbatch, int occ)
+{
+    const long long cap = static_cast<long long>(occ) * sm_count();
+    return static_cast<int>(nbatch < cap ? nbatch : cap);
+}
+
+template <int Q, int EB, int F, int LAYOUT>
+int bk5_q(const double* D, long long E, const void* u, const void* G, const void* mass, double lambda, void* v,
+          cudaStream_t s)
+{
+    using Cfg = BK5Cfg<Eng, Q, EB, F, LAYOUT>;
+    using S = typename Eng::S;
+    static_assert(Cfg::SMEM <= 232448, "BK5 block exceeds the shared memory of an SM");
+    P5<typename Eng::C, Q> prm;
+    for (int i = 0; i < Q * Q; ++i) prm.D[i] = Eng::coef(D[i]);
+    auto kern = bk5_kernel<Eng, Q, EB, F, LAYOUT>;
+    const int occ = prepare(kern, Cfg::SMEM, Cfg::NT);
+    if (occ <= 0) return BK_ERR_CUDA;
+    const int grid = grid_for((E + EB - 1) / EB, occ);
+    kern<<<grid, Cfg::NT, Cfg::SMEM, s>>>(prm, E, static_cast<const S*>(u), static_cast<const S*>(G),
+                                          static_cast<const S*>(mass), lambda, static_cast<S*>(v), dev_ctx());
+    return cudaGetLastError() == cudaSuccess ? BK_OK : BK_ERR_CUDA;
+}
+
+template <int Q>
+int bk5_fl(int F, int layout, int eb, const double* D, long long E, const void* u, const void* G, const void* mass,
+           double lambda, void* v, cudaStream_t s)
+{
+    constexpr int EB = default_eb(Q);
+    (void)eb;
+#define BK5_CASE(FF, LL)                                                            \
+    if (F == FF && layout == LL) return bk5_q<Q, EB, FF, LL>(D, E, u, G, mass, lambda, v, s);
+    BK5_CASE(6, 1)
+    BK5_CASE(6, 0)
+    BK5_CASE(6, 2)
+    BK5_CASE(9, 1)
+    BK5_CASE(9, 0)
+    BK5_CASE(9, 2)
+#undef BK5_CASE
+    return BK_ERR_PREC;
+}
+
+template <int Q, int EB>
+int bk1_q(const double* B, long long E, const void* jxw, const void* u, void* v, cudaStream_t s)
+{
+    using Cfg = BK1Cfg<Eng, Q, EB>;
+    using S = typename Eng::S;
+    static_assert(Cfg::SMEM <= 232448, "BK1 block exceeds the shared memory of an SM");
+    P13<typename Eng::C, Q> prm;
+    for (int i = 0; i < (Q - 1) * Q; ++i) prm.B[i] = Eng::coef(B[i]);
+    for (int i = 0; i < Q * Q; ++i) prm.D[i] = Eng::coef(0.0);
+    auto kern = bk1_kernel<Eng, Q, EB>;
+    const int occ = prepare(kern, Cfg::SMEM, Cfg::NT);
+    if (occ <= 0) return BK_ERR_CUDA;
+    const int grid = grid_for((E + EB - 1) / EB, occ);
+    kern<<<grid, Cfg::NT, Cfg::SMEM, s>>>(prm, E, static_cast<const S*>(u), static_cast<const S*>(jxw),
+                                          static_cast<S*>(v), dev_ctx());
+    return cudaGetLastError() == cudaSuccess ? BK_OK : BK_ERR_CUDA;
+}
+
+template <int Q, int EB>
+int bk3_q(const double* B, const double* D, long long E, const void* G, const void* k, const void* u, void* v,
+          cudaStream_t s)
+{
+    using Cfg = BK3Cfg<Eng, Q, EB>;
+    using S = typename Eng::S;
+    static_assert(Cfg::SMEM <= 232448, "BK3 block exceeds the shared memory of an SM");
+    P13<typename Eng::C, Q> prm;
+    for (int i = 0; i < (Q - 1) * Q; ++i) prm.B[i] = Eng::coef(B[i]);
+    for (int i = 0; i < Q * Q; ++i) prm.D[i] = Eng::coef(D[i]);
+    auto kern = bk3_kernel<Eng, Q, EB>;
+    const int occ = prepare(kern, Cfg::SMEM, Cfg::NT);
+    if (occ <= 0) return BK_ERR_CUDA;
+    const int grid = grid_for((E + EB - 1) / EB, occ);
+    kern<<<grid, Cfg::NT, Cfg::SMEM, s>>>(prm, E, static_cast<const S*>(u), static_cast<const S*>(G),
+                                          static_cast<const S*>(k), static_cast<S*>(v), dev_ctx());
+    return cudaGetLastError() == cudaSuccess ? BK_OK : BK_ERR_CUDA;
+}
+
+}  // namespace
+
+int BK_CAT(launch_bk5, BK_SFX)(int p, long long E, const double* D, const void* G, const void* u, const void* mass,
+                                double lambda, void* v, int F, int layout, int eb, cudaStream_t s)
+{
+    switch (p + 1) {
+        case 2: return bk5_fl<2>(F, layout, eb, D, E, u, G, mass, lambda, v, s);
+        case 3: return bk5_fl<3>(F, layout, eb, D, E, u, G, mass, lambda, v, s);
+        case 4: return bk5_fl<4>(F, layout, eb, D, E, u, G, mass, lambda, v, s);
+        case 5: return bk5_fl<5>(F, layout, eb, D, E, u, G, mass, lambda, v, s);
+        case 6: return bk5_fl<6>(F, layout, eb, D, E, u, G, mass, lambda, v, s);
+        case 7: return bk5_fl<7>(F, layout, eb, D, E, u, G, mass, lambda, v, s);
+        case 8: return bk5_fl<8>(F, layout, eb, D, E, u, G, mass, lambda, v, s);
+        case 9: return bk5_fl<9>(F, layout, eb, D, E, u, G, mass, lambda, v, s);
+        default: return BK_ERR_ORDER;
+    }
+}
+
+int BK_CAT(launch_bk1, BK_SFX)(int p, long long E, const double* B, const void* jxw, const void* u, void* v,
+                                int eb, cudaStream_t s)
+{
+    (void)eb;
+    switch (p + 2) {
+        case 3: return bk1_q<3, default_eb(3)>(B, E, jxw, u, v, s);
+        case 4: return bk1_q<4, default_eb(4)>(B, E, jxw, u, v, s);
+        case 5: return bk1_q<5, default_eb(5)>(B, E, jxw, u, v, s);
+        case 6: return bk1_q<6, default_eb(6)>(B, E, jxw, u, v, s);
+        case 7: return bk1_q<7, default_eb(7)>(B, E, jxw, u, v, s);
+        case 8: return bk1_q<8, default_eb(8)>(B, E, jxw, u, v, s);
+        case 9: return bk1_q<9, default_eb(9)>(B, E, jxw, u, v, s);
+        case 10: return bk1_q<10, default_eb(10)>(B, E, jxw, u, v, s);
+        default: return BK_ERR_ORDER;
+    }
+}
+
+int BK_CAT(launch_bk3, BK_SFX)(int p, long long E, const double* B, const double* D, const void* G, const void* k,
+                                const void* u, void* v, int eb, cudaStream_t s)
+{
+    (void)eb;
+    switch (p + 2) {
+        case 3: return bk3_q<3, default_eb(3)>(B, D, E, G, k, u, v, s);
+        case 4: return bk3_q<4, default_eb(4)>(B, D, E, G, k, u, v, s);
+        case 5: return bk3_q<5, default_eb(5)>(B, D, E, G, k, u, v, s);
+        case 6: return bk3_q<6, default_eb(6)>(B, D, E, G, k, u, v, s);
+        case 7: return bk3_q<7, default_eb(7)>(B, D, E, G, k, u, v, s);
+        case 8: return bk3_q<8, default_eb(8)>(B, D, E, G, k, u, v, s);
+        case 9: return bk3_q<9, default_eb(9)>(B, D, E, G, k, u, v, s);
+        case 10: return bk3_q<10, default_eb(10)>(B, D, E, G, k, u, v, s);
+        default: return BK_ERR_ORDER;
+    }
+}
+
+}  // namespace bkg

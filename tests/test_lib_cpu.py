@@ -1,0 +1,115 @@
+"""CPU-only checks of the CUDA library: it loads, exports every function the
+C headers declare, rejects bad arguments on the host (before any CUDA call),
+and its 1-D rules and matrices satisfy the identities that pin them (the
+reference has no such generators)."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    names = set()
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if not h.endswith(".h"):
+            continue
+        src = open(os.path.join(ROOT, "include", h)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        names |= set(re.findall(r"^\s*(?:int|bk_options|const char\*)\s+(bk\w+)\s*\(", src, flags=re.M))
+    return names
+
+
+def test_exports_every_declared_symbol(bklib):
+    declared = _declared()
+    assert len(declared) >= 20
+    assert declared == set(bklib.EXPORTS), declared ^ set(bklib.EXPORTS)
+    for name in declared:
+        assert hasattr(bklib.lib(), name), name
+
+
+def test_version_and_defaults(bklib):
+    assert "sm_103a" in bklib.version()
+    o = bklib.lib().bk_default_options()
+    assert (o.prec, o.engine, o.layout, o.nfactors, o.elems_per_block) == (0, 0, 1, 6, 0)
+
+
+def test_host_argument_errors(bklib):
+    """with_order's 'unsupported polynomial order' and the other argument
+    errors come back as status codes without a GPU."""
+    L = bklib.lib()
+    D = (C.c_double * 100)()
+    dp = C.cast(D, C.POINTER(C.c_double))
+    a16 = C.c_void_p(0x10000)
+    a8 = C.c_void_p(0x10008)
+    # order outside 1..8
+    for p in (0, 9, -1):
+        assert L.bk5_apply(p, 4, dp, a16, a16, a16, 0, None) == bklib.BK_ERR_ORDER
+        assert L.bk1_apply(p, 4, dp, a16, a16, a16, 0, None) == bklib.BK_ERR_ORDER
+        assert L.bk3_apply(p, 4, dp, dp, a16, a16, a16, 0, None) == bklib.BK_ERR_ORDER
+    assert L.bk5_apply(3, -1, dp, a16, a16, a16, 0, None) == bklib.BK_ERR_SIZE
+    assert L.bk5_apply(3, 4, dp, None, a16, a16, 0, None) == bklib.BK_ERR_NULL
+    assert L.bk5_apply(3, 4, None, a16, a16, a16, 0, None) == bklib.BK_ERR_NULL
+    assert L.bk5_apply(3, 4, dp, a8, a16, a16, 0, None) == bklib.BK_ERR_ALIGN
+    assert L.bk1_apply(3, 4, dp, a16, a8, a16, 0, None) == bklib.BK_ERR_ALIGN
+    assert L.bk3_apply(3, 4, dp, dp, a16, a16, a8, 0, None) == bklib.BK_ERR_ALIGN
+    assert L.bk5_apply(3, 4, dp, a16, a16, a16, 7, None) == bklib.BK_ERR_PREC
+    o = bklib.ApplyOptions(nfactors=7).c()
+    assert L.bk5_apply_opt(3, 4, dp, a16, a16, a16, C.byref(o), None) == bklib.BK_ERR_PREC
+    o = bklib.ApplyOptions(layout=3).c()
+    assert L.bk5_apply_opt(3, 4, dp, a16, a16, a16, C.byref(o), None) == bklib.BK_ERR_PREC
+    o = bklib.ApplyOptions(engine=9).c()
+    assert L.bk5_apply_opt(3, 4, dp, a16, a16, a16, C.byref(o), None) == bklib.BK_ERR_PREC
+    # E = 0 is a no-op, even with null device pointers
+    assert L.bk5_apply(3, 0, dp, None, None, None, 0, None) == bklib.BK_OK
+    assert L.bk1_apply(8, 0, dp, None, None, None, 0, None) == bklib.BK_OK
+
+
+def test_python_error_message(bklib):
+    with pytest.raises(bklib.BKError, match="unsupported polynomial order p"):
+        bklib.bk5_apply(9, 0, np.zeros(100), None, None, None)
+
+
+@pytest.mark.parametrize("n", range(1, 12))
+def test_gauss_rule(bklib, n):
+    x, w = bklib.gauss(n)
+    xr, wr = np.polynomial.legendre.leggauss(n)
+    assert np.allclose(x, xr, atol=1e-15, rtol=0)
+    assert np.allclose(w, wr, atol=1e-15, rtol=0)
+
+
+@pytest.mark.parametrize("n", range(2, 12))
+def test_gll_rule(bklib, n):
+    x, w = bklib.gll(n)
+    assert x[0] == -1.0 and x[-1] == 1.0
+    assert np.all(np.diff(x) > 0)
+    assert abs(w.sum() - 2.0) < 1e-14
+    # interior points are the roots of P_{n-1}'
+    dP = np.polynomial.legendre.Legendre.basis(n - 1).deriv()
+    if n > 2:
+        assert np.max(np.abs(dP(x[1:-1]))) < 1e-12 * max(1.0, np.max(np.abs(dP.coef)))
+    # exact for polynomials of degree 2n - 3
+    for deg in range(2 * n - 2):
+        exact = 0.0 if deg % 2 else 2.0 / (deg + 1)
+        assert abs(w @ x ** deg - exact) < 1e-13
+
+
+@pytest.mark.parametrize("p", range(1, 9))
+def test_interp_and_deriv_identities(bklib, p):
+    B, D3, xq, wq, xn = bklib.bk1_bk3_matrices(p)
+    P, Q = p + 1, p + 2
+    B = B.reshape(P, Q)
+    assert np.allclose(B.sum(axis=0), 1.0, atol=1e-13)        # B^T 1 = 1
+    assert np.allclose(xn @ B, xq, atol=1e-13)                 # interpolates x exactly
+    D3 = D3.reshape(Q, Q)                                      # D(n, q) = l_n'(x_q)
+    assert np.allclose(D3.sum(axis=0), 0.0, atol=1e-12)        # derivative of 1
+    assert np.allclose(xq @ D3, 1.0, atol=1e-12)               # derivative of x
+    D5, x, w = bklib.bk5_matrices(p)
+    D5 = D5.reshape(p + 1, p + 1)                              # D(i, n) = l_n'(x_i)
+    assert np.allclose(D5.sum(axis=1), 0.0, atol=1e-12)
+    assert np.allclose(D5 @ x, 1.0, atol=1e-12)
+    if p >= 2:
+        assert np.allclose(D5 @ x ** 2, 2 * x, atol=1e-11)

@@ -1,0 +1,190 @@
+"""Parity of the CUDA kernels with the oracle (the reference's algorithm
+restated in C, pinned to the reference's own kernels) and with the golden
+vectors of the reference itself.
+
+Tolerances (largest |out - ref| over the largest |ref|, the reference's
+rel_maxdiff, include/bk_harness.h:74-83):
+  FP64 engines (DFMA, float-float)     1e-12  (the target of the work)
+  FP32 storage (FP32, MIXED)           1e-5   (the reference's fail_mark)
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from gpu_util import dev, gpu_apply, host, oracle_apply, random_case, sizes
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+TOL32 = 1e-5
+P_ALL = list(range(1, 9))
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _cuda(bklib):
+    assert torch.cuda.is_available(), "the GPU tests need CUDA: the product has no CPU path"
+    bklib.device_status(reset=True)
+    yield
+    assert bklib.device_status(reset=True) == bklib.BK_OK
+
+
+@pytest.mark.parametrize("bk", [1, 3, 5])
+@pytest.mark.parametrize("p", P_ALL)
+@pytest.mark.parametrize("engine", ["dfma", "ff"])
+def test_fp64_random(bklib, bk, p, engine):
+    E = 13
+    nq, basis, dbasis, g, u = random_case(bk, p, E)
+    eng = bklib.ENGINE_DFMA if engine == "dfma" else bklib.ENGINE_FF
+    out = gpu_apply(bklib, bk, p, E, basis, dbasis, g, u, bklib.PREC_FP64, engine=eng)
+    ref = oracle_apply(bk, nq, E, basis, dbasis, g, u)
+    assert np.all(np.isfinite(out))
+    assert oracle.rel_maxdiff(out, ref) < TOL64
+
+
+@pytest.mark.parametrize("bk", [1, 3, 5])
+@pytest.mark.parametrize("p", P_ALL)
+@pytest.mark.parametrize("prec", ["fp32", "mixed"])
+def test_fp32_random(bklib, bk, p, prec):
+    E = 13
+    nq, basis, dbasis, g, u = random_case(bk, p, E)
+    pr = bklib.PREC_FP32 if prec == "fp32" else bklib.PREC_MIXED
+    out = gpu_apply(bklib, bk, p, E, basis, dbasis, g, u, pr)
+    # the FP32 kernels read the inputs rounded to float
+    ref = oracle_apply(bk, nq, E, basis, dbasis, g.astype(np.float32), u.astype(np.float32))
+    assert np.all(np.isfinite(out))
+    assert oracle.rel_maxdiff(out, ref) < TOL32
+
+
+@pytest.mark.parametrize("bk", [1, 3, 5])
+@pytest.mark.parametrize("p", P_ALL)
+def test_golden_vectors(bklib, golden, bk, p):
+    """Against the reference's own SumFactorization<double, nq> outputs."""
+    arr, meta = golden
+    E = meta["E_rand"]
+    nq, basis, dbasis, g, u = random_case(bk, p, E, meta["seed"])
+    out = gpu_apply(bklib, bk, p, E, basis, dbasis, g, u, bklib.PREC_FP64)
+    assert oracle.rel_maxdiff(out, arr[f"bk{bk}_p{p}_rand_f64"]) < TOL64
+
+
+@pytest.mark.parametrize("bk", [1, 3, 5])
+@pytest.mark.parametrize("p", P_ALL)
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_constant_data_norm(bklib, golden, bk, p, prec):
+    """The drivers' known answer: "norm =" on constant data (in = 3, JxW = 1,
+    G = 2, cos basis) as printed by the reference's BK1/BK3/BK5."""
+    arr, meta = golden
+    E = meta["E_const"]
+    nq, nm, ngeo = sizes(bk, p)
+    dt = np.float32 if prec == "f32" else np.float64
+    u = np.full(E * nm ** 3, 3.0)
+    g = np.full(E * ngeo, 1.0 if bk == 1 else 2.0)
+    basis = oracle.test_basis(nm, nq, dt).astype(np.float64) if bk != 5 else None
+    dbasis = oracle.test_basis(nq, nq, dt).astype(np.float64) if bk != 1 else None
+    pr = bklib.PREC_FP32 if prec == "f32" else bklib.PREC_FP64
+    out = gpu_apply(bklib, bk, p, E, basis, dbasis, g, u, pr)
+    ref = meta["norms"][f"bk{bk}_p{p}_const_{prec}"]
+    nrm = float(np.sqrt(np.sum(out * out)))
+    assert abs(nrm - ref) <= (2e-5 if prec == "f32" else 1e-12) * abs(ref)
+    e0 = arr[f"bk{bk}_p{p}_const_{prec}_e0"]
+    assert oracle.rel_maxdiff(out[: e0.size], e0) < (TOL32 if prec == "f32" else TOL64)
+
+
+@pytest.mark.parametrize("E", [1, 2, 3, 5, 16, 33, 100])
+@pytest.mark.parametrize("bk,p", [(1, 3), (3, 6), (5, 7), (5, 8), (3, 8)])
+def test_element_counts(bklib, bk, p, E):
+    """Any element count: partial last batches, batches whose slices start off
+    a 16-byte boundary (the TMA head/tail path)."""
+    nq, basis, dbasis, g, u = random_case(bk, p, E, seed=E)
+    for prec, tol in ((bklib.PREC_FP64, TOL64), (bklib.PREC_FP32, TOL32)):
+        out = gpu_apply(bklib, bk, p, E, basis, dbasis, g, u, prec)
+        if prec == bklib.PREC_FP32:
+            ref = oracle_apply(bk, nq, E, basis, dbasis, g.astype(np.float32), u.astype(np.float32))
+        else:
+            ref = oracle_apply(bk, nq, E, basis, dbasis, g, u)
+        assert oracle.rel_maxdiff(out, ref) < tol
+
+
+@pytest.mark.parametrize("p", [1, 4, 7, 8])
+@pytest.mark.parametrize("nfactors", [6, 9])
+@pytest.mark.parametrize("layout", [0, 1, 2])
+@pytest.mark.parametrize("engine", ["dfma", "ff"])
+def test_bk5_layouts(bklib, p, nfactors, layout, engine):
+    """BK5 with G in every layout and factor count of make_bk5_G
+    (include/bk_harness.h:217-244)."""
+    E = 7
+    nq, _, dbasis, g6i, u = random_case(5, p, E)
+    G = oracle.make_bk5_G(g6i, E, nq, nfactors, layout)
+    eng = bklib.ENGINE_DFMA if engine == "dfma" else bklib.ENGINE_FF
+    gu, gg = dev(u, "f64"), dev(G, "f64")
+    out = torch.full_like(gu, float("nan"))
+    bklib.bk5_apply(p, E, dbasis, gg, gu, out, engine=eng, layout=layout, nfactors=nfactors)
+    torch.cuda.synchronize()
+    ref = oracle.bk5(nq, E, dbasis, g6i, u)
+    assert oracle.rel_maxdiff(host(out), ref) < TOL64
+
+
+@pytest.mark.parametrize("p", [2, 5, 8])
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_bk5_helmholtz_mass(bklib, p, prec):
+    E = 9
+    nq, _, dbasis, g, u = random_case(5, p, E)
+    mass = np.random.default_rng(p).uniform(0.5, 1.5, E * nq ** 3)
+    pr = bklib.PREC_FP64 if prec == "fp64" else bklib.PREC_MIXED
+    out = gpu_apply(bklib, 5, p, E, None, dbasis, g, u, pr, mass=mass, lam=1.0)
+    if pr == bklib.PREC_FP64:
+        ref = oracle.bk5(nq, E, dbasis, g, u, mass=mass, lam=1.0)
+        tol = TOL64
+    else:
+        f = lambda a: a.astype(np.float32).astype(np.float64)
+        ref = oracle.bk5(nq, E, dbasis, f(g), f(u), mass=f(mass), lam=1.0)
+        tol = TOL32
+    assert oracle.rel_maxdiff(out, ref) < tol
+
+
+@pytest.mark.parametrize("p", [1, 4, 6, 8])
+@pytest.mark.parametrize("engine", ["dfma", "ff"])
+def test_bk3_coefficient(bklib, p, engine):
+    E = 5
+    nq, basis, dbasis, g, u = random_case(3, p, E)
+    k = np.exp(np.random.default_rng(p).normal(0, 0.5, E * nq ** 3))
+    eng = bklib.ENGINE_DFMA if engine == "dfma" else bklib.ENGINE_FF
+    out = gpu_apply(bklib, 3, p, E, basis, dbasis, g, u, bklib.PREC_FP64, engine=eng, k=k)
+    ref = oracle.bk3(nq, E, basis, dbasis, g, u, k=k)
+    assert oracle.rel_maxdiff(out, ref) < TOL64
+
+
+def test_offset_views(bklib):
+    """Arrays that start inside an allocation (16-byte aligned views)."""
+    p, E = 7, 6
+    nq, _, dbasis, g, u = random_case(5, p, E)
+    big_u = dev(np.concatenate([np.zeros(2), u]), "f64")[2:]
+    big_g = dev(np.concatenate([np.zeros(2), g]), "f64")[2:]
+    out = torch.full((E * nq ** 3 + 2,), float("nan"), dtype=torch.float64, device="cuda")[2:]
+    bklib.bk5_apply(p, E, dbasis, big_g, big_u, out)
+    torch.cuda.synchronize()
+    assert oracle.rel_maxdiff(host(out), oracle.bk5(nq, E, dbasis, g, u)) < TOL64
+    # a view one double in is not 16-byte aligned: rejected before any launch
+    with pytest.raises(bklib.BKError, match="misaligned"):
+        bklib.bk5_apply(p, E - 1, dbasis, big_g, big_u[1:], out)
+
+
+def test_bounded_wait_timeout(bklib):
+    """A device-side wait that nothing completes gives up within its limit,
+    records BK_ERR_TIMEOUT, and the context stays usable."""
+    L = bklib.lib()
+    assert bklib.device_status(reset=True) == bklib.BK_OK
+    assert L.bk_set_wait_limit(20000) == 0
+    try:
+        s = torch.cuda.current_stream().cuda_stream
+        assert L.bk_test_wait_timeout(s) == 0
+        torch.cuda.synchronize()
+        assert bklib.device_status(reset=True) == bklib.BK_ERR_TIMEOUT
+    finally:
+        assert L.bk_set_wait_limit(0) == 0
+    # the next apply runs normally
+    p, E = 3, 4
+    nq, _, dbasis, g, u = random_case(5, p, E)
+    out = gpu_apply(bklib, 5, p, E, None, dbasis, g, u, bklib.PREC_FP64)
+    assert oracle.rel_maxdiff(out, oracle.bk5(nq, E, dbasis, g, u)) < TOL64
+    assert bklib.device_status(reset=True) == bklib.BK_OK
