@@ -58,6 +58,10 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--elements", type=int, default=E_FULL, help="override E (profiling a smaller case)")
     ap.add_argument("--engine", default="ff", choices=["ff", "dfma"])
+    ap.add_argument("--prec", default="fp64", choices=["fp64", "mixed", "fp32"],
+                    help="form timed in the main loop (profiling; the headline is fp64)")
+    ap.add_argument("--kernel", default="auto", choices=["auto", "sweep", "column"])
+    ap.add_argument("--layout", type=int, default=1, help="G layout (0 factor, 1 interleaved, 2 column)")
     ap.add_argument("--no-forms", action="store_true", help="skip the side-by-side forms")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-e2e", action="store_true")
@@ -153,7 +157,7 @@ class ClockSampler:
 
 # ---- workload -----------------------------------------------------------------------
 
-def make_inputs(bk, E, torch):
+def make_inputs(bk, E, torch, layout=1):
     """Device inputs of the headline workload (FP64), built on the GPU."""
     D, x, w = bk.bk5_matrices(P_ORDER)
     Q = P_ORDER + 1
@@ -161,7 +165,7 @@ def make_inputs(bk, E, torch):
     u = torch.empty(n, dtype=torch.float64, device="cuda")
     G = torch.empty(6 * n, dtype=torch.float64, device="cuda")
     bk.fill_uniform(u, SEED_U, -1.0, 1.0)
-    bk.geom_trilinear(Q, E, NX, NX, x, w, SEED_G, H, JITTER, G=G, layout=bk.LAYOUT_INTERLEAVED)
+    bk.geom_trilinear(Q, E, NX, NX, x, w, SEED_G, H, JITTER, G=G, layout=layout)
     torch.cuda.synchronize()
     return D, u, G
 
@@ -257,29 +261,36 @@ def main():
     E = args.elements
     Q = P_ORDER + 1
     dofs = E * Q ** 3
-    D, u, G = make_inputs(bk, E, torch)
+    D, u, G = make_inputs(bk, E, torch, args.layout)
     v = torch.empty_like(u)
     engine = bk.ENGINE_FF if args.engine == "ff" else bk.ENGINE_DFMA
+    kernel = {"auto": bk.KERNEL_AUTO, "sweep": bk.KERNEL_SWEEP, "column": bk.KERNEL_COLUMN}[args.kernel]
+    prec = {"fp64": bk.PREC_FP64, "mixed": bk.PREC_MIXED, "fp32": bk.PREC_FP32}[args.prec]
+    if prec != bk.PREC_FP64:
+        u, G = u.float(), G.float()
+        v = torch.empty_like(u)
+    kw = dict(engine=engine, layout=args.layout, kernel=kernel, stream=stream)
 
     def apply():
-        bk.bk5_apply(P_ORDER, E, D, G, u, v, prec=bk.PREC_FP64, engine=engine, stream=stream)
+        bk.bk5_apply(P_ORDER, E, D, G, u, v, prec=prec, **kw)
 
     steps, warmup = args.steps, max(args.warmup, 3)
     with ClockSampler(local) as clk:
         t = time_loop(apply, steps, warmup, world, stream, torch)
     t = max_over_ranks(t, world)
     value = world * dofs / t / 1e9
-    bytes_per_apply = 8 * (2 + 6) * dofs
+    bytes_per_apply = u.element_size() * (2 + 6) * dofs
     peak, peak_kind = measured_peak()
     achieved = bytes_per_apply / t / 1e9
     traffic = traffic_from_profiles() if E == E_FULL else None
 
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps, "warmup": warmup,
            "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-           "dtype": "f64", "data": "synthetic",
+           "dtype": "f64" if prec == bk.PREC_FP64 else "f32", "data": "synthetic",
            "config": {"workload": f"BK5 collocated Laplacian p={P_ORDER} (P=Q=8 GLL) FP64 apply, E={E} "
                                   f"({dofs} DoFs), jittered trilinear mesh, G6 interleaved",
-                      "p": P_ORDER, "elements": E, "engine": args.engine, "l2": "inputs 8.6 GB >> 129 MB L2, no flush",
+                      "p": P_ORDER, "elements": E, "engine": args.engine, "prec": args.prec, "kernel": args.kernel,
+                      "layout": args.layout, "l2": "inputs 8.6 GB >> 129 MB L2, no flush",
                       "parallelism": f"replicas x{world}"},
            "gpu_launches": steps,
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -290,7 +301,7 @@ def main():
 
     # end to end through the C ABI: pinned host u -> device, apply, v -> pinned host
     if not args.no_e2e:
-        uh = torch.empty(u.numel(), dtype=torch.float64, pin_memory=True)
+        uh = torch.empty(u.numel(), dtype=u.dtype, pin_memory=True)
         vh = torch.empty_like(uh)
         uh.copy_(u)
 
@@ -300,17 +311,18 @@ def main():
             vh.copy_(v, non_blocking=True)
 
         te = max_over_ranks(time_loop(e2e, max(3, steps // 10), 2, world, stream, torch), world)
-        out["e2e"] = {"value": world * dofs / te / 1e9, "unit": UNIT, "h2d_bytes_per_step": 8 * dofs,
-                      "d2h_bytes_per_step": 8 * dofs, "ms_per_step": te * 1e3,
+        out["e2e"] = {"value": world * dofs / te / 1e9, "unit": UNIT, "h2d_bytes_per_step": u.element_size() * dofs,
+                      "d2h_bytes_per_step": u.element_size() * dofs, "ms_per_step": te * 1e3,
                       "note": "G (6.4 GB) resident on the device; u in, v out every step"}
 
     # the forms side by side, with their error against the FP64 result
-    if not args.no_forms and rank == 0:
+    if not args.no_forms and rank == 0 and prec == bk.PREC_FP64:
         forms = {}
         ref = v.clone()
         forms["fp64_ff"] = {"gdofs": value / world, "rel_err_vs_fp64": 0.0}
         vd = torch.empty_like(v)
-        td = time_loop(lambda: bk.bk5_apply(P_ORDER, E, D, G, u, vd, engine=bk.ENGINE_DFMA, stream=stream),
+        td = time_loop(lambda: bk.bk5_apply(P_ORDER, E, D, G, u, vd, engine=bk.ENGINE_DFMA, layout=args.layout,
+                                            stream=stream),
                        max(3, steps // 20), 2, 1, stream, torch)
         forms["fp64_dfma"] = {"gdofs": dofs / td / 1e9,
                               "rel_err_vs_fp64": float((vd - ref).abs().max() / ref.abs().max())}
@@ -318,7 +330,8 @@ def main():
         u32, G32 = u.float(), G.float()
         v32 = torch.empty_like(u32)
         for name, prec in (("mixed_fp32_storage", bk.PREC_MIXED), ("fp32", bk.PREC_FP32)):
-            tm = time_loop(lambda: bk.bk5_apply(P_ORDER, E, D, G32, u32, v32, prec=prec, stream=stream),
+            tm = time_loop(lambda: bk.bk5_apply(P_ORDER, E, D, G32, u32, v32, prec=prec, layout=args.layout,
+                                                stream=stream),
                            max(3, steps // 4), 3, 1, stream, torch)
             err = float((v32.double() - ref).abs().max() / ref.abs().max())
             forms[name] = {"gdofs": dofs / tm / 1e9, "rel_err_vs_fp64": err,

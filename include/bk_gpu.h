@@ -96,10 +96,21 @@ typedef struct bk_options {
     int nfactors;  /* BK5: 6 (symmetric rr rs rt ss st tt) or 9 (full 3x3,
                       row-major; bk5_offload.cpp "F") */
     int elems_per_block; /* elements per thread block; 0: the tuned default */
+    int kernel;    /* bk_kernel_shape (BK5); BK1/BK3 have the sweep kernel only */
 } bk_options;
 
+/* BK5 kernel shapes. */
+enum bk_kernel_shape {
+    BK_KERNEL_AUTO = 0,   /* the column kernel */
+    BK_KERNEL_SWEEP = 1,  /* one thread per line of the box per 1-D contraction,
+                             all intermediates in shared memory */
+    BK_KERNEL_COLUMN = 2  /* one thread per k-column of an element, the
+                             k-direction and the pointwise products in
+                             registers, TMA double buffering */
+};
+
 /* bk_options with the defaults: prec FP64, engine AUTO, BK5 layout
- * INTERLEAVED with 6 factors, elems_per_block 0. */
+ * INTERLEAVED with 6 factors, elems_per_block 0, kernel AUTO. */
 bk_options bk_default_options(void);
 
 /* ---- operator apply ------------------------------------------------------- */

@@ -33,6 +33,7 @@ STATUS_NAMES = {0: "ok", 1: "unsupported polynomial order p", 2: "bad element co
 PREC_FP64, PREC_FP32, PREC_MIXED = 0, 1, 2
 ENGINE_AUTO, ENGINE_DFMA, ENGINE_FF = 0, 1, 2
 LAYOUT_FACTOR, LAYOUT_INTERLEAVED, LAYOUT_COLUMN = 0, 1, 2
+KERNEL_AUTO, KERNEL_SWEEP, KERNEL_COLUMN = 0, 1, 2
 
 # every symbol the C headers declare (checked by the CPU tests)
 EXPORTS = [
@@ -54,7 +55,7 @@ class BKError(RuntimeError):
 
 class Options(C.Structure):
     _fields_ = [("prec", C.c_int), ("engine", C.c_int), ("layout", C.c_int), ("nfactors", C.c_int),
-                ("elems_per_block", C.c_int)]
+                ("elems_per_block", C.c_int), ("kernel", C.c_int)]
 
 
 _lib = None
@@ -156,9 +157,10 @@ class ApplyOptions:
     layout: int = LAYOUT_INTERLEAVED
     nfactors: int = 6
     elems_per_block: int = 0
+    kernel: int = KERNEL_AUTO
 
     def c(self) -> Options:
-        return Options(self.prec, self.engine, self.layout, self.nfactors, self.elems_per_block)
+        return Options(self.prec, self.engine, self.layout, self.nfactors, self.elems_per_block, self.kernel)
 
 
 # ---- operator apply (device tensors) -------------------------------------------
@@ -183,11 +185,12 @@ def bk3_apply(p, E, B, D, G, u, v, k=None, prec=PREC_FP64, engine=ENGINE_AUTO, s
 
 
 def bk5_apply(p, E, D, G, u, v, prec=PREC_FP64, engine=ENGINE_AUTO, layout=LAYOUT_INTERLEAVED, nfactors=6,
-              mass=None, lam=0.0, stream=None):
+              mass=None, lam=0.0, kernel=KERNEL_AUTO, elems_per_block=0, stream=None):
     """v = D^T G D u (+ lam * mass * u) per element (openmp/BK5.cpp:18-103)."""
     _order(p, "bk5_apply")
     Dh, Dp = _host(D)
-    o = ApplyOptions(prec=prec, engine=engine, layout=layout, nfactors=nfactors).c()
+    o = ApplyOptions(prec=prec, engine=engine, layout=layout, nfactors=nfactors, kernel=kernel,
+                     elems_per_block=elems_per_block).c()
     check(lib().bk5_apply_ex(p, E, Dp, _ptr(G), _ptr(u), _ptr(mass), float(lam), _ptr(v), C.byref(o),
                              _stream(stream)), "bk5_apply")
 

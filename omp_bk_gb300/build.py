@@ -32,14 +32,18 @@ def nvcc() -> str:
 
 def _flags() -> list[str]:
     return ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-Wall",
-                   "-I" + os.path.join(ROOT, "include"), "-I" + CSRC, "--expt-relaxed-constexpr"]
+                   "-I" + os.path.join(ROOT, "include"), "-I" + CSRC, "--expt-relaxed-constexpr", "-diag-suppress", "177"]
 
 
 def _units() -> list[tuple[str, list[str], str]]:
     """(source, extra flags, object) of every translation unit."""
     u = []
     for eng in range(4):
-        u.append(("bk_ops.cu", [f"-DBK_ENGINE_TU={eng}"], f"bk_ops_{eng}.o"))
+        for op in (1, 3, 5):
+            u.append(("bk_ops.cu", [f"-DBK_ENGINE_TU={eng}", f"-DBK_OP_TU={op}"], f"bk_ops_{eng}_{op}.o"))
+        for lay in range(3):
+            u.append(("bk_ops.cu", [f"-DBK_ENGINE_TU={eng}", "-DBK_OP_TU=6", f"-DBK_LAYOUT_TU={lay}"],
+                      f"bk_ops_{eng}_6_{lay}.o"))
     for src in ("bk_api.cu", "bk_geom.cu", "bk_basis.cpp"):
         u.append((src, [], src.rsplit(".", 1)[0] + ".o"))
     return u
@@ -68,7 +72,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     Returns the library path."""
     os.makedirs(OBJDIR, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
-    units = _units()
+    units = sorted(_units(), key=lambda t: "_6_" not in t[2])
     jobs = jobs or min(len(units), os.cpu_count() or 4)
     with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
         objs = list(ex.map(lambda t: _compile(t[0], t[1], t[2], verbose), units))
@@ -79,7 +83,27 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    _driver(verbose)
     return LIB
+
+
+DRIVER = os.path.join(LIBDIR, "bk_cuda")
+
+
+def _driver(verbose: bool) -> None:
+    """The C++ host driver with the reference drivers' command line, linked
+    against the library (rpath $ORIGIN)."""
+    src = os.path.join(CSRC, "driver", "bk_driver.cpp")
+    if os.path.exists(DRIVER) and os.path.getmtime(DRIVER) >= max(os.path.getmtime(src), os.path.getmtime(LIB)):
+        return
+    cmd = [nvcc()] + ARCH + ["-O2", "-std=c++17", "-Xcompiler", "-fopenmp,-Wall", "-I" + os.path.join(ROOT, "include"),
+                             src, "-o", DRIVER, "-L" + LIBDIR, "-lbk_gb300", "-Xlinker", "-rpath,$ORIGIN",
+                             "-Xcompiler", "-fopenmp"]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"driver build failed:\n{r.stdout}\n{r.stderr}")
 
 
 if __name__ == "__main__":

@@ -131,6 +131,7 @@ bk_options bk_default_options(void)
     o.layout = BK_LAYOUT_INTERLEAVED;
     o.nfactors = 6;
     o.elems_per_block = 0;
+    o.kernel = BK_KERNEL_AUTO;
     return o;
 }
 
@@ -147,16 +148,18 @@ int bk5_apply_ex(int p, int64_t E, const double* D, const void* G, const void* u
     if (mass != nullptr && misaligned(mass)) return BK_ERR_ALIGN;
     if (o.nfactors != 6 && o.nfactors != 9) return BK_ERR_PREC;
     if (o.layout < 0 || o.layout > 2) return BK_ERR_PREC;
+    if (o.kernel < 0 || o.kernel > 2) return BK_ERR_PREC;
+    if (o.elems_per_block < 0 || o.elems_per_block > 64) return BK_ERR_ARG;
     const int eng = engine_of(o);
     if (eng < 0) return BK_ERR_PREC;
     if (E == 0) return BK_OK;
     if ((rc = status_or_null())) return rc;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     switch (eng) {
-        case 0: return launch_bk5_dfma(p, E, D, G, u, mass, lambda, v, o.nfactors, o.layout, o.elems_per_block, s);
-        case 1: return launch_bk5_ff(p, E, D, G, u, mass, lambda, v, o.nfactors, o.layout, o.elems_per_block, s);
-        case 2: return launch_bk5_f32(p, E, D, G, u, mass, lambda, v, o.nfactors, o.layout, o.elems_per_block, s);
-        default: return launch_bk5_mixed(p, E, D, G, u, mass, lambda, v, o.nfactors, o.layout, o.elems_per_block, s);
+        case 0: return launch_bk5_dfma(p, E, D, G, u, mass, lambda, v, o.nfactors, o.layout, o.elems_per_block, o.kernel, s);
+        case 1: return launch_bk5_ff(p, E, D, G, u, mass, lambda, v, o.nfactors, o.layout, o.elems_per_block, o.kernel, s);
+        case 2: return launch_bk5_f32(p, E, D, G, u, mass, lambda, v, o.nfactors, o.layout, o.elems_per_block, o.kernel, s);
+        default: return launch_bk5_mixed(p, E, D, G, u, mass, lambda, v, o.nfactors, o.layout, o.elems_per_block, o.kernel, s);
     }
 }
 

@@ -6,10 +6,16 @@
 #include <cuda_runtime.h>
 
 #include "bk_internal.h"
+#include "bk5_col.cuh"
 #include "bk_kernels.cuh"
 
 #ifndef BK_ENGINE_TU
 #error "BK_ENGINE_TU must be 0 (dfma), 1 (ff), 2 (fp32) or 3 (mixed)"
+#endif
+// BK_OP_TU selects the operator of this translation unit: 1 BK1, 3 BK3,
+// 5 BK5 sweep kernel, 6 BK5 column kernel and the BK5 dispatch.
+#ifndef BK_OP_TU
+#error "BK_OP_TU must be 1, 3, 5 or 6"
 #endif
 
 namespace bkg {
@@ -37,8 +43,9 @@ namespace {
 constexpr int default_eb(int q) { return (q * q >= 100) ? 1 : ((q * q >= 64) ? 2 : (128 + q * q - 1) / (q * q)); }
 
 // Sets the dynamic shared-memory size of a kernel on the current device once
-// and returns its resident blocks per SM (0 if it cannot run).
-template <class K>
+// and returns its resident blocks per SM (0 if it cannot run).  Tag makes the
+// cache one per kernel instantiation (kernels of one signature share K).
+template <class Tag, class K>
 int prepare(K kern, int smem, int nt)
 {
     static int occ[kMaxDevices] = {0};
@@ -59,6 +66,7 @@ int grid_for(long long nbatch, int occ)
     return static_cast<int>(nbatch < cap ? nbatch : cap);
 }
 
+#if BK_OP_TU == 5
 template <int Q, int EB, int F, int LAYOUT>
 int bk5_q(const double* D, long long E, const void* u, const void* G, const void* mass, double lambda, void* v,
           cudaStream_t s)
@@ -69,7 +77,7 @@ int bk5_q(const double* D, long long E, const void* u, const void* G, const void
     P5<typename Eng::C, Q> prm;
     for (int i = 0; i < Q * Q; ++i) prm.D[i] = Eng::coef(D[i]);
     auto kern = bk5_kernel<Eng, Q, EB, F, LAYOUT>;
-    const int occ = prepare(kern, Cfg::SMEM, Cfg::NT);
+    const int occ = prepare<Cfg>(kern, Cfg::SMEM, Cfg::NT);
     if (occ <= 0) return BK_ERR_CUDA;
     const int grid = grid_for((E + EB - 1) / EB, occ);
     kern<<<grid, Cfg::NT, Cfg::SMEM, s>>>(prm, E, static_cast<const S*>(u), static_cast<const S*>(G),
@@ -78,12 +86,11 @@ int bk5_q(const double* D, long long E, const void* u, const void* G, const void
 }
 
 template <int Q>
-int bk5_fl(int F, int layout, int eb, const double* D, long long E, const void* u, const void* G, const void* mass,
-           double lambda, void* v, cudaStream_t s)
+int bk5_sweep_q(int F, int layout, const double* D, long long E, const void* u, const void* G, const void* mass,
+                double lambda, void* v, cudaStream_t s)
 {
     constexpr int EB = default_eb(Q);
-    (void)eb;
-#define BK5_CASE(FF, LL)                                                            \
+#define BK5_CASE(FF, LL) \
     if (F == FF && layout == LL) return bk5_q<Q, EB, FF, LL>(D, E, u, G, mass, lambda, v, s);
     BK5_CASE(6, 1)
     BK5_CASE(6, 0)
@@ -94,7 +101,47 @@ int bk5_fl(int F, int layout, int eb, const double* D, long long E, const void* 
 #undef BK5_CASE
     return BK_ERR_PREC;
 }
+#endif  // BK_OP_TU == 5
 
+#if BK_OP_TU == 6
+// Column kernel: elements per block and stage buffers.  The FP32-storage
+// forms are HBM-bound (double buffering), the FP64 engines ALU-bound (one
+// stage, more blocks per SM).
+constexpr int col_nbuf() { return (sizeof(typename Eng::S) == 4) ? 2 : 1; }
+constexpr int col_eb(int q) { return (q * q >= 64) ? ((sizeof(typename Eng::S) == 4) ? 2 : 1) : (128 + q * q - 1) / (q * q); }
+
+template <int Q, int EB, int F, int LAYOUT, int NBUF>
+int bk5col_q(const double* D, long long E, const void* u, const void* G, const void* mass, double lambda, void* v,
+             cudaStream_t s)
+{
+    using Cfg = BK5ColCfg<Eng, Q, EB, F, NBUF>;
+    using S = typename Eng::S;
+    static_assert(Cfg::SMEM <= 232448, "BK5 block exceeds the shared memory of an SM");
+    P5<typename Eng::C, Q> prm;
+    for (int i = 0; i < Q * Q; ++i) prm.D[i] = Eng::coef(D[i]);
+    auto kern = bk5_col_kernel<Eng, Q, EB, F, LAYOUT, NBUF>;
+    const int occ = prepare<BK5ColCfg<Eng, Q, EB, F * 8 + LAYOUT, NBUF>>(kern, Cfg::SMEM, Cfg::NT);
+    if (occ <= 0) return BK_ERR_CUDA;
+    const int grid = grid_for((E + EB - 1) / EB, occ);
+    kern<<<grid, Cfg::NT, Cfg::SMEM, s>>>(prm, E, static_cast<const S*>(u), static_cast<const S*>(G),
+                                          static_cast<const S*>(mass), lambda, static_cast<S*>(v), dev_ctx());
+    return cudaGetLastError() == cudaSuccess ? BK_OK : BK_ERR_CUDA;
+}
+
+template <int Q>
+int bk5col_f(int F, int eb, const double* D, long long E, const void* u, const void* G, const void* mass,
+             double lambda, void* v, cudaStream_t s)
+{
+    constexpr int NB = col_nbuf();
+    constexpr int EB0 = col_eb(Q);
+    if (eb != 0 && eb != EB0) return BK_ERR_ARG;
+    if (F == 6) return bk5col_q<Q, EB0, 6, BK_LAYOUT_TU, NB>(D, E, u, G, mass, lambda, v, s);
+    if (F == 9) return bk5col_q<Q, EB0, 9, BK_LAYOUT_TU, NB>(D, E, u, G, mass, lambda, v, s);
+    return BK_ERR_PREC;
+}
+#endif  // BK_OP_TU == 6
+
+#if BK_OP_TU == 1
 template <int Q, int EB>
 int bk1_q(const double* B, long long E, const void* jxw, const void* u, void* v, cudaStream_t s)
 {
@@ -105,7 +152,7 @@ int bk1_q(const double* B, long long E, const void* jxw, const void* u, void* v,
     for (int i = 0; i < (Q - 1) * Q; ++i) prm.B[i] = Eng::coef(B[i]);
     for (int i = 0; i < Q * Q; ++i) prm.D[i] = Eng::coef(0.0);
     auto kern = bk1_kernel<Eng, Q, EB>;
-    const int occ = prepare(kern, Cfg::SMEM, Cfg::NT);
+    const int occ = prepare<Cfg>(kern, Cfg::SMEM, Cfg::NT);
     if (occ <= 0) return BK_ERR_CUDA;
     const int grid = grid_for((E + EB - 1) / EB, occ);
     kern<<<grid, Cfg::NT, Cfg::SMEM, s>>>(prm, E, static_cast<const S*>(u), static_cast<const S*>(jxw),
@@ -113,6 +160,9 @@ int bk1_q(const double* B, long long E, const void* jxw, const void* u, void* v,
     return cudaGetLastError() == cudaSuccess ? BK_OK : BK_ERR_CUDA;
 }
 
+#endif  // BK_OP_TU == 1
+
+#if BK_OP_TU == 3
 template <int Q, int EB>
 int bk3_q(const double* B, const double* D, long long E, const void* G, const void* k, const void* u, void* v,
           cudaStream_t s)
@@ -124,7 +174,7 @@ int bk3_q(const double* B, const double* D, long long E, const void* G, const vo
     for (int i = 0; i < (Q - 1) * Q; ++i) prm.B[i] = Eng::coef(B[i]);
     for (int i = 0; i < Q * Q; ++i) prm.D[i] = Eng::coef(D[i]);
     auto kern = bk3_kernel<Eng, Q, EB>;
-    const int occ = prepare(kern, Cfg::SMEM, Cfg::NT);
+    const int occ = prepare<Cfg>(kern, Cfg::SMEM, Cfg::NT);
     if (occ <= 0) return BK_ERR_CUDA;
     const int grid = grid_for((E + EB - 1) / EB, occ);
     kern<<<grid, Cfg::NT, Cfg::SMEM, s>>>(prm, E, static_cast<const S*>(u), static_cast<const S*>(G),
@@ -132,24 +182,64 @@ int bk3_q(const double* B, const double* D, long long E, const void* G, const vo
     return cudaGetLastError() == cudaSuccess ? BK_OK : BK_ERR_CUDA;
 }
 
+#endif  // BK_OP_TU == 3
+
 }  // namespace
 
+#if BK_OP_TU == 5
+#define BK_CATL_(a, b, c) a##_##b##_L##c
+#define BK_CATL(a, b, c) BK_CATL_(a, b, c)
 int BK_CAT(launch_bk5, BK_SFX)(int p, long long E, const double* D, const void* G, const void* u, const void* mass,
-                                double lambda, void* v, int F, int layout, int eb, cudaStream_t s)
+                                double lambda, void* v, int F, int layout, int eb, int kernel, cudaStream_t s)
 {
-    switch (p + 1) {
-        case 2: return bk5_fl<2>(F, layout, eb, D, E, u, G, mass, lambda, v, s);
-        case 3: return bk5_fl<3>(F, layout, eb, D, E, u, G, mass, lambda, v, s);
-        case 4: return bk5_fl<4>(F, layout, eb, D, E, u, G, mass, lambda, v, s);
-        case 5: return bk5_fl<5>(F, layout, eb, D, E, u, G, mass, lambda, v, s);
-        case 6: return bk5_fl<6>(F, layout, eb, D, E, u, G, mass, lambda, v, s);
-        case 7: return bk5_fl<7>(F, layout, eb, D, E, u, G, mass, lambda, v, s);
-        case 8: return bk5_fl<8>(F, layout, eb, D, E, u, G, mass, lambda, v, s);
-        case 9: return bk5_fl<9>(F, layout, eb, D, E, u, G, mass, lambda, v, s);
-        default: return BK_ERR_ORDER;
+    if (p < 1 || p > 8) return BK_ERR_ORDER;
+    if (kernel == BK_KERNEL_SWEEP) return BK_CAT(bk5_sweep, BK_SFX)(p, F, layout, D, E, u, G, mass, lambda, v, s);
+    switch (layout) {
+        case 0: return BK_CATL(bk5_col, BK_SFX, 0)(p, F, eb, D, E, u, G, mass, lambda, v, s);
+        case 1: return BK_CATL(bk5_col, BK_SFX, 1)(p, F, eb, D, E, u, G, mass, lambda, v, s);
+        case 2: return BK_CATL(bk5_col, BK_SFX, 2)(p, F, eb, D, E, u, G, mass, lambda, v, s);
+        default: return BK_ERR_PREC;
     }
 }
 
+int BK_CAT(bk5_sweep, BK_SFX)(int p, int F, int layout, const double* D, long long E, const void* u, const void* G,
+                               const void* mass, double lambda, void* v, cudaStream_t s)
+{
+    switch (p + 1) {
+        case 2: return bk5_sweep_q<2>(F, layout, D, E, u, G, mass, lambda, v, s);
+        case 3: return bk5_sweep_q<3>(F, layout, D, E, u, G, mass, lambda, v, s);
+        case 4: return bk5_sweep_q<4>(F, layout, D, E, u, G, mass, lambda, v, s);
+        case 5: return bk5_sweep_q<5>(F, layout, D, E, u, G, mass, lambda, v, s);
+        case 6: return bk5_sweep_q<6>(F, layout, D, E, u, G, mass, lambda, v, s);
+        case 7: return bk5_sweep_q<7>(F, layout, D, E, u, G, mass, lambda, v, s);
+        case 8: return bk5_sweep_q<8>(F, layout, D, E, u, G, mass, lambda, v, s);
+        case 9: return bk5_sweep_q<9>(F, layout, D, E, u, G, mass, lambda, v, s);
+        default: return BK_ERR_ORDER;
+    }
+}
+#endif
+
+#if BK_OP_TU == 6
+#define BK_CAT3_(a, b, c) a##_##b##_L##c
+#define BK_CAT3(a, b, c) BK_CAT3_(a, b, c)
+int BK_CAT3(bk5_col, BK_SFX, BK_LAYOUT_TU)(int p, int F, int eb, const double* D, long long E, const void* u,
+                                            const void* G, const void* mass, double lambda, void* v, cudaStream_t s)
+{
+    switch (p + 1) {
+        case 2: return bk5col_f<2>(F, eb, D, E, u, G, mass, lambda, v, s);
+        case 3: return bk5col_f<3>(F, eb, D, E, u, G, mass, lambda, v, s);
+        case 4: return bk5col_f<4>(F, eb, D, E, u, G, mass, lambda, v, s);
+        case 5: return bk5col_f<5>(F, eb, D, E, u, G, mass, lambda, v, s);
+        case 6: return bk5col_f<6>(F, eb, D, E, u, G, mass, lambda, v, s);
+        case 7: return bk5col_f<7>(F, eb, D, E, u, G, mass, lambda, v, s);
+        case 8: return bk5col_f<8>(F, eb, D, E, u, G, mass, lambda, v, s);
+        case 9: return bk5col_f<9>(F, eb, D, E, u, G, mass, lambda, v, s);
+        default: return BK_ERR_ORDER;
+    }
+}
+#endif
+
+#if BK_OP_TU == 1
 int BK_CAT(launch_bk1, BK_SFX)(int p, long long E, const double* B, const void* jxw, const void* u, void* v,
                                 int eb, cudaStream_t s)
 {
@@ -167,6 +257,9 @@ int BK_CAT(launch_bk1, BK_SFX)(int p, long long E, const double* B, const void* 
     }
 }
 
+#endif
+
+#if BK_OP_TU == 3
 int BK_CAT(launch_bk3, BK_SFX)(int p, long long E, const double* B, const double* D, const void* G, const void* k,
                                 const void* u, void* v, int eb, cudaStream_t s)
 {
@@ -183,5 +276,7 @@ int BK_CAT(launch_bk3, BK_SFX)(int p, long long E, const double* B, const double
         default: return BK_ERR_ORDER;
     }
 }
+
+#endif
 
 }  // namespace bkg

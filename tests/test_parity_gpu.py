@@ -108,20 +108,46 @@ def test_element_counts(bklib, bk, p, E):
 @pytest.mark.parametrize("p", [1, 4, 7, 8])
 @pytest.mark.parametrize("nfactors", [6, 9])
 @pytest.mark.parametrize("layout", [0, 1, 2])
-@pytest.mark.parametrize("engine", ["dfma", "ff"])
-def test_bk5_layouts(bklib, p, nfactors, layout, engine):
+@pytest.mark.parametrize("engine", ["dfma", "ff", "fp32"])
+@pytest.mark.parametrize("kernel", ["sweep", "column"])
+def test_bk5_layouts(bklib, p, nfactors, layout, engine, kernel):
     """BK5 with G in every layout and factor count of make_bk5_G
-    (include/bk_harness.h:217-244)."""
+    (include/bk_harness.h:217-244), with both kernel shapes."""
     E = 7
     nq, _, dbasis, g6i, u = random_case(5, p, E)
     G = oracle.make_bk5_G(g6i, E, nq, nfactors, layout)
-    eng = bklib.ENGINE_DFMA if engine == "dfma" else bklib.ENGINE_FF
-    gu, gg = dev(u, "f64"), dev(G, "f64")
+    kern = bklib.KERNEL_SWEEP if kernel == "sweep" else bklib.KERNEL_COLUMN
+    if engine == "fp32":
+        dt, prec, eng, tol = "f32", bklib.PREC_FP32, 0, TOL32
+        f = lambda a: a.astype(np.float32).astype(np.float64)
+        ref = oracle.bk5(nq, E, dbasis, f(g6i), f(u))
+    else:
+        dt, prec, tol = "f64", bklib.PREC_FP64, TOL64
+        eng = bklib.ENGINE_DFMA if engine == "dfma" else bklib.ENGINE_FF
+        ref = oracle.bk5(nq, E, dbasis, g6i, u)
+    gu, gg = dev(u, dt), dev(G, dt)
     out = torch.full_like(gu, float("nan"))
-    bklib.bk5_apply(p, E, dbasis, gg, gu, out, engine=eng, layout=layout, nfactors=nfactors)
+    bklib.bk5_apply(p, E, dbasis, gg, gu, out, prec=prec, engine=eng, layout=layout, nfactors=nfactors, kernel=kern)
     torch.cuda.synchronize()
-    ref = oracle.bk5(nq, E, dbasis, g6i, u)
-    assert oracle.rel_maxdiff(host(out), ref) < TOL64
+    assert oracle.rel_maxdiff(host(out), ref) < tol
+
+
+@pytest.mark.parametrize("p", [1, 2, 3, 4, 5, 6, 7, 8])
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_bk5_kernel_shapes_agree(bklib, p, prec):
+    """The sweep and column kernels give the same operator."""
+    E = 37
+    nq, _, dbasis, g, u = random_case(5, p, E, seed=99)
+    pr = bklib.PREC_FP64 if prec == "fp64" else bklib.PREC_MIXED
+    dt = "f64" if prec == "fp64" else "f32"
+    gu, gg = dev(u, dt), dev(g, dt)
+    outs = []
+    for kern in (bklib.KERNEL_SWEEP, bklib.KERNEL_COLUMN):
+        out = torch.full_like(gu, float("nan"))
+        bklib.bk5_apply(p, E, dbasis, gg, gu, out, prec=pr, kernel=kern)
+        outs.append(host(out))
+    torch.cuda.synchronize()
+    assert oracle.rel_maxdiff(outs[1], outs[0]) < (TOL64 if prec == "fp64" else TOL32)
 
 
 @pytest.mark.parametrize("p", [2, 5, 8])
