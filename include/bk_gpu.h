@@ -161,6 +161,19 @@ int bk5_apply_ex(int p, int64_t E, const double* D, const void* G, const void* u
 int bk3_apply_k(int p, int64_t E, const double* B, const double* D, const void* G, const void* k,
                 const void* u, void* v, const bk_options* opt, bk_stream_t stream);
 
+/* Backward of the variable-coefficient BK3 operator (no reference
+ * counterpart).  For L = 1/2 |A(k) u - f|^2 and res = A(k) u - f (computed
+ * by the caller with bk3_apply_k and an axpby):
+ *   dk(e, x)    = dL/dk at every quadrature point           (E x Q^3)
+ *   dG(e, f, x) = dL/dG for the six stored symmetric factors  (E x 6 x Q^3,
+ *                 factor-major; an off-diagonal factor stands for both of
+ *                 its entries)
+ * The gradients of u and res at the points are recomputed, not stored.  The
+ * operator is symmetric, so dL/du = A(k) res is bk3_apply_k itself. */
+int bk3_adjoint(int p, int64_t E, const double* B, const double* D, const void* G, const void* k,
+                const void* u, const void* res, void* dk, void* dG, const bk_options* opt,
+                bk_stream_t stream);
+
 /* ---- device status -------------------------------------------------------- */
 
 /* Reads (and, if reset != 0, clears) the status word of the current device:

@@ -42,6 +42,7 @@ EXPORTS = [
     "bk_test_wait_timeout", "bk_version",
     "bk_gauss_points", "bk_gll_points", "bk_lagrange_interp", "bk_lagrange_deriv", "bk_fill_uniform",
     "bk_fill_lognormal", "bk_geom_affine", "bk_coords_affine", "bk_geom_trilinear", "bk_convert",
+    "bk3_adjoint", "bk_stream_kernel", "bk_dot_workspace_bytes", "bk_dot", "bk_axpby",
 ]
 
 
@@ -98,11 +99,17 @@ def lib():
         "bk_geom_trilinear": [C.c_int, C.c_longlong, C.c_int, C.c_int, _dp, _dp, C.c_ulonglong, C.c_double,
                               C.c_double, _vp, C.c_int, _vp, _vp, _vp],
         "bk_convert": [_vp, _vp, C.c_longlong, C.c_int, _vp],
+        "bk3_adjoint": [C.c_int, _i64, _dp, _dp, _vp, _vp, _vp, _vp, _vp, _vp, C.POINTER(Options), _vp],
+        "bk_stream_kernel": [C.c_int, C.c_longlong, _vp, _vp, _vp, C.c_int, _vp],
+        "bk_dot": [C.c_longlong, _vp, _vp, C.c_int, _vp, _vp, C.c_longlong, C.c_int, _vp],
+        "bk_axpby": [C.c_longlong, C.c_double, _vp, C.c_double, _vp, C.c_int, _vp],
     }
     for name, args in sig.items():
         f = getattr(L, name)
         f.argtypes = args
         f.restype = C.c_int
+    L.bk_dot_workspace_bytes.argtypes = [C.c_longlong]
+    L.bk_dot_workspace_bytes.restype = C.c_longlong
     L.bk_version.restype = C.c_char_p
     L.bk_default_options.restype = Options
     _lib = L
@@ -315,3 +322,46 @@ def convert(src, dst, stream=None):
     check(lib().bk_convert(_ptr(src), _ptr(dst), src.numel(), int(dst.dtype == torch.float32), _stream(stream)),
           "bk_convert")
     return dst
+
+
+# ---- adjoint, vector kernels ---------------------------------------------------
+
+def bk3_adjoint(p, E, B, D, G, k, u, res, dk, dG, prec=PREC_FP64, engine=ENGINE_AUTO, stream=None):
+    """dL/dk (E x Q^3) and dL/dG (E x 6 x Q^3) of L = 1/2 |A(k) u - f|^2 given
+    res = A(k) u - f; the forward kernel is bk3_apply(..., k=k)."""
+    _order(p, "bk3_adjoint")
+    Bh, Bp = _host(B)
+    Dh, Dp = _host(D)
+    o = ApplyOptions(prec=prec, engine=engine).c()
+    check(lib().bk3_adjoint(p, E, Bp, Dp, _ptr(G), _ptr(k), _ptr(u), _ptr(res), _ptr(dk), _ptr(dG), C.byref(o),
+                            _stream(stream)), "bk3_adjoint")
+
+
+STREAM_COPY, STREAM_TRIAD, STREAM_MIX = 0, 1, 2
+
+
+def stream_kernel(kind, a, b, c=None, reads=1, stream=None):
+    nbytes = a.numel() * a.element_size()
+    check(lib().bk_stream_kernel(kind, nbytes, _ptr(a), _ptr(b), _ptr(c), reads, _stream(stream)),
+          "bk_stream_kernel")
+
+
+def dot_workspace(n, device="cuda"):
+    import torch
+    return torch.empty(int(lib().bk_dot_workspace_bytes(n)) // 8, dtype=torch.float64, device=device)
+
+
+def dot(x, y, out, workspace, half=False, stream=None):
+    """out[0] = x . y (FP64 accumulation, deterministic); out a device double."""
+    import torch
+    check(lib().bk_dot(x.numel(), _ptr(x), _ptr(y), int(x.dtype == torch.float64), _ptr(out), _ptr(workspace),
+                       workspace.numel() * 8, int(half), _stream(stream)), "bk_dot")
+    return out
+
+
+def axpby(a, x, b, y, stream=None):
+    """y = a x + b y."""
+    import torch
+    check(lib().bk_axpby(x.numel(), float(a), _ptr(x), float(b), _ptr(y), int(y.dtype == torch.float64),
+                         _stream(stream)), "bk_axpby")
+    return y

@@ -39,12 +39,12 @@ def _units() -> list[tuple[str, list[str], str]]:
     """(source, extra flags, object) of every translation unit."""
     u = []
     for eng in range(4):
-        for op in (1, 3, 5):
+        for op in (1, 3, 5, 7):
             u.append(("bk_ops.cu", [f"-DBK_ENGINE_TU={eng}", f"-DBK_OP_TU={op}"], f"bk_ops_{eng}_{op}.o"))
         for lay in range(3):
             u.append(("bk_ops.cu", [f"-DBK_ENGINE_TU={eng}", "-DBK_OP_TU=6", f"-DBK_LAYOUT_TU={lay}"],
                       f"bk_ops_{eng}_6_{lay}.o"))
-    for src in ("bk_api.cu", "bk_geom.cu", "bk_basis.cpp"):
+    for src in ("bk_api.cu", "bk_geom.cu", "bk_basis.cpp", "bk_vec.cu"):
         u.append((src, [], src.rsplit(".", 1)[0] + ".o"))
     return u
 

@@ -242,6 +242,27 @@ int bk3_apply(int p, int64_t E, const double* B, const double* D, const void* G,
     return bk3_apply_opt(p, E, B, D, G, u, v, &o, stream);
 }
 
+int bk3_adjoint(int p, int64_t E, const double* B, const double* D, const void* G, const void* k, const void* u,
+                const void* res, void* dk, void* dG, const bk_options* opt, bk_stream_t stream)
+{
+    const bk_options o = opt ? *opt : bk_default_options();
+    int rc = check_common(p, 8, E);
+    if (rc) return rc;
+    if (B == nullptr || D == nullptr) return BK_ERR_NULL;
+    if ((rc = check_ptrs(E, {G, k, u, res, dk, dG}))) return rc;
+    const int eng = engine_of(o);
+    if (eng < 0) return BK_ERR_PREC;
+    if (E == 0) return BK_OK;
+    if ((rc = status_or_null())) return rc;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    switch (eng) {
+        case 0: return launch_bk3_adjoint_dfma(p, E, B, D, G, k, u, res, dk, dG, s);
+        case 1: return launch_bk3_adjoint_ff(p, E, B, D, G, k, u, res, dk, dG, s);
+        case 2: return launch_bk3_adjoint_f32(p, E, B, D, G, k, u, res, dk, dG, s);
+        default: return launch_bk3_adjoint_mixed(p, E, B, D, G, k, u, res, dk, dG, s);
+    }
+}
+
 int bk_device_status(int* status, int reset, bk_stream_t stream)
 {
     if (status == nullptr) return BK_ERR_NULL;

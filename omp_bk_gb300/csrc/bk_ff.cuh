@@ -118,6 +118,21 @@ __device__ __forceinline__ ff ff_mul(const ff a, const ff b)
 
 // ---- binary64 <-> float-float ------------------------------------------------
 
+// The rare out-of-range cases, out of line: kept off the fast path so that
+// the compiler cannot predicate their FP64-pipe instructions into it.
+__device__ __noinline__ ff split_slow(const double x)
+{
+    ff r;
+    r.hi = __double2float_rz(x);
+    r.lo = __double2float_rn(x - static_cast<double>(r.hi));
+    return r;
+}
+
+__device__ __noinline__ double join_slow(const float s, const float t)
+{
+    return static_cast<double>(s) + static_cast<double>(t);
+}
+
 // Split x into hi (x truncated to 24 significant bits) and lo (the remaining
 // 29 mantissa bits rounded to a float).  Fast path for biased exponents
 // 949..1150 (2^-74 <= |x| < 2^128): pure integer work plus one I2F and one
@@ -139,8 +154,7 @@ __device__ __forceinline__ ff split(const double x)
         const float scale = __uint_as_float(((e - 948u) << 23) | sign);
         r.lo = __fmul_rn(__uint2float_rn(wlo & 0x1fffffffu), scale);
     } else {
-        r.hi = __double2float_rz(x);
-        r.lo = __double2float_rn(x - static_cast<double>(r.hi));
+        r = split_slow(x);
     }
     return r;
 }
@@ -173,7 +187,7 @@ __device__ __forceinline__ double join(const ff v)
                                         static_cast<unsigned long long>(static_cast<long long>(k));
         return __longlong_as_double(static_cast<long long>(bits));
     }
-    return static_cast<double>(s) + static_cast<double>(t);
+    return join_slow(s, t);
 }
 
 }  // namespace bkg

@@ -7,15 +7,17 @@
 
 #include "bk_internal.h"
 #include "bk5_col.cuh"
+#include "bk_adjoint.cuh"
 #include "bk_kernels.cuh"
 
 #ifndef BK_ENGINE_TU
 #error "BK_ENGINE_TU must be 0 (dfma), 1 (ff), 2 (fp32) or 3 (mixed)"
 #endif
 // BK_OP_TU selects the operator of this translation unit: 1 BK1, 3 BK3,
-// 5 BK5 sweep kernel, 6 BK5 column kernel and the BK5 dispatch.
+// 5 BK5 sweep kernel and the BK5 dispatch, 6 BK5 column kernel (one G
+// layout, BK_LAYOUT_TU), 7 the BK3 adjoint.
 #ifndef BK_OP_TU
-#error "BK_OP_TU must be 1, 3, 5 or 6"
+#error "BK_OP_TU must be 1, 3, 5, 6 or 7"
 #endif
 
 namespace bkg {
@@ -114,13 +116,13 @@ template <int Q, int EB, int F, int LAYOUT, int NBUF>
 int bk5col_q(const double* D, long long E, const void* u, const void* G, const void* mass, double lambda, void* v,
              cudaStream_t s)
 {
-    using Cfg = BK5ColCfg<Eng, Q, EB, F, NBUF>;
+    using Cfg = BK5ColCfg<Eng, Q, EB, F, NBUF, LAYOUT>;
     using S = typename Eng::S;
     static_assert(Cfg::SMEM <= 232448, "BK5 block exceeds the shared memory of an SM");
     P5<typename Eng::C, Q> prm;
     for (int i = 0; i < Q * Q; ++i) prm.D[i] = Eng::coef(D[i]);
     auto kern = bk5_col_kernel<Eng, Q, EB, F, LAYOUT, NBUF>;
-    const int occ = prepare<BK5ColCfg<Eng, Q, EB, F * 8 + LAYOUT, NBUF>>(kern, Cfg::SMEM, Cfg::NT);
+    const int occ = prepare<Cfg>(kern, Cfg::SMEM, Cfg::NT);
     if (occ <= 0) return BK_ERR_CUDA;
     const int grid = grid_for((E + EB - 1) / EB, occ);
     kern<<<grid, Cfg::NT, Cfg::SMEM, s>>>(prm, E, static_cast<const S*>(u), static_cast<const S*>(G),
@@ -183,6 +185,29 @@ int bk3_q(const double* B, const double* D, long long E, const void* G, const vo
 }
 
 #endif  // BK_OP_TU == 3
+
+#if BK_OP_TU == 7
+template <int Q>
+int bk3adj_q(const double* B, const double* D, long long E, const void* G, const void* k, const void* u,
+             const void* res, void* dk, void* dG, cudaStream_t s)
+{
+    constexpr int EB = default_eb(Q) / 2 > 0 ? default_eb(Q) / 2 : 1;
+    using Cfg = BK3AdjCfg<Eng, Q, EB>;
+    using S = typename Eng::S;
+    static_assert(Cfg::SMEM <= 232448, "BK3 adjoint block exceeds the shared memory of an SM");
+    P13<typename Eng::C, Q> prm;
+    for (int i = 0; i < (Q - 1) * Q; ++i) prm.B[i] = Eng::coef(B[i]);
+    for (int i = 0; i < Q * Q; ++i) prm.D[i] = Eng::coef(D[i]);
+    auto kern = bk3_adjoint_kernel<Eng, Q, EB>;
+    const int occ = prepare<Cfg>(kern, Cfg::SMEM, Cfg::NT);
+    if (occ <= 0) return BK_ERR_CUDA;
+    const int grid = grid_for((E + EB - 1) / EB, occ);
+    kern<<<grid, Cfg::NT, Cfg::SMEM, s>>>(prm, E, static_cast<const S*>(u), static_cast<const S*>(res),
+                                          static_cast<const S*>(G), static_cast<const S*>(k), static_cast<S*>(dk),
+                                          static_cast<S*>(dG), dev_ctx());
+    return cudaGetLastError() == cudaSuccess ? BK_OK : BK_ERR_CUDA;
+}
+#endif  // BK_OP_TU == 7
 
 }  // namespace
 
@@ -277,6 +302,25 @@ int BK_CAT(launch_bk3, BK_SFX)(int p, long long E, const double* B, const double
     }
 }
 
+#endif
+
+#if BK_OP_TU == 7
+int BK_CAT(launch_bk3_adjoint, BK_SFX)(int p, long long E, const double* B, const double* D, const void* G,
+                                        const void* k, const void* u, const void* res, void* dk, void* dG,
+                                        cudaStream_t s)
+{
+    switch (p + 2) {
+        case 3: return bk3adj_q<3>(B, D, E, G, k, u, res, dk, dG, s);
+        case 4: return bk3adj_q<4>(B, D, E, G, k, u, res, dk, dG, s);
+        case 5: return bk3adj_q<5>(B, D, E, G, k, u, res, dk, dG, s);
+        case 6: return bk3adj_q<6>(B, D, E, G, k, u, res, dk, dG, s);
+        case 7: return bk3adj_q<7>(B, D, E, G, k, u, res, dk, dG, s);
+        case 8: return bk3adj_q<8>(B, D, E, G, k, u, res, dk, dG, s);
+        case 9: return bk3adj_q<9>(B, D, E, G, k, u, res, dk, dG, s);
+        case 10: return bk3adj_q<10>(B, D, E, G, k, u, res, dk, dG, s);
+        default: return BK_ERR_ORDER;
+    }
+}
 #endif
 
 }  // namespace bkg

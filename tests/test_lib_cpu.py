@@ -19,7 +19,7 @@ def _declared():
             continue
         src = open(os.path.join(ROOT, "include", h)).read()
         src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-        names |= set(re.findall(r"^\s*(?:int|bk_options|const char\*)\s+(bk\w+)\s*\(", src, flags=re.M))
+        names |= set(re.findall(r"^\s*(?:int|long long|bk_options|const char\*)\s+(bk\w+)\s*\(", src, flags=re.M))
     return names
 
 
