@@ -120,7 +120,7 @@ __device__ __forceinline__ ff ff_mul(const ff a, const ff b)
 
 // The rare out-of-range cases, out of line: kept off the fast path so that
 // the compiler cannot predicate their FP64-pipe instructions into it.
-__device__ __noinline__ ff split_slow(const double x)
+static __device__ __noinline__ ff split_slow(const double x)
 {
     ff r;
     r.hi = __double2float_rz(x);
@@ -128,7 +128,7 @@ __device__ __noinline__ ff split_slow(const double x)
     return r;
 }
 
-__device__ __noinline__ double join_slow(const float s, const float t)
+static __device__ __noinline__ double join_slow(const float s, const float t)
 {
     return static_cast<double>(s) + static_cast<double>(t);
 }

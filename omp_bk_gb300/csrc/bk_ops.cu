@@ -39,7 +39,18 @@ using Eng = EngMixed;
 #define BK_CAT2(a, b) a##_##b
 #define BK_CAT(a, b) BK_CAT2(a, b)
 
-namespace {
+#ifndef BK_LAYOUT_TU
+#define BK_LAYOUT_TU 9
+#endif
+// A namespace of its own per translation unit: every unit compiles this file,
+// and nvcc may give an anonymous namespace the same name in all of them, so
+// same-named helpers of different engines or layouts would be merged (or
+// clash) at link time.
+#define BK_NS3_(a, b, c) tu_##a##_##b##_##c
+#define BK_NS3(a, b, c) BK_NS3_(a, b, c)
+#define BK_TU_NS BK_NS3(BK_ENGINE_TU, BK_OP_TU, BK_LAYOUT_TU)
+
+namespace BK_TU_NS {
 
 // Elements per block: about 128 lines per sweep (Q^2 lines per element).
 constexpr int default_eb(int q) { return (q * q >= 100) ? 1 : ((q * q >= 64) ? 2 : (128 + q * q - 1) / (q * q)); }
@@ -209,7 +220,8 @@ int bk3adj_q(const double* B, const double* D, long long E, const void* G, const
 }
 #endif  // BK_OP_TU == 7
 
-}  // namespace
+}  // namespace BK_TU_NS
+using namespace BK_TU_NS;
 
 #if BK_OP_TU == 5
 #define BK_CATL_(a, b, c) a##_##b##_L##c
