@@ -1,0 +1,74 @@
+/* bk_solver.h -- C ABI of the batched mixed-order Helmholtz operator and its
+ * CG solver (no reference counterpart: the reference has neither mixed orders
+ * nor a solver).  Return values are bk_status codes (bk_gpu.h).
+ *
+ * Data: the elements of each order are stored one order after another, in
+ * the order of the plan's ranges: u, v, mass (the collocated GLL mass w detJ)
+ * with E_p (p+1)^3 values per order, G with E_p 6 (p+1)^3 values per order in
+ * the column layout G(e, f, k, i, j) (BK_LAYOUT_COLUMN).  The operator is
+ *     v = D^T G D u + lambda mass .* u
+ * (BK5, openmp/BK5.cpp:19-103, plus the diagonal term), orders p = 2..8. */
+#ifndef BK_SOLVER_H
+#define BK_SOLVER_H
+
+#include "bk_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { BK_ERR_NOCONV = 9 };   /* the solver stopped above its tolerance */
+
+typedef struct bk_order_range {
+    int p;               /* polynomial order, 2..8 (q = p + 1 points) */
+    int64_t E;           /* elements of this order */
+    int elems_per_tile;  /* elements per tile of the persistent launch, with
+                            elems_per_tile * q^2 <= 256; 0: 256 / q^2 */
+} bk_order_range;
+
+typedef struct bk_hplan* bk_hplan_t;
+
+/* A plan over norders (1..7) ranges; D[r] is the host (p+1) x (p+1) GLL
+ * derivative of range r, D(i,n) = D[r][i*q + n].  Allocates the tile list
+ * and the solver's work vectors on the current device (once, here: the
+ * applies and solves allocate nothing).  Synchronizes `stream`. */
+int bk_hplan_create(bk_hplan_t* plan, int norders, const bk_order_range* orders, const double* const* D,
+                    bk_stream_t stream);
+int bk_hplan_destroy(bk_hplan_t plan);
+/* what = 0: values of a vector (sum E_p q^3); 1: values of G; 2: tiles. */
+long long bk_hplan_size(bk_hplan_t plan, int what);
+
+/* v = A u for all orders in ONE persistent launch.  prec BK_PREC_FP64 (engine
+ * AUTO/FF: float-float, DFMA: native), BK_PREC_MIXED or BK_PREC_FP32 (float
+ * storage).  mass may be NULL (plain BK5). */
+int bk_hplan_apply(bk_hplan_t plan, const void* G, const void* mass, double lambda, const void* u, void* v,
+                   int prec, int engine, bk_stream_t stream);
+
+typedef struct bk_cg_options {
+    double rtol;        /* stop at |f - A x| <= rtol |f| (FP64 residual); default 1e-10 */
+    int max_outer;      /* refinement steps; default 8 */
+    double inner_rtol;  /* inner FP32 CG tolerance (relative); default 1e-5 */
+    int max_inner;      /* inner iterations per refinement step; default 10000 */
+} bk_cg_options;
+
+typedef struct bk_cg_stats {
+    int outer;          /* refinement steps taken */
+    int inner;          /* inner CG iterations, all steps */
+    double relres;      /* final |f - A x| / |f| in FP64 */
+} bk_cg_stats;
+
+/* Solves A x = f (x holds the initial guess; f, x FP64 device vectors).
+ * The residual is formed in FP64 with G64/mass64 (double); the inner CG
+ * applies the FP32-storage operator G32/mass32 (float) with FP64 dot
+ * products, its iterations captured once per operator in a CUDA graph with a
+ * conditional WHILE node (no host round trip inside a solve).  Returns BK_OK,
+ * BK_ERR_NOCONV if rtol was not reached, or an error.  opt, stats may be NULL. */
+int bk_hplan_cg(bk_hplan_t plan, const void* G64, const void* mass64, const void* G32, const void* mass32,
+                double lambda, const double* f, double* x, const bk_cg_options* opt, bk_cg_stats* stats,
+                bk_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BK_SOLVER_H */

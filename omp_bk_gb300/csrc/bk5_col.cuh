@@ -116,6 +116,10 @@ __device__ __forceinline__ void bk5_col_batch(const typename Eng::C* __restrict_
     const int i = c / Q;
     const int j = c - i * Q;
     const bool active = el < ne;
+    // lambda in the working type, tested once (an FP64 compare per point
+    // would queue on the FP64 pipe)
+    const bool lam_scaled = (mb != nullptr) && (lambda != 1.0);
+    const V lam = Eng::load(S(lambda));
     // with GDIR, the G of this thread's column, loaded from HBM before the
     // derivatives so that the loads are in flight while they are computed
     typename Eng::S gcol[GDIR ? F : 1][GDIR ? Q : 1];
@@ -252,7 +256,7 @@ __device__ __forceinline__ void bk5_col_batch(const typename Eng::C* __restrict_
                 A am = Eng::zero();
                 Eng::add(am, res);
                 V m = Eng::load(mo[k]);
-                if (lambda != 1.0) m = Eng::mul(Eng::load(S(lambda)), m);
+                if (lam_scaled) m = Eng::mul(lam, m);
                 Eng::vmadd(am, m, ucol[k]);
                 res = Eng::result(am);
             }

@@ -1,0 +1,175 @@
+// bk5_multi.cuh -- one persistent launch over elements of mixed orders.
+//
+// The elements of each order q = p + 1 (3..9) form a segment; a segment is
+// cut into tiles of eb_q elements (eb_q chosen per order by the autotuner),
+// and the tiles of all segments form one work list.  Block b of the grid
+// takes tiles b, b + gridDim.x, ... (the list is ordered by decreasing cost,
+// so every block gets a similar mix of orders), stages each tile's u (and G
+// for the FP64 engines) by TMA into one of two stage buffers, prefetching the
+// block's next tile while it computes, and runs the column batch body of
+// bk5_col.cuh for the tile's order.  The operator is BK5 plus lambda times the
+// collocated mass (the Helmholtz operator), G in the column layout
+// G(e, f, k, i, j).
+#pragma once
+
+#include "bk5_col.cuh"
+
+namespace bkg {
+
+constexpr int kMultiQmin = 3;
+constexpr int kMultiQmax = 9;
+constexpr int kMultiNQ = kMultiQmax - kMultiQmin + 1;
+
+struct MultiSeg {
+    int q;               // points per direction
+    int eb;              // elements per tile
+    long long E;         // elements of the segment
+    long long uoff;      // offset (values) of the segment in u, v and mass
+    long long goff;      // offset (values) of the segment in G
+};
+
+struct MultiTile {
+    int seg;
+    int ne;
+    long long e_first;   // first element, within the segment
+};
+
+// offset of D_q in the concatenation of D_3 .. D_9
+constexpr int multi_doff(int q)
+{
+    int o = 0;
+    for (int r = kMultiQmin; r < q; ++r) o += r * r;
+    return o;
+}
+constexpr int kMultiDTotal = multi_doff(kMultiQmax + 1);
+
+template <class C>
+struct PMulti {
+    C D[kMultiDTotal];          // D_q(i, n) at multi_doff(q) + i*q + n
+    MultiSeg seg[kMultiNQ];
+    int nseg;
+};
+
+// G is staged by TMA here (not held in registers): the kernel carries the
+// bodies of all seven orders and must fit two blocks per SM.
+template <class Eng, int NT, int NBUF>
+__global__ void __launch_bounds__(NT, 2)
+    bk5_multi_kernel(const __grid_constant__ PMulti<typename Eng::C> prm, const MultiTile* __restrict__ tiles,
+                     const int ntiles, const typename Eng::S* __restrict__ u, const typename Eng::S* __restrict__ G,
+                     const typename Eng::S* __restrict__ mass, const double lambda, typename Eng::S* __restrict__ v,
+                     const int stage_bytes_, const int col_bytes, const DevCtx ctx)
+{
+    using S = typename Eng::S;
+    using V = typename Eng::V;
+    constexpr bool GDIR = false;
+    extern __shared__ __align__(16) unsigned char smem[];
+    unsigned char* stage0 = smem;
+    V* UV = reinterpret_cast<V*>(smem + NBUF * stage_bytes_);
+    V* R0 = reinterpret_cast<V*>(reinterpret_cast<unsigned char*>(UV) + col_bytes);
+    V* R1 = reinterpret_cast<V*>(reinterpret_cast<unsigned char*>(R0) + col_bytes);
+    V* Ds = reinterpret_cast<V*>(reinterpret_cast<unsigned char*>(R1) + col_bytes);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(reinterpret_cast<unsigned char*>(Ds) +
+                                                 ((kMultiDTotal * int(sizeof(V)) + 15) / 16) * 16);
+    const int tid = threadIdx.x;
+
+    for (int x = tid; x < kMultiDTotal; x += NT) Ds[x] = prm.D[x];
+    if (tid == 0) {
+        for (int b = 0; b < NBUF; ++b) mbar_init(&bars[b], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+
+    const int stride = gridDim.x;
+    const S* us_slot0 = nullptr;
+    const S* us_slot1 = nullptr;
+    const S* gs_slot0 = nullptr;
+    const S* gs_slot1 = nullptr;
+
+    auto issue = [&](int t, int sb) {
+        const MultiTile tl = tiles[t];
+        const MultiSeg& sg = prm.seg[tl.seg];
+        const int q3 = sg.q * sg.q * sg.q;
+        unsigned char* st = stage0 + sb * stage_bytes_;
+        uint32_t tx = 0;
+        if (tid == 0) fence_proxy_async();
+        const S* us_ = stage_issue<S>(st, u + sg.uoff + tl.e_first * q3, tl.ne * q3, &bars[sb], tx, tid, NT);
+        const S* gs_ = nullptr;
+        if constexpr (!GDIR) {
+            // the G stage follows the u stage of the largest tile
+            const int ub = ((tl.ne * q3 * int(sizeof(S)) + 15) / 16) * 16 + 16;
+            gs_ = stage_issue<S>(st + ub, G + sg.goff + tl.e_first * 6 * q3, tl.ne * 6 * q3, &bars[sb], tx, tid, NT);
+        }
+        if (sb == 0) {
+            us_slot0 = us_;
+            gs_slot0 = gs_;
+        } else {
+            us_slot1 = us_;
+            gs_slot1 = gs_;
+        }
+        if (tid == 0) mbar_arrive_expect_tx(&bars[sb], tx);
+    };
+
+    for (int b = 0; b < NBUF; ++b) {
+        const int t = blockIdx.x + b * stride;
+        if (t < ntiles) issue(t, b);
+    }
+    int it = 0;
+    for (int t = blockIdx.x; t < ntiles; t += stride, ++it) {
+        const int sb = it % NBUF;
+        const uint32_t parity = uint32_t(it / NBUF) & 1u;
+        if (batch_wait_failed(&bars[sb], parity, ctx, tid)) return;
+        const MultiTile tl = tiles[t];
+        const MultiSeg& sg = prm.seg[tl.seg];
+        const int q3 = sg.q * sg.q * sg.q;
+        const S* ub = (sb == 0) ? us_slot0 : us_slot1;
+        const S* gb = GDIR ? G + sg.goff + tl.e_first * 6 * q3 : ((sb == 0) ? gs_slot0 : gs_slot1);
+        S* vb = v + sg.uoff + tl.e_first * q3;
+        const S* mb = (mass != nullptr) ? mass + sg.uoff + tl.e_first * q3 : nullptr;
+        auto after = [&]() {
+            const int tn = t + NBUF * stride;
+            if (tn < ntiles) issue(tn, sb);
+        };
+        switch (sg.q) {
+#define BK_MULTI_CASE(QQ)                                                                                       \
+    case QQ:                                                                                                    \
+        bk5_col_batch<Eng, QQ, 6, 2, GDIR>(prm.D + multi_doff(QQ), Ds + multi_doff(QQ), ub, gb, UV, R0, R1,   \
+                                           nullptr, tl.ne, tid, NT, vb, mb, lambda, after);                    \
+        break;
+            BK_MULTI_CASE(3)
+            BK_MULTI_CASE(4)
+            BK_MULTI_CASE(5)
+            BK_MULTI_CASE(6)
+            BK_MULTI_CASE(7)
+            BK_MULTI_CASE(8)
+            BK_MULTI_CASE(9)
+#undef BK_MULTI_CASE
+            default:
+                break;
+        }
+    }
+}
+
+// Shared-memory sizes of a launch over the segments: one stage buffer (the
+// largest tile's u, and G when staged) and one padded column buffer.
+template <class Eng>
+inline void multi_smem(const MultiSeg* seg, int nseg, int& stage_bytes_, int& col_bytes, int& total, int nbuf)
+{
+    using S = typename Eng::S;
+    using V = typename Eng::V;
+    constexpr bool GDIR = false;
+    stage_bytes_ = 16;
+    col_bytes = 16;
+    for (int s = 0; s < nseg; ++s) {
+        const int q = seg[s].q, eb = seg[s].eb, q3 = q * q * q;
+        int st = ((eb * q3 * int(sizeof(S)) + 15) / 16) * 16 + 16;
+        if (!GDIR) st += ((eb * 6 * q3 * int(sizeof(S)) + 15) / 16) * 16 + 16;
+        if (st > stage_bytes_) stage_bytes_ = st;
+        const int cb = eb * q * q * col_rs(q, int(sizeof(V))) * int(sizeof(V));
+        if (cb > col_bytes) col_bytes = cb;
+    }
+    stage_bytes_ = (stage_bytes_ + 15) / 16 * 16;
+    col_bytes = (col_bytes + 15) / 16 * 16;
+    total = nbuf * stage_bytes_ + 3 * col_bytes + ((kMultiDTotal * int(sizeof(V)) + 15) / 16) * 16 + 16 * nbuf;
+}
+
+}  // namespace bkg

@@ -1,0 +1,584 @@
+// bk_helmholtz.cu -- batched mixed-order Helmholtz operator and its CG solver.
+//
+// A plan describes elements of several orders p (2..8; BK5 points q = p + 1)
+// stored one order after another (u, v, mass: E_p q^3 values each; G: E_p 6
+// q^3 values in the column layout), cut into tiles whose sizes per order
+// come from the caller (the autotuner of omp_bk_gb300.tune).  The apply
+// v = D^T G D u + lambda mass u is ONE persistent launch over the tile list
+// (bk5_multi.cuh).
+//
+// The solver is conjugate gradients in mixed precision with FP64 residual
+// refinement: the outer loop forms the FP64 residual r = f - A x with the
+// FP64-accurate apply (float-float engine, FP64 storage) and stops at
+// |r| <= rtol |f|; the inner loop solves A d = r / |r| approximately with CG
+// on the FP32-storage operator (mixed engine), FP32 vectors and FP64 dot
+// products, and x += |r| d.  The inner CG is captured once in a CUDA graph:
+// its iteration (apply, dot, updates, next direction) is the body of a
+// conditional WHILE node whose condition a device kernel sets from the
+// residual, so the whole inner solve is one graph launch with no host round
+// trip.  The reference has no solver; this is the standard preconditioner-free
+// CG (Hestenes-Stiefel) with iterative refinement.
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "bk5_multi.cuh"
+#include "bk_internal.h"
+#include "bk_solver.h"
+
+namespace bkg {
+namespace {
+
+constexpr int kNT = 256;   // threads per block of the persistent kernel
+constexpr int kRedBlocks = 608;
+constexpr int kRedThreads = 256;
+
+enum Scalar { S_RR = 0, S_RR0, S_PAP, S_IT, S_TOL2, S_MAXIT, S_NORM, S_INV, S_RN2, S_FN2, S_NSCAL };
+
+template <class Eng, int NBUF>
+struct MultiLaunch {
+    static int run(const PMulti<typename Eng::C>& prm, const MultiTile* tiles, int ntiles, const void* u,
+                   const void* G, const void* mass, double lambda, void* v, cudaStream_t s)
+    {
+        using S = typename Eng::S;
+        int st = 0, cb = 0, total = 0;
+        multi_smem<Eng>(prm.seg, prm.nseg, st, cb, total, NBUF);
+        if (total > 232448) return BK_ERR_ARG;
+        auto kern = bk5_multi_kernel<Eng, kNT, NBUF>;
+        // the attribute is raised to the largest size any plan has needed
+        static int set_bytes[kMaxDevices] = {0};
+        const int dev = current_device();
+        if (dev < 0 || dev >= kMaxDevices) return BK_ERR_CUDA;
+        if (total > set_bytes[dev]) {
+            if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448) != cudaSuccess)
+                return BK_ERR_CUDA;
+            set_bytes[dev] = 232448;
+        }
+        int occ = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kNT, total) != cudaSuccess || occ < 1)
+            return BK_ERR_CUDA;
+        int grid = occ * sm_count();
+        if (grid > ntiles) grid = ntiles;
+        if (grid < 1) return BK_OK;
+        kern<<<grid, kNT, total, s>>>(prm, tiles, ntiles, static_cast<const S*>(u), static_cast<const S*>(G),
+                                      static_cast<const S*>(mass), lambda, static_cast<S*>(v), st, cb, dev_ctx());
+        return cudaGetLastError() == cudaSuccess ? BK_OK : BK_ERR_CUDA;
+    }
+};
+
+// ---- CG kernels --------------------------------------------------------------
+
+__global__ void cg_start_kernel(long long n, const double* __restrict__ r64, const double* __restrict__ sc,
+                                float* __restrict__ r, float* __restrict__ p, float* __restrict__ d)
+{
+    const double inv = sc[S_INV];
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float x = float(r64[i] * inv);
+        r[i] = x;
+        p[i] = x;
+        d[i] = 0.0f;
+    }
+}
+
+// partial sums of x.y (FP64) per block
+__global__ void __launch_bounds__(kRedThreads) red_dot_kernel(long long n, const float* __restrict__ x,
+                                                              const float* __restrict__ y, double* __restrict__ part)
+{
+    __shared__ double sh[kRedThreads];
+    double s = 0.0;
+    for (long long i = blockIdx.x * (long long)kRedThreads + threadIdx.x; i < n; i += (long long)gridDim.x * kRedThreads)
+        s = fma(double(x[i]), double(y[i]), s);
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = kRedThreads / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+__device__ __forceinline__ double block_sum(const double* __restrict__ part, int nb)
+{
+    __shared__ double sh[kRedThreads];
+    double s = 0.0;
+    for (int i = threadIdx.x; i < nb; i += kRedThreads) s += part[i];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = kRedThreads / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    return sh[0];
+}
+
+// scalars after the first r.r: rr0 = rr, it = 0
+__global__ void __launch_bounds__(kRedThreads) cg_init_scalars_kernel(const double* __restrict__ part, int nb,
+                                                                      double* __restrict__ sc)
+{
+    const double rr = block_sum(part, nb);
+    if (threadIdx.x == 0) {
+        sc[S_RR] = rr;
+        sc[S_RR0] = rr;
+        sc[S_IT] = 0.0;
+    }
+}
+
+__global__ void __launch_bounds__(kRedThreads) cg_pap_kernel(const double* __restrict__ part, int nb,
+                                                             double* __restrict__ sc)
+{
+    const double pap = block_sum(part, nb);
+    if (threadIdx.x == 0) sc[S_PAP] = pap;
+}
+
+// d += alpha p, r -= alpha Ap and the partial sums of r.r
+__global__ void __launch_bounds__(kRedThreads) cg_update_kernel(long long n, const double* __restrict__ sc,
+                                                                const float* __restrict__ p,
+                                                                const float* __restrict__ Ap, float* __restrict__ d,
+                                                                float* __restrict__ r, double* __restrict__ part)
+{
+    __shared__ double sh[kRedThreads];
+    const double pap = sc[S_PAP];
+    const float alpha = float(pap != 0.0 ? sc[S_RR] / pap : 0.0);
+    double s = 0.0;
+    for (long long i = blockIdx.x * (long long)kRedThreads + threadIdx.x; i < n; i += (long long)gridDim.x * kRedThreads) {
+        d[i] = fmaf(alpha, p[i], d[i]);
+        const float ri = fmaf(-alpha, Ap[i], r[i]);
+        r[i] = ri;
+        s = fma(double(ri), double(ri), s);
+    }
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = kRedThreads / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+// rr_new, beta, iteration count and the loop condition
+__global__ void __launch_bounds__(kRedThreads) cg_step_kernel(const double* __restrict__ part, int nb,
+                                                              double* __restrict__ sc, double* __restrict__ beta_out,
+                                                              cudaGraphConditionalHandle handle)
+{
+    const double rr = block_sum(part, nb);
+    if (threadIdx.x == 0) {
+        const double old = sc[S_RR];
+        beta_out[0] = old != 0.0 ? rr / old : 0.0;
+        sc[S_RR] = rr;
+        const double it = sc[S_IT] + 1.0;
+        sc[S_IT] = it;
+        const bool go = (rr > sc[S_TOL2] * sc[S_RR0]) && (it < sc[S_MAXIT]);
+        cudaGraphSetConditional(handle, go ? 1u : 0u);
+    }
+}
+
+__global__ void cg_dir_kernel(long long n, const double* __restrict__ beta_in, const float* __restrict__ r,
+                              float* __restrict__ p)
+{
+    const float beta = float(beta_in[0]);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        p[i] = fmaf(beta, p[i], r[i]);
+}
+
+// x += |r| d (FP64), the norm from the scalars
+__global__ void cg_correct_kernel(long long n, const double* __restrict__ sc, const float* __restrict__ d,
+                                  double* __restrict__ x)
+{
+    const double nrm = sc[S_NORM];
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        x[i] = fma(nrm, double(d[i]), x[i]);
+}
+
+// r = f - r (the apply wrote A x into r); partial sums of r.r
+__global__ void __launch_bounds__(kRedThreads) res64_kernel(long long n, const double* __restrict__ f,
+                                                            double* __restrict__ r, double* __restrict__ part)
+{
+    __shared__ double sh[kRedThreads];
+    double s = 0.0;
+    for (long long i = blockIdx.x * (long long)kRedThreads + threadIdx.x; i < n; i += (long long)gridDim.x * kRedThreads) {
+        const double ri = f[i] - r[i];
+        r[i] = ri;
+        s = fma(ri, ri, s);
+    }
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = kRedThreads / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+__global__ void __launch_bounds__(kRedThreads) norm_kernel(const double* __restrict__ part, int nb,
+                                                           double* __restrict__ sc)
+{
+    const double rn2 = block_sum(part, nb);
+    if (threadIdx.x == 0) {
+        sc[S_RN2] = rn2;
+        const double nrm = sqrt(rn2);
+        sc[S_NORM] = nrm;
+        sc[S_INV] = nrm > 0.0 ? 1.0 / nrm : 0.0;
+    }
+}
+
+__global__ void __launch_bounds__(kRedThreads) dot64_partial_kernel(long long n, const double* __restrict__ x,
+                                                                    const double* __restrict__ y,
+                                                                    double* __restrict__ part)
+{
+    __shared__ double sh[kRedThreads];
+    double s = 0.0;
+    for (long long i = blockIdx.x * (long long)kRedThreads + threadIdx.x; i < n; i += (long long)gridDim.x * kRedThreads)
+        s = fma(x[i], y[i], s);
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = kRedThreads / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+__global__ void __launch_bounds__(kRedThreads) sum_to_kernel(const double* __restrict__ part, int nb,
+                                                             double* __restrict__ out)
+{
+    const double v = block_sum(part, nb);
+    if (threadIdx.x == 0) out[0] = v;
+}
+
+int grid_n(long long n)
+{
+    const long long g = (n + 1023) / 1024;
+    return int(g < 1216 ? (g > 0 ? g : 1) : 1216);
+}
+
+}  // namespace
+}  // namespace bkg
+
+using namespace bkg;
+
+struct bk_hplan {
+    int device;
+    int nseg;
+    MultiSeg seg[kMultiNQ];
+    std::vector<MultiTile> htiles;
+    MultiTile* tiles;   // device
+    int ntiles;
+    long long n;        // values of a vector
+    long long ng;       // values of G
+    PMulti<double> p_dfma;
+    PMulti<ff> p_ff;
+    PMulti<float> p_f32;
+    // solver state
+    double* r64;
+    float* r32;
+    float* p32;
+    float* Ap32;
+    float* d32;
+    double* part;
+    double* sc;
+    double* beta;
+    cudaGraphExec_t inner_exec;
+    cudaGraph_t inner_graph;
+    const void* g_key[3];   // operator pointers the graph was built for
+    double key_lambda;
+};
+
+namespace {
+
+template <class C>
+void fill_params(PMulti<C>& P, const bk_hplan& h, const double* const* Dq, C (*conv)(double))
+{
+    std::memset(&P, 0, sizeof(P));
+    for (int s = 0; s < h.nseg; ++s) {
+        const int q = h.seg[s].q;
+        for (int x = 0; x < q * q; ++x) P.D[multi_doff(q) + x] = conv(Dq[s][x]);
+        P.seg[s] = h.seg[s];
+    }
+    P.nseg = h.nseg;
+}
+
+double conv_d(double x) { return x; }
+float conv_f(double x) { return float(x); }
+ff conv_ff(double x) { return EngFF::coef(x); }
+
+int apply_plan(bk_hplan* h, int eng, const void* G, const void* mass, double lambda, const void* u, void* v,
+               cudaStream_t s)
+{
+    switch (eng) {
+        case 0: return MultiLaunch<EngDfma, 1>::run(h->p_dfma, h->tiles, h->ntiles, u, G, mass, lambda, v, s);
+        case 1: return MultiLaunch<EngFF, 1>::run(h->p_ff, h->tiles, h->ntiles, u, G, mass, lambda, v, s);
+        case 2: return MultiLaunch<EngF32, 2>::run(h->p_f32, h->tiles, h->ntiles, u, G, mass, lambda, v, s);
+        default: return MultiLaunch<EngMixed, 2>::run(h->p_f32, h->tiles, h->ntiles, u, G, mass, lambda, v, s);
+    }
+}
+
+int ck(cudaError_t e) { return e == cudaSuccess ? BK_OK : BK_ERR_CUDA; }
+
+void free_graph(bk_hplan* h)
+{
+    if (h->inner_exec) cudaGraphExecDestroy(h->inner_exec);
+    if (h->inner_graph) cudaGraphDestroy(h->inner_graph);
+    h->inner_exec = nullptr;
+    h->inner_graph = nullptr;
+}
+
+// The inner CG as a graph: start, r.r, then WHILE(cond) { A p, p.Ap, update,
+// step (sets cond), new direction }.
+int build_inner_graph(bk_hplan* h, const void* G32, const void* mass32, double lambda, cudaStream_t s)
+{
+    free_graph(h);
+    cudaGraph_t g = nullptr;
+    if (cudaGraphCreate(&g, 0) != cudaSuccess) return BK_ERR_CUDA;
+    cudaGraphConditionalHandle handle;
+    if (cudaGraphConditionalHandleCreate(&handle, g, 1, cudaGraphCondAssignDefault) != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return BK_ERR_CUDA;
+    }
+    const long long n = h->n;
+    const int gn = grid_n(n);
+    // prologue, captured into g
+    int rc = BK_OK;
+    if (cudaStreamBeginCaptureToGraph(s, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return BK_ERR_CUDA;
+    }
+    cg_start_kernel<<<gn, 256, 0, s>>>(n, h->r64, h->sc, h->r32, h->p32, h->d32);
+    red_dot_kernel<<<kRedBlocks, kRedThreads, 0, s>>>(n, h->r32, h->r32, h->part);
+    cg_init_scalars_kernel<<<1, kRedThreads, 0, s>>>(h->part, kRedBlocks, h->sc);
+    cudaGraph_t captured = nullptr;
+    if (cudaStreamEndCapture(s, &captured) != cudaSuccess) rc = BK_ERR_CUDA;
+    // the WHILE node after the prologue
+    cudaGraphNode_t leaf = nullptr;
+    if (rc == BK_OK) {
+        size_t nn = 0;
+        cudaGraphGetNodes(g, nullptr, &nn);
+        std::vector<cudaGraphNode_t> nodes(nn);
+        cudaGraphGetNodes(g, nodes.data(), &nn);
+        for (cudaGraphNode_t nd : nodes) {
+            size_t ndep = 0;
+            cudaGraphNodeGetDependentNodes(nd, nullptr, nullptr, &ndep);
+            if (ndep == 0) leaf = nd;
+        }
+        cudaGraphNodeParams cp = {};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = handle;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t cnode;
+        if (cudaGraphAddNode(&cnode, g, leaf ? &leaf : nullptr, nullptr, leaf ? 1 : 0, &cp) != cudaSuccess) {
+            rc = BK_ERR_CUDA;
+        } else {
+            cudaGraph_t body = cp.conditional.phGraph_out[0];
+            if (cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) !=
+                cudaSuccess) {
+                rc = BK_ERR_CUDA;
+            } else {
+                int arc = apply_plan(h, 3, G32, mass32, lambda, h->p32, h->Ap32, s);
+                red_dot_kernel<<<kRedBlocks, kRedThreads, 0, s>>>(n, h->p32, h->Ap32, h->part);
+                cg_pap_kernel<<<1, kRedThreads, 0, s>>>(h->part, kRedBlocks, h->sc);
+                cg_update_kernel<<<kRedBlocks, kRedThreads, 0, s>>>(n, h->sc, h->p32, h->Ap32, h->d32, h->r32,
+                                                                    h->part);
+                cg_step_kernel<<<1, kRedThreads, 0, s>>>(h->part, kRedBlocks, h->sc, h->beta, handle);
+                cg_dir_kernel<<<gn, 256, 0, s>>>(n, h->beta, h->r32, h->p32);
+                cudaGraph_t body_out = nullptr;
+                if (cudaStreamEndCapture(s, &body_out) != cudaSuccess || arc != BK_OK) rc = BK_ERR_CUDA;
+            }
+        }
+    }
+    if (rc == BK_OK && cudaGraphInstantiate(&h->inner_exec, g, 0) != cudaSuccess) rc = BK_ERR_CUDA;
+    if (rc != BK_OK) {
+        cudaGetLastError();
+        cudaGraphDestroy(g);
+        h->inner_exec = nullptr;
+        return rc;
+    }
+    h->inner_graph = g;
+    h->g_key[0] = G32;
+    h->g_key[1] = mass32;
+    h->key_lambda = lambda;
+    return BK_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bk_hplan_create(bk_hplan_t* out, int norders, const bk_order_range* orders, const double* const* D,
+                    bk_stream_t stream)
+{
+    if (!out || !orders || !D) return BK_ERR_NULL;
+    *out = nullptr;
+    if (norders < 1 || norders > kMultiNQ) return BK_ERR_ARG;
+    bk_hplan* h = new bk_hplan();
+    std::memset(h->seg, 0, sizeof(h->seg));
+    h->device = current_device();
+    h->nseg = norders;
+    long long uo = 0, go = 0;
+    for (int s = 0; s < norders; ++s) {
+        const int p = orders[s].p;
+        if (p < kMultiQmin - 1 || p > kMultiQmax - 1) {
+            delete h;
+            return BK_ERR_ORDER;
+        }
+        const int q = p + 1;
+        int eb = orders[s].elems_per_tile;
+        if (eb <= 0) eb = (kNT / (q * q)) > 0 ? kNT / (q * q) : 1;
+        if (eb * q * q > kNT || orders[s].E < 0 || !D[s]) {
+            delete h;
+            return orders[s].E < 0 ? BK_ERR_SIZE : BK_ERR_ARG;
+        }
+        h->seg[s].q = q;
+        h->seg[s].eb = eb;
+        h->seg[s].E = orders[s].E;
+        h->seg[s].uoff = uo;
+        h->seg[s].goff = go;
+        uo += orders[s].E * q * q * q;
+        go += orders[s].E * 6 * q * q * q;
+    }
+    h->n = uo;
+    h->ng = go;
+    // tiles, most expensive order first
+    std::vector<int> order(norders);
+    for (int s = 0; s < norders; ++s) order[s] = s;
+    for (int a = 0; a < norders; ++a)
+        for (int b = a + 1; b < norders; ++b)
+            if (h->seg[order[b]].q > h->seg[order[a]].q) std::swap(order[a], order[b]);
+    for (int s : order) {
+        for (long long e = 0; e < h->seg[s].E; e += h->seg[s].eb) {
+            MultiTile t;
+            t.seg = s;
+            t.ne = int((h->seg[s].E - e) < h->seg[s].eb ? (h->seg[s].E - e) : h->seg[s].eb);
+            t.e_first = e;
+            h->htiles.push_back(t);
+        }
+    }
+    h->ntiles = int(h->htiles.size());
+    fill_params(h->p_dfma, *h, D, conv_d);
+    fill_params(h->p_ff, *h, D, conv_ff);
+    fill_params(h->p_f32, *h, D, conv_f);
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    int rc = BK_OK;
+    const size_t nb = size_t(h->n);
+    rc |= ck(cudaMalloc(&h->tiles, sizeof(MultiTile) * (h->ntiles > 0 ? h->ntiles : 1)));
+    rc |= ck(cudaMalloc(&h->r64, 8 * (nb + 1)));
+    rc |= ck(cudaMalloc(&h->r32, 4 * (nb + 4)));
+    rc |= ck(cudaMalloc(&h->p32, 4 * (nb + 4)));
+    rc |= ck(cudaMalloc(&h->Ap32, 4 * (nb + 4)));
+    rc |= ck(cudaMalloc(&h->d32, 4 * (nb + 4)));
+    rc |= ck(cudaMalloc(&h->part, 8 * kRedBlocks));
+    rc |= ck(cudaMalloc(&h->sc, 8 * S_NSCAL));
+    rc |= ck(cudaMalloc(&h->beta, 8 * 2));
+    if (rc == BK_OK && h->ntiles > 0)
+        rc = ck(cudaMemcpyAsync(h->tiles, h->htiles.data(), sizeof(MultiTile) * h->ntiles, cudaMemcpyHostToDevice, s));
+    if (rc == BK_OK) rc = ck(cudaStreamSynchronize(s));
+    if (rc != BK_OK) {
+        bk_hplan_destroy(h);
+        return BK_ERR_CUDA;
+    }
+    *out = h;
+    return BK_OK;
+}
+
+int bk_hplan_destroy(bk_hplan_t h)
+{
+    if (!h) return BK_OK;
+    free_graph(h);
+    cudaFree(h->tiles);
+    cudaFree(h->r64);
+    cudaFree(h->r32);
+    cudaFree(h->p32);
+    cudaFree(h->Ap32);
+    cudaFree(h->d32);
+    cudaFree(h->part);
+    cudaFree(h->sc);
+    cudaFree(h->beta);
+    delete h;
+    return BK_OK;
+}
+
+long long bk_hplan_size(bk_hplan_t h, int what)
+{
+    if (!h) return -1;
+    if (what == 0) return h->n;
+    if (what == 1) return h->ng;
+    if (what == 2) return h->ntiles;
+    return -1;
+}
+
+int bk_hplan_apply(bk_hplan_t h, const void* G, const void* mass, double lambda, const void* u, void* v, int prec,
+                   int engine, bk_stream_t stream)
+{
+    if (!h) return BK_ERR_NULL;
+    if (h->n == 0) return BK_OK;
+    if (!G || !u || !v) return BK_ERR_NULL;
+    if ((reinterpret_cast<uintptr_t>(G) | reinterpret_cast<uintptr_t>(u) | reinterpret_cast<uintptr_t>(v) |
+         reinterpret_cast<uintptr_t>(mass)) & 15)
+        return BK_ERR_ALIGN;
+    int eng;
+    if (prec == BK_PREC_FP32) eng = 2;
+    else if (prec == BK_PREC_MIXED) eng = 3;
+    else if (prec == BK_PREC_FP64) eng = (engine == BK_ENGINE_DFMA) ? 0 : 1;
+    else return BK_ERR_PREC;
+    if (prec == BK_PREC_FP64 && engine != BK_ENGINE_AUTO && engine != BK_ENGINE_DFMA && engine != BK_ENGINE_FF)
+        return BK_ERR_PREC;
+    if (dev_ctx().status == nullptr) return BK_ERR_CUDA;
+    return apply_plan(h, eng, G, mass, lambda, u, v, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int bk_hplan_cg(bk_hplan_t h, const void* G64, const void* mass64, const void* G32, const void* mass32,
+                double lambda, const double* f, double* x, const bk_cg_options* opt, bk_cg_stats* stats,
+                bk_stream_t stream)
+{
+    if (!h || !f || !x || !G64 || !G32) return BK_ERR_NULL;
+    bk_cg_options o;
+    o.rtol = 1e-10;
+    o.max_outer = 8;
+    o.inner_rtol = 1e-5;
+    o.max_inner = 10000;
+    if (opt) o = *opt;
+    if (!(o.rtol > 0) || !(o.inner_rtol > 0) || o.max_outer < 1 || o.max_inner < 1) return BK_ERR_ARG;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const long long n = h->n;
+    int rc;
+    if (dev_ctx().status == nullptr) return BK_ERR_CUDA;
+    if (!h->inner_exec || h->g_key[0] != G32 || h->g_key[1] != mass32 || h->key_lambda != lambda) {
+        if ((rc = build_inner_graph(h, G32, mass32, lambda, s))) return rc;
+    }
+    const double sc_init[2] = {o.inner_rtol * o.inner_rtol, double(o.max_inner)};
+    if ((rc = ck(cudaMemcpyAsync(h->sc + S_TOL2, sc_init, 2 * sizeof(double), cudaMemcpyHostToDevice, s)))) return rc;
+    // |f|^2
+    dot64_partial_kernel<<<kRedBlocks, kRedThreads, 0, s>>>(n, f, f, h->part);
+    sum_to_kernel<<<1, kRedThreads, 0, s>>>(h->part, kRedBlocks, h->sc + S_FN2);
+    double hs[S_NSCAL];
+    int outer = 0, inner_total = 0;
+    double relres = 0.0;
+    for (;;) {
+        // r = f - A x (FP64-accurate apply), |r|
+        if ((rc = apply_plan(h, 1, G64, mass64, lambda, x, h->r64, s))) return rc;
+        res64_kernel<<<kRedBlocks, kRedThreads, 0, s>>>(n, f, h->r64, h->part);
+        norm_kernel<<<1, kRedThreads, 0, s>>>(h->part, kRedBlocks, h->sc);
+        if ((rc = ck(cudaMemcpyAsync(hs, h->sc, sizeof(hs), cudaMemcpyDeviceToHost, s)))) return rc;
+        if ((rc = ck(cudaStreamSynchronize(s)))) return rc;
+        if (outer > 0) inner_total += int(hs[S_IT]);
+        relres = hs[S_FN2] > 0 ? std::sqrt(hs[S_RN2] / hs[S_FN2]) : std::sqrt(hs[S_RN2]);
+        if (relres <= o.rtol || outer >= o.max_outer || !(relres == relres)) break;
+        // inner solve A d = r / |r| in FP32 (one graph launch), x += |r| d
+        if ((rc = ck(cudaGraphLaunch(h->inner_exec, s)))) return rc;
+        cg_correct_kernel<<<grid_n(n), 256, 0, s>>>(n, h->sc, h->d32, x);
+        ++outer;
+    }
+    if (stats) {
+        stats->outer = outer;
+        stats->inner = inner_total;
+        stats->relres = relres;
+    }
+    int st = 0;
+    if ((rc = bk_device_status(&st, 0, stream))) return rc;
+    if (st != BK_OK) return st;
+    return relres <= o.rtol ? BK_OK : BK_ERR_NOCONV;
+}
+
+}  // extern "C"

@@ -1,0 +1,113 @@
+"""The batched mixed-order Helmholtz operator (one persistent launch over
+orders p = 2..8) and its mixed-precision CG with FP64 refinement.
+
+  - the persistent apply equals the per-order BK5 apply with the mass term
+    (FP64: < 1e-12 relative; FP32 storage: < 1e-5) and the oracle's FP64
+    BK5 + lambda mass (oracle/bk_oracle.c);
+  - CG reaches |f - A x| <= 1e-10 |f| (FP64 residual), checked again with the
+    oracle's FP64 operator on the host.
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from gpu_util import host
+
+pytestmark = pytest.mark.gpu
+
+
+def _slices(plan, k):
+    q = plan.p[k] + 1
+    E = plan.E[k]
+    return (slice(plan.uoff[k], plan.uoff[k] + E * q ** 3), slice(plan.goff[k], plan.goff[k] + 6 * E * q ** 3))
+
+
+def _col_to_interleaved(Gc, E, q):
+    """G(e, f, k, i, j) -> G(e, i, j, f, k)."""
+    return np.ascontiguousarray(Gc.reshape(E, 6, q, q, q).transpose(0, 3, 4, 1, 2)).ravel()
+
+
+@pytest.fixture(scope="module")
+def small_plan(bklib):
+    from omp_bk_gb300.helmholtz import HelmholtzPlan
+    orders = [(p, 5 + 2 * p) for p in range(2, 9)]
+    plan = HelmholtzPlan(orders)
+    G, M = plan.geometry(seed=3)
+    u = bklib.fill_uniform(torch.empty(plan.n, dtype=torch.float64, device="cuda"), 4)
+    yield plan, G, M, u
+    plan.close()
+
+
+@pytest.mark.parametrize("prec", ["ff", "dfma", "mixed", "fp32"])
+def test_multi_apply_matches_per_order(bklib, small_plan, prec):
+    bk = bklib
+    plan, G, M, u = small_plan
+    lam = 1.0 if prec != "dfma" else 0.75
+    if prec in ("ff", "dfma"):
+        pr, eng, dt, tol = bk.PREC_FP64, (bk.ENGINE_FF if prec == "ff" else bk.ENGINE_DFMA), torch.float64, 1e-12
+    else:
+        pr, eng, dt, tol = (bk.PREC_MIXED if prec == "mixed" else bk.PREC_FP32), 0, torch.float32, 1e-5
+    Gd, Md, ud = G.to(dt), M.to(dt), u.to(dt)
+    v = torch.full_like(ud, float("nan"))
+    plan.apply(Gd, Md, lam, ud, v, prec=pr, engine=eng)
+    torch.cuda.synchronize()
+    for k, p in enumerate(plan.p):
+        su, sg = _slices(plan, k)
+        D, _, _ = bk.bk5_matrices(p)
+        w = torch.full_like(ud[su], float("nan"))
+        bk.bk5_apply(p, plan.E[k], D, Gd[sg], ud[su], w, prec=pr, engine=eng, layout=bk.LAYOUT_COLUMN,
+                     mass=Md[su], lam=lam)
+        torch.cuda.synchronize()
+        assert oracle.rel_maxdiff(host(v[su]), host(w)) < tol, p
+        # the oracle: FP64 BK5 on the same (rounded) inputs, G interleaved
+        q = p + 1
+        f = (lambda a: host(a)) if dt == torch.float64 else (lambda a: host(a).astype(np.float32).astype(np.float64))
+        ref = oracle.bk5(q, plan.E[k], D, _col_to_interleaved(f(Gd[sg]), plan.E[k], q), f(ud[su]),
+                         mass=f(Md[su]), lam=lam)
+        assert oracle.rel_maxdiff(host(v[su]), ref) < tol, p
+
+
+def test_cg_converges(bklib, small_plan):
+    bk = bklib
+    plan, G, M, ustar = small_plan
+    f = torch.empty_like(ustar)
+    plan.apply(G, M, 1.0, ustar, f, prec=bk.PREC_FP64)
+    x = torch.zeros_like(ustar)
+    st = plan.cg(G, M, G.float(), M.float(), 1.0, f, x, rtol=1e-10)
+    torch.cuda.synchronize()
+    assert st["converged"] and st["relres"] <= 1e-10, st
+    assert st["outer"] >= 1 and st["inner"] >= 1
+    # FP64 residual on the host with the oracle
+    r2 = 0.0
+    for k, p in enumerate(plan.p):
+        su, sg = _slices(plan, k)
+        q = p + 1
+        D, _, _ = bk.bk5_matrices(p)
+        Ax = oracle.bk5(q, plan.E[k], D, _col_to_interleaved(host(G[sg]), plan.E[k], q), host(x[su]),
+                        mass=host(M[su]), lam=1.0)
+        r2 += float(np.sum((host(f[su]) - Ax) ** 2))
+    assert np.sqrt(r2) <= 2e-10 * float(torch.linalg.norm(f))
+    assert float(torch.linalg.norm(x - ustar) / torch.linalg.norm(ustar)) < 1e-6
+
+
+def test_cg_graph_reused_and_restarted(bklib, small_plan):
+    """A second solve reuses the captured graph; a warm start converges in
+    fewer refinement steps."""
+    bk = bklib
+    plan, G, M, ustar = small_plan
+    f = torch.empty_like(ustar)
+    plan.apply(G, M, 1.0, ustar, f, prec=bk.PREC_FP64)
+    G32, M32 = G.float(), M.float()
+    x = torch.zeros_like(ustar)
+    a = plan.cg(G, M, G32, M32, 1.0, f, x, rtol=1e-10)
+    b = plan.cg(G, M, G32, M32, 1.0, f, x, rtol=1e-10)
+    assert a["converged"] and b["converged"]
+    assert b["outer"] == 0 and b["relres"] <= 1e-10
+
+
+def test_tuner(bklib):
+    from omp_bk_gb300 import tune
+    best = tune.tune([(2, 512), (5, 256), (8, 64)], max_elements=512, reps=2, use_cache=False)
+    for p in (2, 5, 8):
+        assert best[p] in tune.candidates(p)
