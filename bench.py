@@ -5,8 +5,10 @@
 Workload (the headline configuration): BK5 collocated Laplacian, plain FP64,
 p = 7 (P = Q = 8 GLL points), E = 262144 elements = 134,217,728 DoFs on a
 64^3 grid of spacing h = 1/64 whose vertices are jittered by U[-0.15h, 0.15h]
-(seeded), G = w detJ J^-1 J^-T with 6 symmetric factors in BK5.cpp's
-interleaved layout, D the 8 x 8 GLL derivative, u ~ U[-1, 1] (seeded).  All
+(seeded), G = w detJ J^-1 J^-T with 6 symmetric factors generated directly in
+the column layout G(e, f, k, i, j) (the layout of the reference's column-sweep
+variants; BK5.cpp's interleaved layout is --layout 1), D the 8 x 8 GLL
+derivative, u ~ U[-1, 1] (seeded).  All
 inputs are synthetic (the reference names no dataset); the inputs (8.6 GB per
 apply) are 65x the 129 MB L2, so no flush is needed between steps.
 
@@ -61,7 +63,7 @@ def parse():
     ap.add_argument("--prec", default="fp64", choices=["fp64", "mixed", "fp32"],
                     help="form timed in the main loop (profiling; the headline is fp64)")
     ap.add_argument("--kernel", default="auto", choices=["auto", "sweep", "column"])
-    ap.add_argument("--layout", type=int, default=1, help="G layout (0 factor, 1 interleaved, 2 column)")
+    ap.add_argument("--layout", type=int, default=2, help="G layout (0 factor, 1 interleaved, 2 column)")
     ap.add_argument("--no-forms", action="store_true", help="skip the side-by-side forms")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-e2e", action="store_true")
@@ -288,7 +290,7 @@ def main():
            "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "f64" if prec == bk.PREC_FP64 else "f32", "data": "synthetic",
            "config": {"workload": f"BK5 collocated Laplacian p={P_ORDER} (P=Q=8 GLL) FP64 apply, E={E} "
-                                  f"({dofs} DoFs), jittered trilinear mesh, G6 interleaved",
+                                  f"({dofs} DoFs), jittered trilinear mesh, G6 layout {args.layout}",
                       "p": P_ORDER, "elements": E, "engine": args.engine, "prec": args.prec, "kernel": args.kernel,
                       "layout": args.layout, "l2": "inputs 8.6 GB >> 129 MB L2, no flush",
                       "parallelism": f"replicas x{world}"},

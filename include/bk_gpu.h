@@ -101,7 +101,8 @@ typedef struct bk_options {
 
 /* BK5 kernel shapes. */
 enum bk_kernel_shape {
-    BK_KERNEL_AUTO = 0,   /* the column kernel */
+    BK_KERNEL_AUTO = 0,   /* the faster of the two as measured on GB300 (the
+                             sweep kernel at p = 7 for every form) */
     BK_KERNEL_SWEEP = 1,  /* one thread per line of the box per 1-D contraction,
                              all intermediates in shared memory */
     BK_KERNEL_COLUMN = 2  /* one thread per k-column of an element, the

@@ -40,26 +40,52 @@ enum Scalar { S_RR = 0, S_RR0, S_PAP, S_IT, S_TOL2, S_MAXIT, S_NORM, S_INV, S_RN
 
 template <class Eng, int NBUF>
 struct MultiLaunch {
+    // Sets the kernel's shared-memory limit on the current device (once) and
+    // returns its resident blocks per SM for `total` bytes; outside any
+    // stream capture.
+    static int prepare(int total)
+    {
+        auto kern = bk5_multi_kernel<Eng, kNT, NBUF>;
+        static int set[kMaxDevices] = {0};
+        static int occ_of[kMaxDevices][2] = {{0, 0}};
+        const int dev = current_device();
+        if (dev < 0 || dev >= kMaxDevices) return 0;
+        if (!set[dev]) {
+            if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448) != cudaSuccess) {
+                cudaGetLastError();
+                return 0;
+            }
+            set[dev] = 1;
+        }
+        if (occ_of[dev][0] != total) {
+            int occ = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kNT, total) != cudaSuccess) {
+                cudaGetLastError();
+                return 0;
+            }
+            occ_of[dev][0] = total;
+            occ_of[dev][1] = occ;
+        }
+        return occ_of[dev][1];
+    }
+
+    static int smem(const PMulti<typename Eng::C>& prm, int& st, int& cb)
+    {
+        int total = 0;
+        multi_smem<Eng>(prm.seg, prm.nseg, st, cb, total, NBUF);
+        return total;
+    }
+
     static int run(const PMulti<typename Eng::C>& prm, const MultiTile* tiles, int ntiles, const void* u,
                    const void* G, const void* mass, double lambda, void* v, cudaStream_t s)
     {
         using S = typename Eng::S;
-        int st = 0, cb = 0, total = 0;
-        multi_smem<Eng>(prm.seg, prm.nseg, st, cb, total, NBUF);
+        int st = 0, cb = 0;
+        const int total = smem(prm, st, cb);
         if (total > 232448) return BK_ERR_ARG;
         auto kern = bk5_multi_kernel<Eng, kNT, NBUF>;
-        // the attribute is raised to the largest size any plan has needed
-        static int set_bytes[kMaxDevices] = {0};
-        const int dev = current_device();
-        if (dev < 0 || dev >= kMaxDevices) return BK_ERR_CUDA;
-        if (total > set_bytes[dev]) {
-            if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448) != cudaSuccess)
-                return BK_ERR_CUDA;
-            set_bytes[dev] = 232448;
-        }
-        int occ = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kNT, total) != cudaSuccess || occ < 1)
-            return BK_ERR_CUDA;
+        const int occ = prepare(total);
+        if (occ < 1) return BK_ERR_CUDA;
         int grid = occ * sm_count();
         if (grid > ntiles) grid = ntiles;
         if (grid < 1) return BK_OK;
@@ -327,13 +353,35 @@ void free_graph(bk_hplan* h)
 
 // The inner CG as a graph: start, r.r, then WHILE(cond) { A p, p.Ap, update,
 // step (sets cond), new direction }.
-int build_inner_graph(bk_hplan* h, const void* G32, const void* mass32, double lambda, cudaStream_t s)
+int build_inner_graph(bk_hplan* h, const void* G32, const void* mass32, double lambda, cudaStream_t user)
 {
     free_graph(h);
+    {
+        // kernel attributes and occupancy outside the capture
+        int st = 0, cb = 0;
+        if (MultiLaunch<EngMixed, 2>::prepare(MultiLaunch<EngMixed, 2>::smem(h->p_f32, st, cb)) < 1)
+            return BK_ERR_CUDA;
+    }
+    // the legacy default stream cannot be captured: capture on a private
+    // stream (the graph is launched on the caller's stream)
+    (void)user;
+    cudaStream_t s = nullptr;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        return BK_ERR_CUDA;
+    }
+    struct StreamGuard {
+        cudaStream_t s;
+        ~StreamGuard() { cudaStreamDestroy(s); }
+    } guard{s};
     cudaGraph_t g = nullptr;
-    if (cudaGraphCreate(&g, 0) != cudaSuccess) return BK_ERR_CUDA;
+    if (cudaGraphCreate(&g, 0) != cudaSuccess) {
+        cudaGetLastError();
+        return BK_ERR_CUDA;
+    }
     cudaGraphConditionalHandle handle;
     if (cudaGraphConditionalHandleCreate(&handle, g, 1, cudaGraphCondAssignDefault) != cudaSuccess) {
+        cudaGetLastError();
         cudaGraphDestroy(g);
         return BK_ERR_CUDA;
     }
@@ -342,6 +390,7 @@ int build_inner_graph(bk_hplan* h, const void* G32, const void* mass32, double l
     // prologue, captured into g
     int rc = BK_OK;
     if (cudaStreamBeginCaptureToGraph(s, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
         cudaGraphDestroy(g);
         return BK_ERR_CUDA;
     }

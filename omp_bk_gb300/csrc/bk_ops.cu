@@ -230,7 +230,10 @@ int BK_CAT(launch_bk5, BK_SFX)(int p, long long E, const double* D, const void* 
                                 double lambda, void* v, int F, int layout, int eb, int kernel, cudaStream_t s)
 {
     if (p < 1 || p > 8) return BK_ERR_ORDER;
-    if (kernel == BK_KERNEL_SWEEP) return BK_CAT(bk5_sweep, BK_SFX)(p, F, layout, D, E, u, G, mass, lambda, v, s);
+    // AUTO: the sweep kernel, measured equal or faster than the column kernel
+    // for every form at p = 7 (GB300)
+    if (kernel == BK_KERNEL_SWEEP || kernel == BK_KERNEL_AUTO)
+        return BK_CAT(bk5_sweep, BK_SFX)(p, F, layout, D, E, u, G, mass, lambda, v, s);
     switch (layout) {
         case 0: return BK_CATL(bk5_col, BK_SFX, 0)(p, F, eb, D, E, u, G, mass, lambda, v, s);
         case 1: return BK_CATL(bk5_col, BK_SFX, 1)(p, F, eb, D, E, u, G, mass, lambda, v, s);

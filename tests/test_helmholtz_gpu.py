@@ -56,8 +56,9 @@ def test_multi_apply_matches_per_order(bklib, small_plan, prec):
         su, sg = _slices(plan, k)
         D, _, _ = bk.bk5_matrices(p)
         w = torch.full_like(ud[su], float("nan"))
-        bk.bk5_apply(p, plan.E[k], D, Gd[sg], ud[su], w, prec=pr, engine=eng, layout=bk.LAYOUT_COLUMN,
-                     mass=Md[su], lam=lam)
+        # the per-order entry point wants 16-byte aligned arrays: copies
+        bk.bk5_apply(p, plan.E[k], D, Gd[sg].clone(), ud[su].clone(), w, prec=pr, engine=eng,
+                     layout=bk.LAYOUT_COLUMN, mass=Md[su].clone(), lam=lam)
         torch.cuda.synchronize()
         assert oracle.rel_maxdiff(host(v[su]), host(w)) < tol, p
         # the oracle: FP64 BK5 on the same (rounded) inputs, G interleaved
