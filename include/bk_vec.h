@@ -34,6 +34,18 @@ long long bk_dot_workspace_bytes(long long n);
 int bk_dot(long long n, const void* x, const void* y, int f64, double* result, void* workspace,
            long long workspace_bytes, int half, bk_stream_t stream);
 
+/* The same dot product with no workspace argument and no allocation, for
+ * callers that cannot allocate device memory (no counterpart in the
+ * reference, whose host loops need no scratch).  Its partial sums live in a
+ * fixed 32 KiB array of this library on each device (4096 doubles, one per
+ * chunk of 65536 values): n <= BK_DOT_NOALLOC_MAX_N = 268,435,456, larger n
+ * returns BK_ERR_SIZE.  The first call on a device looks the array's device
+ * address up (cudaGetSymbolAddress): make it before capturing a stream.
+ * Calls share the array: calls that overlap on the GPU race on it. */
+#define BK_DOT_NOALLOC_MAX_N 268435456LL
+int bk_dot_noalloc(long long n, const void* x, const void* y, int f64, double* result, int half,
+                   bk_stream_t stream);
+
 /* y = a x + b y (double or float vectors, FP64 scalars). */
 int bk_axpby(long long n, double a, const void* x, double b, void* y, int f64, bk_stream_t stream);
 

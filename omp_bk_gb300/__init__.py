@@ -44,6 +44,7 @@ EXPORTS = [
     "bk_fill_lognormal", "bk_geom_affine", "bk_coords_affine", "bk_geom_trilinear", "bk_convert",
     "bk3_adjoint", "bk_stream_kernel", "bk_dot_workspace_bytes", "bk_dot", "bk_axpby",
     "bk_hplan_create", "bk_hplan_destroy", "bk_hplan_size", "bk_hplan_apply", "bk_hplan_cg",
+    "bk_dot_noalloc",
 ]
 
 
