@@ -31,6 +31,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -67,6 +68,8 @@ def parse():
     ap.add_argument("--no-forms", action="store_true", help="skip the side-by-side forms")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--workload", default="bk5", choices=["bk5", "bk1", "bk3", "adjoint", "helmholtz"],
+                    help="bk5: the headline; the others: the remaining configurations, one JSON line each")
     return ap.parse_args()
 
 
@@ -250,10 +253,229 @@ def run_reference(args):
     return 0
 
 
+# ---- the other configurations ------------------------------------------------
+
+def _events_ms(fn, steps, warmup, torch):
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record()
+    for _ in range(steps):
+        fn()
+    t1.record()
+    torch.cuda.synchronize()
+    return t0.elapsed_time(t1) / steps
+
+
+def _rel(a, ref):
+    d = (a.double() - ref).abs()
+    return float(d.max() / ref.abs().max()), float(d.pow(2).mean().sqrt() / ref.pow(2).mean().sqrt())
+
+
+def _line(args, workload, value, ms, dtype, extra):
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+           "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": dtype, "data": "synthetic", "config": {"workload": workload}}
+    out.update(extra)
+    print(json.dumps(out), flush=True)
+
+
+def run_bk1(args):
+    """BK1 mass apply p = 3 (P = 4 GLL nodes, Q = 5 Gauss points), E = 4096,
+    affine elements (h = 1/16, U[-0.2, 0.2] perturbation), u ~ U[-1, 1]."""
+    import torch
+
+    import omp_bk_gb300 as bk
+    p, E = 3, 4096
+    P, Q = p + 1, p + 2
+    B, _, xq, wq, _ = bk.bk1_bk3_matrices(p)
+    qd = torch.empty(E * Q ** 3, dtype=torch.float64, device="cuda")
+    bk.geom_affine(Q, E, xq, wq, 21, 1.0 / 16, 0.2, qdata=qd)
+    u = bk.fill_uniform(torch.empty(E * P ** 3, dtype=torch.float64, device="cuda"), 22)
+    v = torch.empty_like(u)
+    dofs = E * P ** 3
+    steps, warm = max(args.steps, 20), max(args.warmup, 3)
+    ms = _events_ms(lambda: bk.bk1_apply(p, E, B, qd, u, v), steps, warm, torch)
+    forms = {}
+    ref = v.clone()
+    vd = torch.empty_like(v)
+    md = _events_ms(lambda: bk.bk1_apply(p, E, B, qd, u, vd, engine=bk.ENGINE_DFMA), steps, warm, torch)
+    forms["fp64_dfma"] = {"gdofs": dofs / md / 1e6, "rel_max_err": _rel(vd, ref)[0]}
+    u32, q32 = u.float(), qd.float()
+    v32 = torch.empty_like(u32)
+    for name, pr in (("fp32", bk.PREC_FP32), ("mixed", bk.PREC_MIXED)):
+        m32 = _events_ms(lambda: bk.bk1_apply(p, E, B, q32, u32, v32, prec=pr), steps, warm, torch)
+        forms[name] = {"gdofs": dofs / m32 / 1e6, "rel_max_err": _rel(v32, ref)[0]}
+    import oracle
+    t = time.perf_counter()
+    host = oracle.bk1(Q, E, B, qd.cpu().numpy(), u.cpu().numpy(), fast=True)
+    cpu_s = time.perf_counter() - t
+    err = float(abs(torch.from_numpy(host) - ref.cpu()).max() / ref.abs().max())
+    _line(args, f"BK1 mass apply p={p} (P=4 GLL, Q=5 Gauss), E={E}, FP64 float-float, L2-resident (8.3 MB)",
+          dofs / ms / 1e6, ms, "f64",
+          {"forms": forms, "rel_max_err_vs_oracle": err,
+           "cpu_baseline": {"value": dofs / cpu_s / 1e9, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                            "sample": f"full workload, one apply (oracle/bk_oracle.c, OpenMP)"}})
+
+
+def run_bk3(args):
+    """BK3 p = 6 (P = 7, Q = 8), E = 131072, affine elements: FP64 against the
+    mixed form, max and RMS relative error for u ~ U[-1,1] and the smooth
+    u = sin(pi x) sin(pi y) sin(pi z) at the GLL nodes."""
+    import torch
+
+    import omp_bk_gb300 as bk
+    p, E = 6, 131072
+    P, Q = p + 1, p + 2
+    B, D, xq, wq, xn = bk.bk1_bk3_matrices(p)
+    G = torch.empty(E * 6 * Q ** 3, dtype=torch.float64, device="cuda")
+    bk.geom_affine(Q, E, xq, wq, 31, 1.0 / 64, 0.2, G=G, layout=bk.LAYOUT_FACTOR)
+    u_rand = bk.fill_uniform(torch.empty(E * P ** 3, dtype=torch.float64, device="cuda"), 32)
+    X = torch.empty(E * P ** 3 * 3, dtype=torch.float64, device="cuda")
+    bk.coords_affine(P, E, 64, 64, xn, 31, 1.0 / 64, 0.2, X)
+    X = X.view(-1, 3)
+    u_smooth = (torch.sin(math.pi * X[:, 0]) * torch.sin(math.pi * X[:, 1]) * torch.sin(math.pi * X[:, 2])).contiguous()
+    dofs = E * P ** 3
+    steps, warm = max(args.steps // 4, 10), max(args.warmup, 3)
+    v = torch.empty_like(u_rand)
+    ms = _events_ms(lambda: bk.bk3_apply(p, E, B, D, G, u_rand, v), steps, warm, torch)
+    G32 = G.float()
+    v32 = torch.empty(E * P ** 3, dtype=torch.float32, device="cuda")
+    errs = {}
+    for name, uu in (("random", u_rand), ("smooth", u_smooth)):
+        bk.bk3_apply(p, E, B, D, G, uu, v)
+        u32 = uu.float()
+        bk.bk3_apply(p, E, B, D, G32, u32, v32, prec=bk.PREC_MIXED)
+        mx, rms = _rel(v32, v)
+        errs[name] = {"rel_max": mx, "rel_rms": rms}
+    mm = _events_ms(lambda: bk.bk3_apply(p, E, B, D, G32, u32, v32, prec=bk.PREC_MIXED), steps, warm, torch)
+    vd = torch.empty_like(v)
+    md = _events_ms(lambda: bk.bk3_apply(p, E, B, D, G, u_smooth, vd, engine=bk.ENGINE_DFMA), max(3, steps // 4),
+                    2, torch)
+    bytes64 = 8 * (2 * dofs + 6 * E * Q ** 3)
+    _line(args, f"BK3 Poisson p={p} (P=7 GLL, Q=8 Gauss), E={E}, FP64 float-float vs mixed (FP32 storage)",
+          dofs / ms / 1e6, ms, "f64",
+          {"forms": {"fp64_ff": {"gdofs": dofs / ms / 1e6, "hbm_frac": bytes64 / ms / 1e6 / measured_peak()[0]},
+                     "fp64_dfma": {"gdofs": dofs / md / 1e6},
+                     "mixed": {"gdofs": dofs / mm / 1e6, "speedup_vs_fp64": ms / mm,
+                               "hbm_frac": bytes64 / 2 / mm / 1e6 / measured_peak()[0], "errors": errs}}})
+
+
+def run_adjoint(args):
+    """BK3 adjoint p = 4 (P = 5, Q = 6), E = 65536, log k ~ N(0, 0.5^2):
+    forward + backward timing and the central-difference check (h = 1e-6)."""
+    import torch
+
+    import omp_bk_gb300 as bk
+    p, E = 4, 65536
+    P, Q = p + 1, p + 2
+    B, D, xq, wq, _ = bk.bk1_bk3_matrices(p)
+    G = torch.empty(E * 6 * Q ** 3, dtype=torch.float64, device="cuda")
+    bk.geom_affine(Q, E, xq, wq, 41, 1.0 / 16, 0.2, G=G, layout=bk.LAYOUT_FACTOR)
+    k = bk.fill_lognormal(torch.empty(E * Q ** 3, dtype=torch.float64, device="cuda"), 42, 0.5)
+    u = bk.fill_uniform(torch.empty(E * P ** 3, dtype=torch.float64, device="cuda"), 43)
+    f = bk.fill_uniform(torch.empty(E * P ** 3, dtype=torch.float64, device="cuda"), 44)
+    r = torch.empty_like(u)
+    dk = torch.empty_like(k)
+    dG = torch.empty_like(G)
+
+    def fwd(kk, GG, rr, eng=bk.ENGINE_AUTO):
+        bk.bk3_apply(p, E, B, D, GG, u, rr, k=kk, engine=eng)
+        bk.axpby(-1.0, f, 1.0, rr)
+
+    steps, warm = max(args.steps // 4, 10), max(args.warmup, 3)
+    mf = _events_ms(lambda: fwd(k, G, r), steps, warm, torch)
+    mb = _events_ms(lambda: bk.bk3_adjoint(p, E, B, D, G, k, u, r, dk, dG), steps, warm, torch)
+    ws = bk.dot_workspace(6 * E * Q ** 3)
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    fwd(k, G, r, bk.ENGINE_DFMA)
+    bk.bk3_adjoint(p, E, B, D, G, k, u, r, dk, dG)
+    h = 1e-6
+    worst = 0.0
+    rp, rm = torch.empty_like(r), torch.empty_like(r)
+    dkd, dGd = torch.empty_like(k), torch.empty_like(G)
+    for t in range(64):
+        bk.fill_uniform(dkd, 1000 + t)
+        bk.fill_uniform(dGd, 2000 + t)
+        dGd.mul_(G.abs().mean())
+        fwd(k + h * dkd, G + h * dGd, rp, bk.ENGINE_DFMA)
+        fwd(k - h * dkd, G - h * dGd, rm, bk.ENGINE_DFMA)
+        bk.dot(rp - rm, rp + rm, out, ws)
+        fd = out.item() / (4 * h)
+        bk.dot(dk, dkd, out, ws)
+        an = out.item()
+        bk.dot(dG, dGd, out, ws)
+        an += out.item()
+        worst = max(worst, abs(fd - an) / abs(an))
+    qdofs = E * Q ** 3
+    _line(args, f"BK3 adjoint p={p} (P=5, Q=6), E={E}, FP64: dL/dk, dL/dG of 1/2|A(k)u - f|^2",
+          qdofs / mb / 1e6, mb, "f64",
+          {"adjoint": {"backward_ms": mb, "forward_ms": mf, "backward_gpoints_s": qdofs / mb / 1e6,
+                       "backward_hbm_gbs": 8 * (2 * E * P ** 3 + 14 * qdofs) / mb / 1e6,
+                       "fd_directions": 64, "fd_step": h, "fd_max_rel_err": worst},
+           "unit_note": "value = quadrature points per second of the backward kernel (G points/s)"})
+
+
+def run_helmholtz(args):
+    """Mixed-order Helmholtz (BK5 + GLL mass, lambda = 1), p = 2..8, E_p =
+    2^(8-p) 4096: tiles tuned per order, one persistent launch, CG to 1e-10
+    with FP32 inner applies and FP64 refinement; against per-order FP64
+    launches."""
+    import torch
+
+    import omp_bk_gb300 as bk
+    from omp_bk_gb300 import helmholtz as hz
+    from omp_bk_gb300 import tune
+    orders = hz.config_orders()
+    best = tune.tune(orders)
+    plan = hz.HelmholtzPlan([(p, E, best[p]) for p, E in orders])
+    G, M = plan.geometry(seed=11)
+    G32, M32 = G.float(), M.float()
+    ustar = bk.fill_uniform(torch.empty(plan.n, dtype=torch.float64, device="cuda"), 5)
+    f = torch.empty_like(ustar)
+    plan.apply(G, M, 1.0, ustar, f, prec=bk.PREC_FP64)
+    u32, v32, v64 = ustar.float(), torch.empty(plan.n, dtype=torch.float32, device="cuda"), torch.empty_like(ustar)
+    steps, warm = max(args.steps // 4, 10), max(args.warmup, 3)
+    m_multi = _events_ms(lambda: plan.apply(G32, M32, 1.0, u32, v32, prec=bk.PREC_MIXED), steps, warm, torch)
+    m_multi64 = _events_ms(lambda: plan.apply(G, M, 1.0, ustar, v64, prec=bk.PREC_FP64), max(3, steps // 4), 2, torch)
+
+    def per_order(prec, GG, MM, uu, vv):
+        for kk, p in enumerate(plan.p):
+            q, E = p + 1, plan.E[kk]
+            su = slice(plan.uoff[kk], plan.uoff[kk] + E * q ** 3)
+            sg = slice(plan.goff[kk], plan.goff[kk] + 6 * E * q ** 3)
+            bk.bk5_apply(p, E, bk.bk5_matrices(p)[0], GG[sg], uu[su], vv[su], prec=prec,
+                         layout=bk.LAYOUT_COLUMN, mass=MM[su], lam=1.0)
+
+    aligned = all((o * 8) % 16 == 0 for o in plan.uoff) and all((o * 8) % 16 == 0 for o in plan.goff)
+    m_per64 = _events_ms(lambda: per_order(bk.PREC_FP64, G, M, ustar, v64), max(3, steps // 4), 2, torch) \
+        if aligned else None
+    x = torch.zeros_like(ustar)
+    plan.cg(G, M, G32, M32, 1.0, f, x, rtol=1e-10, allow_noconv=True)   # builds the graph
+    x.zero_()
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    st = plan.cg(G, M, G32, M32, 1.0, f, x, rtol=1e-10, allow_noconv=True)
+    torch.cuda.synchronize()
+    solve_s = time.perf_counter() - t
+    err = float(torch.linalg.norm(x - ustar) / torch.linalg.norm(ustar))
+    _line(args, f"mixed-order Helmholtz p=2..8, E_p=2^(8-p)*4096 ({plan.n} DoFs), one persistent launch",
+          plan.n / m_multi / 1e6, m_multi, "f32",
+          {"helmholtz": {"dofs": plan.n, "tiles": plan.ntiles, "tile_elems": best,
+                         "multi_mixed_gdofs": plan.n / m_multi / 1e6, "multi_fp64_gdofs": plan.n / m_multi64 / 1e6,
+                         "per_order_fp64_gdofs": (plan.n / m_per64 / 1e6) if m_per64 else None,
+                         "cg": st, "cg_seconds": solve_s, "solution_rel_err": err}})
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload != "bk5":
+        {"bk1": run_bk1, "bk3": run_bk3, "adjoint": run_adjoint, "helmholtz": run_helmholtz}[args.workload](args)
+        return 0
     import torch
 
     import omp_bk_gb300 as bk

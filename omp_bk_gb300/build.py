@@ -39,11 +39,12 @@ def _units() -> list[tuple[str, list[str], str]]:
     """(source, extra flags, object) of every translation unit."""
     u = []
     for eng in range(4):
-        for op in (1, 3, 5, 7):
+        for op in (1, 3, 7):
             u.append(("bk_ops.cu", [f"-DBK_ENGINE_TU={eng}", f"-DBK_OP_TU={op}"], f"bk_ops_{eng}_{op}.o"))
-        for lay in range(3):
-            u.append(("bk_ops.cu", [f"-DBK_ENGINE_TU={eng}", "-DBK_OP_TU=6", f"-DBK_LAYOUT_TU={lay}"],
-                      f"bk_ops_{eng}_6_{lay}.o"))
+        for op in (5, 6):
+            for lay in range(3):
+                u.append(("bk_ops.cu", [f"-DBK_ENGINE_TU={eng}", f"-DBK_OP_TU={op}", f"-DBK_LAYOUT_TU={lay}"],
+                          f"bk_ops_{eng}_{op}_{lay}.o"))
     for src in ("bk_helmholtz.cu", "bk_api.cu", "bk_geom.cu", "bk_basis.cpp", "bk_vec.cu", "bk_noalloc.cu"):
         u.append((src, [], src.rsplit(".", 1)[0] + ".o"))
     return u
@@ -72,7 +73,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     Returns the library path."""
     os.makedirs(OBJDIR, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
-    units = sorted(_units(), key=lambda t: "_6_" not in t[2])
+    units = sorted(_units(), key=lambda t: not ("_6_" in t[2] or "_5_" in t[2]))
     jobs = jobs or min(len(units), os.cpu_count() or 4)
     with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
         objs = list(ex.map(lambda t: _compile(t[0], t[1], t[2], verbose), units))

@@ -31,6 +31,8 @@ struct EngDfma {
     __device__ static __forceinline__ void add(A& acc, V x) { acc += x; }
     __device__ static __forceinline__ V result(A acc) { return acc; }
     __device__ static __forceinline__ V mul(V a, V b) { return a * b; }
+    __device__ static __forceinline__ V vadd(V a, V b) { return a + b; }
+    __device__ static __forceinline__ V vsub(V a, V b) { return a - b; }
     static C coef(double d) { return d; }
 };
 
@@ -48,6 +50,8 @@ struct EngFF {
     __device__ static __forceinline__ void add(A& acc, V x) { acc_add(acc, x); }
     __device__ static __forceinline__ V result(A acc) { return acc_result(acc); }
     __device__ static __forceinline__ V mul(V a, V b) { return ff_mul(a, b); }
+    __device__ static __forceinline__ V vadd(V a, V b) { return ff_add(a, b); }
+    __device__ static __forceinline__ V vsub(V a, V b) { return ff_add(a, ff{-b.hi, -b.lo}); }
     static C coef(double d)
     {
         C c;
@@ -71,6 +75,8 @@ struct EngF32 {
     __device__ static __forceinline__ void add(A& acc, V x) { acc += x; }
     __device__ static __forceinline__ V result(A acc) { return acc; }
     __device__ static __forceinline__ V mul(V a, V b) { return a * b; }
+    __device__ static __forceinline__ V vadd(V a, V b) { return a + b; }
+    __device__ static __forceinline__ V vsub(V a, V b) { return a - b; }
     static C coef(double d) { return static_cast<float>(d); }
 };
 

@@ -116,6 +116,17 @@ __device__ __forceinline__ ff ff_mul(const ff a, const ff b)
     return r;
 }
 
+// a + b, both float-float, normalised (TwoSum of the hi parts, lo parts added).
+__device__ __forceinline__ ff ff_add(const ff a, const ff b)
+{
+    float s, e;
+    two_sum(a.hi, b.hi, s, e);
+    e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+    ff r;
+    fast_two_sum(s, e, r.hi, r.lo);
+    return r;
+}
+
 // ---- binary64 <-> float-float ------------------------------------------------
 
 // The rare out-of-range cases, out of line: kept off the fast path so that

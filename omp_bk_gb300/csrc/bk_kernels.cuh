@@ -143,6 +143,100 @@ __device__ __forceinline__ void sweep(const typename Eng::V* in, typename Eng::V
     }
 }
 
+// Even-odd form of a square Q x Q matrix M with M(Q-1-o, Q-1-n) = -M(o, n)
+// (the derivative matrix on points symmetric about 0, and its transpose):
+// with H = Q/2, e(n) = x(n) + x(Q-1-n), d(n) = x(n) - x(Q-1-n) (n < H) and
+// the middle value x(m) of an odd Q,
+//   a(o) = sum_n A(o,n) e(n) + c(o) x(m),  b(o) = sum_n B(o,n) d(n),
+//   out(o) = a(o) + b(o),  out(Q-1-o) = b(o) - a(o),  out(m) = sum_n r(n) d(n)
+// with A = (M(o,n) + M(o,Q-1-n))/2, B = (M(o,n) - M(o,Q-1-n))/2, c(o) =
+// M(o,m), r(n) = M(m,n): Q^2/2 multiply-adds instead of Q^2 (the classic
+// even-odd decomposition of spectral-element codes).
+template <class C, int Q>
+struct EOMat {
+    static constexpr int H = Q / 2;
+    C A[H * H];
+    C B[H * H];
+    C c[H];
+    C r[H];
+};
+
+// Host side: the even-odd form of M(o, n) = m[o*ld + n] (trans: m[n*ld + o]);
+// true if M is centro-antisymmetric to within 1e-13 of its largest entry.
+template <class C, int Q, class Conv>
+inline bool make_eo(const double* m, bool trans, EOMat<C, Q>& out, Conv conv)
+{
+    constexpr int H = Q / 2;
+    auto M = [&](int o, int n) { return trans ? m[n * Q + o] : m[o * Q + n]; };
+    double big = 0, asym = 0;
+    for (int o = 0; o < Q; ++o)
+        for (int n = 0; n < Q; ++n) {
+            big = big > (M(o, n) < 0 ? -M(o, n) : M(o, n)) ? big : (M(o, n) < 0 ? -M(o, n) : M(o, n));
+            const double a = M(o, n) + M(Q - 1 - o, Q - 1 - n);
+            asym = asym > (a < 0 ? -a : a) ? asym : (a < 0 ? -a : a);
+        }
+    for (int o = 0; o < H; ++o) {
+        for (int n = 0; n < H; ++n) {
+            out.A[o * H + n] = conv(0.5 * (M(o, n) + M(o, Q - 1 - n)));
+            out.B[o * H + n] = conv(0.5 * (M(o, n) - M(o, Q - 1 - n)));
+        }
+        out.c[o] = conv((Q & 1) ? M(o, H) : 0.0);
+        out.r[o] = conv((Q & 1) ? M(H, o) : 0.0);
+    }
+    return asym <= 1e-13 * big;
+}
+
+// Even-odd sweep of direction DIR of a Q x Q x Q box (in == out allowed);
+// see EOMat.  When ADD is set, out(o) = M x + X(o) + Y(o) for the lines of
+// direction 2 (BK5's last transposed derivative plus the other two terms).
+template <class Eng, class WB, int DIR, int Q, class EM>
+__device__ __forceinline__ void sweep_eo(const typename Eng::V* in, typename Eng::V* out, int ne, const EM& m,
+                                         int tid, int nt)
+{
+    using V = typename Eng::V;
+    using A = typename Eng::A;
+    constexpr int H = Q / 2;
+    constexpr int LB = Q;
+    constexpr int L = Q * Q;
+    constexpr int SD = DIR == 0 ? WB::PS : (DIR == 1 ? WB::ZP : 1);
+    for (int w = tid; w < ne * L; w += nt) {
+        const int e = w / L;
+        const int l = w - e * L;
+        const int a = l / LB;
+        const int b = l - a * LB;
+        int base = (DIR == 0) ? a * WB::ZP + b : (DIR == 1 ? a * WB::PS + b : a * WB::PS + b * WB::ZP);
+        base += e * WB::size;
+        V x[Q];
+#pragma unroll
+        for (int n = 0; n < Q; ++n) x[n] = in[base + n * SD];
+        V ev[H > 0 ? H : 1], dv[H > 0 ? H : 1];
+#pragma unroll
+        for (int n = 0; n < H; ++n) {
+            ev[n] = Eng::vadd(x[n], x[Q - 1 - n]);
+            dv[n] = Eng::vsub(x[n], x[Q - 1 - n]);
+        }
+#pragma unroll
+        for (int o = 0; o < H; ++o) {
+            A aa = Eng::zero(), bb = Eng::zero();
+#pragma unroll
+            for (int n = 0; n < H; ++n) {
+                Eng::madd(aa, m.A[o * H + n], ev[n]);
+                Eng::madd(bb, m.B[o * H + n], dv[n]);
+            }
+            if (Q & 1) Eng::madd(aa, m.c[o], x[H]);
+            const V av = Eng::result(aa), bv = Eng::result(bb);
+            out[base + o * SD] = Eng::vadd(bv, av);
+            out[base + (Q - 1 - o) * SD] = Eng::vsub(bv, av);
+        }
+        if (Q & 1) {
+            A t = Eng::zero();
+#pragma unroll
+            for (int n = 0; n < H; ++n) Eng::madd(t, m.r[n], dv[n]);
+            out[base + H * SD] = Eng::result(t);
+        }
+    }
+}
+
 // Dense (X, Y, Z) slice of S values of `ne` elements (element stride estride)
 // -> padded work box, converted to the working type.
 template <class Eng, class WB, int X, int Y, int Z>
@@ -204,7 +298,9 @@ __device__ __forceinline__ bool batch_wait_failed(uint64_t* bar, uint32_t phase,
 
 template <class C, int Q>
 struct P5 {
-    C D[Q * Q];   // D(i, n) = D[i*Q + n]
+    C D[Q * Q];          // D(i, n) = D[i*Q + n]
+    EOMat<C, Q> eo;      // even-odd form of D (used when the kernel's EO is set)
+    EOMat<C, Q> eot;     // even-odd form of D^T
 };
 
 template <class C, int Q>
@@ -223,7 +319,10 @@ __device__ __forceinline__ int g_index(int i, int j, int f, int k)
     return ((f * Q + k) * Q + i) * Q + j;
 }
 
-template <class Eng, int Q, int EB, int F, int LAYOUT>
+// GD: G read from global memory in the pointwise stage (coalesced in every
+// layout: points are walked in G's own order) instead of staged by TMA, which
+// leaves the block's shared memory to u and the work boxes.
+template <class Eng, int Q, int EB, int F, int LAYOUT, bool GD = false>
 struct BK5Cfg {
     using S = typename Eng::S;
     using V = typename Eng::V;
@@ -231,19 +330,19 @@ struct BK5Cfg {
     static constexpr int Q3 = Q * Q * Q;
     static constexpr int NT = ((EB * Q * Q + 31) / 32) * 32 < 64 ? 64 : ((EB * Q * Q + 31) / 32) * 32;
     static constexpr int U_BYTES = stage_bytes<S>(EB * Q3);
-    static constexpr int G_BYTES = stage_bytes<S>(EB * F * Q3);
+    static constexpr int G_BYTES = GD ? 0 : stage_bytes<S>(EB * F * Q3);
     static constexpr int W_BYTES = 3 * EB * WB::size * int(sizeof(V));
     static constexpr int SMEM = U_BYTES + G_BYTES + W_BYTES + 16;
 };
 
-template <class Eng, int Q, int EB, int F, int LAYOUT>
-__global__ void __launch_bounds__(BK5Cfg<Eng, Q, EB, F, LAYOUT>::NT)
+template <class Eng, int Q, int EB, int F, int LAYOUT, bool EO = false, bool GD = false>
+__global__ void __launch_bounds__(BK5Cfg<Eng, Q, EB, F, LAYOUT, GD>::NT)
     bk5_kernel(const __grid_constant__ P5<typename Eng::C, Q> prm, const long long E,
                const typename Eng::S* __restrict__ u, const typename Eng::S* __restrict__ G,
                const typename Eng::S* __restrict__ mass, const double lambda, typename Eng::S* __restrict__ v,
                const DevCtx ctx)
 {
-    using Cfg = BK5Cfg<Eng, Q, EB, F, LAYOUT>;
+    using Cfg = BK5Cfg<Eng, Q, EB, F, LAYOUT, GD>;
     using S = typename Eng::S;
     using V = typename Eng::V;
     using A = typename Eng::A;
@@ -275,7 +374,7 @@ __global__ void __launch_bounds__(BK5Cfg<Eng, Q, EB, F, LAYOUT>::NT)
         uint32_t tx = 0;
         if (tid == 0) fence_proxy_async();
         const S* us = stage_issue<S>(ustage, u + e0 * Q3, ne * Q3, bar, tx, tid, nt);
-        const S* gs = stage_issue<S>(gstage, G + e0 * F * Q3, ne * F * Q3, bar, tx, tid, nt);
+        const S* gs = GD ? G + e0 * F * Q3 : stage_issue<S>(gstage, G + e0 * F * Q3, ne * F * Q3, bar, tx, tid, nt);
         if (tid == 0) mbar_arrive_expect_tx(bar, tx);
         if (batch_wait_failed(bar, phase, ctx, tid)) return;
         // 2. u -> W2 (working type, padded)
@@ -283,10 +382,17 @@ __global__ void __launch_bounds__(BK5Cfg<Eng, Q, EB, F, LAYOUT>::NT)
         __syncthreads();
         // 3. gradient: qr -> W0 (along i), qs -> W1 (along j); qt along k
         //    in place into W2 after the other two have read it
-        sweep<Eng, WB, 0, Q, Q, Q, Q>(W2, W0, ne, Dm, tid, nt);
-        sweep<Eng, WB, 1, Q, Q, Q, Q>(W2, W1, ne, Dm, tid, nt);
-        __syncthreads();
-        sweep<Eng, WB, 2, Q, Q, Q, Q>(W2, W2, ne, Dm, tid, nt);
+        if constexpr (EO) {
+            sweep_eo<Eng, WB, 0, Q>(W2, W0, ne, prm.eo, tid, nt);
+            sweep_eo<Eng, WB, 1, Q>(W2, W1, ne, prm.eo, tid, nt);
+            __syncthreads();
+            sweep_eo<Eng, WB, 2, Q>(W2, W2, ne, prm.eo, tid, nt);
+        } else {
+            sweep<Eng, WB, 0, Q, Q, Q, Q>(W2, W0, ne, Dm, tid, nt);
+            sweep<Eng, WB, 1, Q, Q, Q, Q>(W2, W1, ne, Dm, tid, nt);
+            __syncthreads();
+            sweep<Eng, WB, 2, Q, Q, Q, Q>(W2, W2, ne, Dm, tid, nt);
+        }
         __syncthreads();
         // 4. fluxes with the symmetric (F = 6) or full (F = 9) factors
         for (int w = tid; w < ne * Q3; w += nt) {
@@ -323,11 +429,19 @@ __global__ void __launch_bounds__(BK5Cfg<Eng, Q, EB, F, LAYOUT>::NT)
         }
         __syncthreads();
         // 5. transposed derivatives: along i in place on W0, along j on W1
-        sweep<Eng, WB, 0, Q, Q, Q, Q>(W0, W0, ne, Dt, tid, nt);
-        sweep<Eng, WB, 1, Q, Q, Q, Q>(W1, W1, ne, Dt, tid, nt);
+        if constexpr (EO) {
+            sweep_eo<Eng, WB, 0, Q>(W0, W0, ne, prm.eot, tid, nt);
+            sweep_eo<Eng, WB, 1, Q>(W1, W1, ne, prm.eot, tid, nt);
+            __syncthreads();
+            sweep_eo<Eng, WB, 2, Q>(W2, W2, ne, prm.eot, tid, nt);
+        } else {
+            sweep<Eng, WB, 0, Q, Q, Q, Q>(W0, W0, ne, Dt, tid, nt);
+            sweep<Eng, WB, 1, Q, Q, Q, Q>(W1, W1, ne, Dt, tid, nt);
+        }
         __syncthreads();
-        // 6. along k on W2, plus the other two terms (and the Helmholtz mass
-        //    term), written densely into the u staging area
+        // 6. along k on W2 (already contracted when EO), plus the other two
+        //    terms (and the Helmholtz mass term), written densely into the u
+        //    staging area
         S* vs = const_cast<S*>(us);
         {
             constexpr int L = Q * Q;
@@ -343,8 +457,12 @@ __global__ void __launch_bounds__(BK5Cfg<Eng, Q, EB, F, LAYOUT>::NT)
 #pragma unroll
                 for (int o = 0; o < Q; ++o) {
                     A acc = Eng::zero();
+                    if constexpr (EO) {
+                        Eng::add(acc, x[o]);
+                    } else {
 #pragma unroll
-                    for (int n = 0; n < Q; ++n) Eng::madd(acc, Dt(o, n), x[n]);
+                        for (int n = 0; n < Q; ++n) Eng::madd(acc, Dt(o, n), x[n]);
+                    }
                     V res;
                     if constexpr (HasSum3<Eng>::value) {
                         res = Eng::sum3(Eng::result(acc), W0[base + o], W1[base + o]);

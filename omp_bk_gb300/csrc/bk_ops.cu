@@ -14,8 +14,8 @@
 #error "BK_ENGINE_TU must be 0 (dfma), 1 (ff), 2 (fp32) or 3 (mixed)"
 #endif
 // BK_OP_TU selects the operator of this translation unit: 1 BK1, 3 BK3,
-// 5 BK5 sweep kernel and the BK5 dispatch, 6 BK5 column kernel (one G
-// layout, BK_LAYOUT_TU), 7 the BK3 adjoint.
+// 5 BK5 sweep kernel and 6 BK5 column kernel (one G layout each,
+// BK_LAYOUT_TU), 7 the BK3 adjoint and the BK5 dispatch.
 #ifndef BK_OP_TU
 #error "BK_OP_TU must be 1, 3, 5, 6 or 7"
 #endif
@@ -80,17 +80,22 @@ int grid_for(long long nbatch, int occ)
 }
 
 #if BK_OP_TU == 5
-template <int Q, int EB, int F, int LAYOUT>
+template <int Q, int EB, int F, int LAYOUT, bool GD>
 int bk5_q(const double* D, long long E, const void* u, const void* G, const void* mass, double lambda, void* v,
           cudaStream_t s)
 {
-    using Cfg = BK5Cfg<Eng, Q, EB, F, LAYOUT>;
+    using Cfg = BK5Cfg<Eng, Q, EB, F, LAYOUT, GD>;
     using S = typename Eng::S;
     static_assert(Cfg::SMEM <= 232448, "BK5 block exceeds the shared memory of an SM");
     P5<typename Eng::C, Q> prm;
     for (int i = 0; i < Q * Q; ++i) prm.D[i] = Eng::coef(D[i]);
-    auto kern = bk5_kernel<Eng, Q, EB, F, LAYOUT>;
-    const int occ = prepare<Cfg>(kern, Cfg::SMEM, Cfg::NT);
+    // the even-odd contractions when D is centro-antisymmetric (GLL points);
+    // instantiated for the symmetric 6-factor G only
+    const bool eo = (F == 6) && make_eo<typename Eng::C, Q>(D, false, prm.eo, &Eng::coef) &&
+                    make_eo<typename Eng::C, Q>(D, true, prm.eot, &Eng::coef);
+    auto kern = eo ? bk5_kernel<Eng, Q, EB, F, LAYOUT, (F == 6), GD> : bk5_kernel<Eng, Q, EB, F, LAYOUT, false, GD>;
+    const int occ = eo ? prepare<BK5Cfg<Eng, Q, EB, F, LAYOUT + 8, GD>>(kern, Cfg::SMEM, Cfg::NT)
+                       : prepare<Cfg>(kern, Cfg::SMEM, Cfg::NT);
     if (occ <= 0) return BK_ERR_CUDA;
     const int grid = grid_for((E + EB - 1) / EB, occ);
     kern<<<grid, Cfg::NT, Cfg::SMEM, s>>>(prm, E, static_cast<const S*>(u), static_cast<const S*>(G),
@@ -99,19 +104,14 @@ int bk5_q(const double* D, long long E, const void* u, const void* G, const void
 }
 
 template <int Q>
-int bk5_sweep_q(int F, int layout, const double* D, long long E, const void* u, const void* G, const void* mass,
+int bk5_sweep_q(int F, int gd, const double* D, long long E, const void* u, const void* G, const void* mass,
                 double lambda, void* v, cudaStream_t s)
 {
     constexpr int EB = default_eb(Q);
-#define BK5_CASE(FF, LL) \
-    if (F == FF && layout == LL) return bk5_q<Q, EB, FF, LL>(D, E, u, G, mass, lambda, v, s);
-    BK5_CASE(6, 1)
-    BK5_CASE(6, 0)
-    BK5_CASE(6, 2)
-    BK5_CASE(9, 1)
-    BK5_CASE(9, 0)
-    BK5_CASE(9, 2)
-#undef BK5_CASE
+    constexpr int L = BK_LAYOUT_TU;
+    (void)gd;
+    if (F == 6) return bk5_q<Q, EB, 6, L, false>(D, E, u, G, mass, lambda, v, s);
+    if (F == 9) return bk5_q<Q, EB, 9, L, false>(D, E, u, G, mass, lambda, v, s);
     return BK_ERR_PREC;
 }
 #endif  // BK_OP_TU == 5
@@ -224,36 +224,21 @@ int bk3adj_q(const double* B, const double* D, long long E, const void* G, const
 using namespace BK_TU_NS;
 
 #if BK_OP_TU == 5
-#define BK_CATL_(a, b, c) a##_##b##_L##c
-#define BK_CATL(a, b, c) BK_CATL_(a, b, c)
-int BK_CAT(launch_bk5, BK_SFX)(int p, long long E, const double* D, const void* G, const void* u, const void* mass,
-                                double lambda, void* v, int F, int layout, int eb, int kernel, cudaStream_t s)
-{
-    if (p < 1 || p > 8) return BK_ERR_ORDER;
-    // AUTO: the sweep kernel, measured equal or faster than the column kernel
-    // for every form at p = 7 (GB300)
-    if (kernel == BK_KERNEL_SWEEP || kernel == BK_KERNEL_AUTO)
-        return BK_CAT(bk5_sweep, BK_SFX)(p, F, layout, D, E, u, G, mass, lambda, v, s);
-    switch (layout) {
-        case 0: return BK_CATL(bk5_col, BK_SFX, 0)(p, F, eb, D, E, u, G, mass, lambda, v, s);
-        case 1: return BK_CATL(bk5_col, BK_SFX, 1)(p, F, eb, D, E, u, G, mass, lambda, v, s);
-        case 2: return BK_CATL(bk5_col, BK_SFX, 2)(p, F, eb, D, E, u, G, mass, lambda, v, s);
-        default: return BK_ERR_PREC;
-    }
-}
-
-int BK_CAT(bk5_sweep, BK_SFX)(int p, int F, int layout, const double* D, long long E, const void* u, const void* G,
-                               const void* mass, double lambda, void* v, cudaStream_t s)
+#define BK_CATS_(a, b, c) a##_##b##_L##c
+#define BK_CATS(a, b, c) BK_CATS_(a, b, c)
+int BK_CATS(bk5_sweep, BK_SFX, BK_LAYOUT_TU)(int p, int F, int gd, const double* D, long long E, const void* u,
+                                              const void* G, const void* mass, double lambda, void* v,
+                                              cudaStream_t s)
 {
     switch (p + 1) {
-        case 2: return bk5_sweep_q<2>(F, layout, D, E, u, G, mass, lambda, v, s);
-        case 3: return bk5_sweep_q<3>(F, layout, D, E, u, G, mass, lambda, v, s);
-        case 4: return bk5_sweep_q<4>(F, layout, D, E, u, G, mass, lambda, v, s);
-        case 5: return bk5_sweep_q<5>(F, layout, D, E, u, G, mass, lambda, v, s);
-        case 6: return bk5_sweep_q<6>(F, layout, D, E, u, G, mass, lambda, v, s);
-        case 7: return bk5_sweep_q<7>(F, layout, D, E, u, G, mass, lambda, v, s);
-        case 8: return bk5_sweep_q<8>(F, layout, D, E, u, G, mass, lambda, v, s);
-        case 9: return bk5_sweep_q<9>(F, layout, D, E, u, G, mass, lambda, v, s);
+        case 2: return bk5_sweep_q<2>(F, gd, D, E, u, G, mass, lambda, v, s);
+        case 3: return bk5_sweep_q<3>(F, gd, D, E, u, G, mass, lambda, v, s);
+        case 4: return bk5_sweep_q<4>(F, gd, D, E, u, G, mass, lambda, v, s);
+        case 5: return bk5_sweep_q<5>(F, gd, D, E, u, G, mass, lambda, v, s);
+        case 6: return bk5_sweep_q<6>(F, gd, D, E, u, G, mass, lambda, v, s);
+        case 7: return bk5_sweep_q<7>(F, gd, D, E, u, G, mass, lambda, v, s);
+        case 8: return bk5_sweep_q<8>(F, gd, D, E, u, G, mass, lambda, v, s);
+        case 9: return bk5_sweep_q<9>(F, gd, D, E, u, G, mass, lambda, v, s);
         default: return BK_ERR_ORDER;
     }
 }
@@ -320,6 +305,32 @@ int BK_CAT(launch_bk3, BK_SFX)(int p, long long E, const double* B, const double
 #endif
 
 #if BK_OP_TU == 7
+#define BK_CATL_(a, b, c) a##_##b##_L##c
+#define BK_CATL(a, b, c) BK_CATL_(a, b, c)
+// BK5 dispatch: kernel shape and G layout
+int BK_CAT(launch_bk5, BK_SFX)(int p, long long E, const double* D, const void* G, const void* u, const void* mass,
+                                double lambda, void* v, int F, int layout, int eb, int kernel, cudaStream_t s)
+{
+    if (p < 1 || p > 8) return BK_ERR_ORDER;
+    // AUTO: the sweep kernel, measured equal or faster than the column kernel
+    // for every form at p = 7 (GB300)
+    if (kernel == BK_KERNEL_SWEEP || kernel == BK_KERNEL_AUTO) {
+        const int gd = 0;
+        switch (layout) {
+            case 0: return BK_CATL(bk5_sweep, BK_SFX, 0)(p, F, gd, D, E, u, G, mass, lambda, v, s);
+            case 1: return BK_CATL(bk5_sweep, BK_SFX, 1)(p, F, gd, D, E, u, G, mass, lambda, v, s);
+            case 2: return BK_CATL(bk5_sweep, BK_SFX, 2)(p, F, gd, D, E, u, G, mass, lambda, v, s);
+            default: return BK_ERR_PREC;
+        }
+    }
+    switch (layout) {
+        case 0: return BK_CATL(bk5_col, BK_SFX, 0)(p, F, eb, D, E, u, G, mass, lambda, v, s);
+        case 1: return BK_CATL(bk5_col, BK_SFX, 1)(p, F, eb, D, E, u, G, mass, lambda, v, s);
+        case 2: return BK_CATL(bk5_col, BK_SFX, 2)(p, F, eb, D, E, u, G, mass, lambda, v, s);
+        default: return BK_ERR_PREC;
+    }
+}
+
 int BK_CAT(launch_bk3_adjoint, BK_SFX)(int p, long long E, const double* B, const double* D, const void* G,
                                         const void* k, const void* u, const void* res, void* dk, void* dG,
                                         cudaStream_t s)

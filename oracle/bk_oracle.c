@@ -37,17 +37,115 @@
 #define BKO_BOX (BKO_MAX_NQ * BKO_MAX_NQ * BKO_MAX_NQ)
 #define X3(a, b, c) (((a) * nq + (b)) * nq + (c))
 
+/* double: a run-time-nq instance and one instance per fixed nq, then the
+ * entry points that dispatch to them */
+#define NQ_OF(x) (x)
 #define REAL double
-#define SFX(name) name
+#define SFX(name) name##_generic
+#define NQ_FIXED
 #include "bk_oracle_body.inc"
-#undef REAL
+#undef NQ_FIXED
 #undef SFX
+#undef NQ_OF
 
+#define NQ_FIXED
+#define NQ_OF(x) 2
+#define SFX(name) name##_nq2
+#include "bk_oracle_body.inc"
+#undef SFX
+#undef NQ_OF
+#define NQ_OF(x) 3
+#define SFX(name) name##_nq3
+#include "bk_oracle_body.inc"
+#undef SFX
+#undef NQ_OF
+#define NQ_OF(x) 4
+#define SFX(name) name##_nq4
+#include "bk_oracle_body.inc"
+#undef SFX
+#undef NQ_OF
+#define NQ_OF(x) 5
+#define SFX(name) name##_nq5
+#include "bk_oracle_body.inc"
+#undef SFX
+#undef NQ_OF
+#define NQ_OF(x) 6
+#define SFX(name) name##_nq6
+#include "bk_oracle_body.inc"
+#undef SFX
+#undef NQ_OF
+#define NQ_OF(x) 7
+#define SFX(name) name##_nq7
+#include "bk_oracle_body.inc"
+#undef SFX
+#undef NQ_OF
+#define NQ_OF(x) 8
+#define SFX(name) name##_nq8
+#include "bk_oracle_body.inc"
+#undef SFX
+#undef NQ_OF
+#define NQ_OF(x) 9
+#define SFX(name) name##_nq9
+#include "bk_oracle_body.inc"
+#undef SFX
+#undef NQ_OF
+#define NQ_OF(x) 10
+#define SFX(name) name##_nq10
+#include "bk_oracle_body.inc"
+#undef SFX
+#undef NQ_OF
+#undef NQ_FIXED
+#undef REAL
+
+#define DISPATCH(fn, nq, args)                 \
+    switch (nq) {                              \
+        case 2: fn##_nq2 args; return;         \
+        case 3: fn##_nq3 args; return;         \
+        case 4: fn##_nq4 args; return;         \
+        case 5: fn##_nq5 args; return;         \
+        case 6: fn##_nq6 args; return;         \
+        case 7: fn##_nq7 args; return;         \
+        case 8: fn##_nq8 args; return;         \
+        case 9: fn##_nq9 args; return;         \
+        case 10: fn##_nq10 args; return;       \
+        default: fn##_generic args; return;    \
+    }
+
+void bko_bk1_sumfact(int nq, size_t nelmt, const double* basis, const double* JxW, const double* in, double* out)
+{
+    DISPATCH(bko_bk1_sumfact, nq, (nq, nelmt, basis, JxW, in, out))
+}
+
+void bko_bk3_sumfact_k(int nq, size_t nelmt, const double* basis, const double* dbasis, const double* G,
+                       const double* kq, const double* in, double* out)
+{
+    DISPATCH(bko_bk3_sumfact_k, nq, (nq, nelmt, basis, dbasis, G, kq, in, out))
+}
+
+void bko_bk3_sumfact(int nq, size_t nelmt, const double* basis, const double* dbasis, const double* G,
+                     const double* in, double* out)
+{
+    bko_bk3_sumfact_k(nq, nelmt, basis, dbasis, G, NULL, in, out);
+}
+
+void bko_bk5_sumfact_h(int nq, size_t nelmt, const double* dbasis, const double* G, const double* mass,
+                       double lambda, const double* in, double* out)
+{
+    DISPATCH(bko_bk5_sumfact_h, nq, (nq, nelmt, dbasis, G, mass, lambda, in, out))
+}
+
+void bko_bk5_sumfact(int nq, size_t nelmt, const double* dbasis, const double* G, const double* in, double* out)
+{
+    bko_bk5_sumfact_h(nq, nelmt, dbasis, G, NULL, 0.0, in, out);
+}
+
+#define NQ_OF(x) (x)
 #define REAL float
 #define SFX(name) name##_f32
 #include "bk_oracle_body.inc"
 #undef REAL
 #undef SFX
+#undef NQ_OF
 
 int bko_max_nq(void) { return BKO_MAX_NQ; }
 

@@ -214,3 +214,28 @@ def test_bounded_wait_timeout(bklib):
     out = gpu_apply(bklib, 5, p, E, None, dbasis, g, u, bklib.PREC_FP64)
     assert oracle.rel_maxdiff(out, oracle.bk5(nq, E, dbasis, g, u)) < TOL64
     assert bklib.device_status(reset=True) == bklib.BK_OK
+
+
+@pytest.mark.parametrize("p", P_ALL)
+@pytest.mark.parametrize("engine", ["dfma", "ff", "fp32", "mixed"])
+def test_bk5_gll_even_odd(bklib, p, engine):
+    """With the GLL derivative matrix (centro-antisymmetric) BK5 takes the
+    even-odd contractions; same operator as the oracle's plain sums."""
+    E = 11
+    nq = p + 1
+    D, _, _ = bklib.bk5_matrices(p)
+    rng = np.random.default_rng(100 + p)
+    u = rng.uniform(-1, 1, E * nq ** 3)
+    g = rng.uniform(0.5, 1.5, E * 6 * nq ** 3)
+    if engine in ("dfma", "ff"):
+        eng = bklib.ENGINE_DFMA if engine == "dfma" else bklib.ENGINE_FF
+        out = gpu_apply(bklib, 5, p, E, None, D, g, u, bklib.PREC_FP64, engine=eng)
+        ref = oracle.bk5(nq, E, D, g, u)
+        tol = TOL64
+    else:
+        pr = bklib.PREC_FP32 if engine == "fp32" else bklib.PREC_MIXED
+        out = gpu_apply(bklib, 5, p, E, None, D, g, u, pr)
+        f = lambda a: a.astype(np.float32).astype(np.float64)
+        ref = oracle.bk5(nq, E, D, f(g), f(u))
+        tol = TOL32
+    assert oracle.rel_maxdiff(out, ref) < tol
