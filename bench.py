@@ -344,12 +344,22 @@ def run_bk3(args):
     G32 = G.float()
     v32 = torch.empty(E * P ** 3, dtype=torch.float32, device="cuda")
     errs = {}
+    G32d = G32.double()
+    vr = torch.empty_like(v)
     for name, uu in (("random", u_rand), ("smooth", u_smooth)):
         bk.bk3_apply(p, E, B, D, G, uu, v)
         u32 = uu.float()
         bk.bk3_apply(p, E, B, D, G32, u32, v32, prec=bk.PREC_MIXED)
         mx, rms = _rel(v32, v)
-        errs[name] = {"rel_max": mx, "rel_rms": rms}
+        # the same split for FP64 applied to the FP32-rounded inputs: the
+        # part of the error that storing u and G in FP32 causes by itself
+        # (large for smooth u, whose image cancels) and the part the FP32
+        # arithmetic adds
+        bk.bk3_apply(p, E, B, D, G32d, u32.double(), vr)
+        mx_in, rms_in = _rel(vr, v)
+        mx_ar, rms_ar = _rel(v32, vr)
+        errs[name] = {"rel_max": mx, "rel_rms": rms, "input_rounding_rel_max": mx_in,
+                      "input_rounding_rel_rms": rms_in, "arithmetic_rel_max": mx_ar, "arithmetic_rel_rms": rms_ar}
     mm = _events_ms(lambda: bk.bk3_apply(p, E, B, D, G32, u32, v32, prec=bk.PREC_MIXED), steps, warm, torch)
     vd = torch.empty_like(v)
     md = _events_ms(lambda: bk.bk3_apply(p, E, B, D, G, u_smooth, vd, engine=bk.ENGINE_DFMA), max(3, steps // 4),
@@ -452,6 +462,15 @@ def run_helmholtz(args):
     aligned = all((o * 8) % 16 == 0 for o in plan.uoff) and all((o * 8) % 16 == 0 for o in plan.goff)
     m_per64 = _events_ms(lambda: per_order(bk.PREC_FP64, G, M, ustar, v64), max(3, steps // 4), 2, torch) \
         if aligned else None
+    aligned32 = all((o * 4) % 16 == 0 for o in plan.uoff) and all((o * 4) % 16 == 0 for o in plan.goff)
+    m_per32 = _events_ms(lambda: per_order(bk.PREC_MIXED, G32, M32, u32, v32), steps, warm, torch) \
+        if aligned32 else None
+    # the column body of the same launch (tiles tuned for it)
+    best_col = tune.tune(orders, kernel=bk.KERNEL_COLUMN)
+    plan_col = hz.HelmholtzPlan([(p, E, best_col[p]) for p, E in orders])
+    plan_col.set_kernel(bk.KERNEL_COLUMN)
+    m_col = _events_ms(lambda: plan_col.apply(G32, M32, 1.0, u32, v32, prec=bk.PREC_MIXED), steps, warm, torch)
+    plan_col.close()
     x = torch.zeros_like(ustar)
     plan.cg(G, M, G32, M32, 1.0, f, x, rtol=1e-10, allow_noconv=True)   # builds the graph
     x.zero_()
@@ -464,7 +483,10 @@ def run_helmholtz(args):
     _line(args, f"mixed-order Helmholtz p=2..8, E_p=2^(8-p)*4096 ({plan.n} DoFs), one persistent launch",
           plan.n / m_multi / 1e6, m_multi, "f32",
           {"helmholtz": {"dofs": plan.n, "tiles": plan.ntiles, "tile_elems": best,
+                         "kernel": {bk.KERNEL_SWEEP: "sweep (even-odd)", bk.KERNEL_COLUMN: "column"}[plan.kernel],
                          "multi_mixed_gdofs": plan.n / m_multi / 1e6, "multi_fp64_gdofs": plan.n / m_multi64 / 1e6,
+                         "multi_mixed_column_gdofs": plan.n / m_col / 1e6, "tile_elems_column": best_col,
+                         "per_order_mixed_gdofs": (plan.n / m_per32 / 1e6) if m_per32 else None,
                          "per_order_fp64_gdofs": (plan.n / m_per64 / 1e6) if m_per64 else None,
                          "cg": st, "cg_seconds": solve_s, "solution_rel_err": err}})
 

@@ -23,7 +23,7 @@ typedef struct bk_order_range {
     int p;               /* polynomial order, 2..8 (q = p + 1 points) */
     int64_t E;           /* elements of this order */
     int elems_per_tile;  /* elements per tile of the persistent launch, with
-                            elems_per_tile * q^2 <= 256; 0: 256 / q^2 */
+                            elems_per_tile * q^2 <= 256; 0: about 128 / q^2 */
 } bk_order_range;
 
 typedef struct bk_hplan* bk_hplan_t;
@@ -35,8 +35,16 @@ typedef struct bk_hplan* bk_hplan_t;
 int bk_hplan_create(bk_hplan_t* plan, int norders, const bk_order_range* orders, const double* const* D,
                     bk_stream_t stream);
 int bk_hplan_destroy(bk_hplan_t plan);
-/* what = 0: values of a vector (sum E_p q^3); 1: values of G; 2: tiles. */
+/* what = 0: values of a vector (sum E_p q^3); 1: values of G; 2: tiles;
+ * 3: the kernel shape of the applies (BK_KERNEL_SWEEP or BK_KERNEL_COLUMN). */
 long long bk_hplan_size(bk_hplan_t plan, int what);
+
+/* The body of the persistent launch: BK_KERNEL_SWEEP (line sweeps in the
+ * even-odd form, half the multiply-adds; needs every D centro-antisymmetric,
+ * which GLL derivatives are, BK_ERR_ARG otherwise), BK_KERNEL_COLUMN (one
+ * thread per k-column, any D) or BK_KERNEL_AUTO (SWEEP when possible: the
+ * default of a new plan). */
+int bk_hplan_set_kernel(bk_hplan_t plan, int kernel);
 
 /* v = A u for all orders in ONE persistent launch.  prec BK_PREC_FP64 (engine
  * AUTO/FF: float-float, DFMA: native), BK_PREC_MIXED or BK_PREC_FP32 (float

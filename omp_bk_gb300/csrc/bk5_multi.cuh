@@ -10,6 +10,13 @@
 // bk5_col.cuh for the tile's order.  The operator is BK5 plus lambda times the
 // collocated mass (the Helmholtz operator), G in the column layout
 // G(e, f, k, i, j).
+//
+// bk5_multi_eo_kernel is the same launch over the sweep body of
+// bk_kernels.cuh (bk5_sweep_batch) in its even-odd form, for derivative
+// matrices that are centro-antisymmetric (every GLL D is): half the
+// multiply-adds of the column body's derivative contractions.  One stage
+// buffer per block; the overlap of copies and compute comes from the blocks
+// resident on each SM, as in the single-order launches.
 #pragma once
 
 #include "bk5_col.cuh"
@@ -170,6 +177,140 @@ inline void multi_smem(const MultiSeg* seg, int nseg, int& stage_bytes_, int& co
     stage_bytes_ = (stage_bytes_ + 15) / 16 * 16;
     col_bytes = (col_bytes + 15) / 16 * 16;
     total = nbuf * stage_bytes_ + 3 * col_bytes + ((kMultiDTotal * int(sizeof(V)) + 15) / 16) * 16 + 16 * nbuf;
+}
+
+// ---- even-odd sweep body -------------------------------------------------------
+
+template <class C, int Q>
+struct EOPair {
+    EOMat<C, Q> eo;    // D
+    EOMat<C, Q> eot;   // D^T
+};
+
+template <class C>
+struct EOSet : EOPair<C, 3>, EOPair<C, 4>, EOPair<C, 5>, EOPair<C, 6>, EOPair<C, 7>, EOPair<C, 8>, EOPair<C, 9> {
+    template <int Q>
+    __host__ __device__ const EOPair<C, Q>& at() const
+    {
+        return *static_cast<const EOPair<C, Q>*>(this);
+    }
+    template <int Q>
+    EOPair<C, Q>& at()
+    {
+        return *static_cast<EOPair<C, Q>*>(this);
+    }
+};
+
+template <class C>
+struct PMultiEO {
+    EOSet<C> eo;
+    MultiSeg seg[kMultiNQ];
+    int nseg;
+};
+
+// Host: the even-odd forms of D_q (D(i, n) = d[i*q + n]) into P; false if D_q
+// is not centro-antisymmetric.
+template <class C, class Conv>
+inline bool multi_eo_fill(EOSet<C>& P, int q, const double* d, Conv conv)
+{
+    switch (q) {
+#define BK_MULTI_EO_FILL(QQ) \
+    case QQ: return make_eo<C, QQ>(d, false, P.template at<QQ>().eo, conv) && make_eo<C, QQ>(d, true, P.template at<QQ>().eot, conv);
+        BK_MULTI_EO_FILL(3)
+        BK_MULTI_EO_FILL(4)
+        BK_MULTI_EO_FILL(5)
+        BK_MULTI_EO_FILL(6)
+        BK_MULTI_EO_FILL(7)
+        BK_MULTI_EO_FILL(8)
+        BK_MULTI_EO_FILL(9)
+#undef BK_MULTI_EO_FILL
+        default: return false;
+    }
+}
+
+// Bytes of one padded work box of eb elements of order q for values of vbytes.
+inline int multi_wbox_bytes(int q, int eb, int vbytes)
+{
+    return eb * q * box_ps(q, vbytes) * vbytes;
+}
+
+// Shared memory of the even-odd launch: u stage, G stage, three work boxes
+// (each the largest tile's), one mbarrier.
+template <class Eng>
+inline void multi_eo_smem(const MultiSeg* seg, int nseg, int& u_bytes, int& g_bytes, int& w_bytes, int& total)
+{
+    using S = typename Eng::S;
+    using V = typename Eng::V;
+    u_bytes = 16;
+    g_bytes = 16;
+    w_bytes = 16;
+    for (int s = 0; s < nseg; ++s) {
+        const int q = seg[s].q, eb = seg[s].eb, q3 = q * q * q;
+        const int ub = stage_bytes<S>(eb * q3), gb = stage_bytes<S>(eb * 6 * q3);
+        const int wb = (multi_wbox_bytes(q, eb, int(sizeof(V))) + 15) / 16 * 16;
+        u_bytes = ub > u_bytes ? ub : u_bytes;
+        g_bytes = gb > g_bytes ? gb : g_bytes;
+        w_bytes = wb > w_bytes ? wb : w_bytes;
+    }
+    total = u_bytes + g_bytes + 3 * w_bytes + 16;
+}
+
+template <class Eng, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
+    bk5_multi_eo_kernel(const __grid_constant__ PMultiEO<typename Eng::C> prm, const MultiTile* __restrict__ tiles,
+                        const int ntiles, const typename Eng::S* __restrict__ u, const typename Eng::S* __restrict__ G,
+                        const typename Eng::S* __restrict__ mass, const double lambda,
+                        typename Eng::S* __restrict__ v, const int u_bytes, const int g_bytes, const int w_bytes,
+                        const DevCtx ctx)
+{
+    using S = typename Eng::S;
+    using V = typename Eng::V;
+    extern __shared__ __align__(16) unsigned char smem[];
+    unsigned char* ustage = smem;
+    unsigned char* gstage = smem + u_bytes;
+    V* W0 = reinterpret_cast<V*>(gstage + g_bytes);
+    V* W1 = reinterpret_cast<V*>(reinterpret_cast<unsigned char*>(W0) + w_bytes);
+    V* W2 = reinterpret_cast<V*>(reinterpret_cast<unsigned char*>(W1) + w_bytes);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(reinterpret_cast<unsigned char*>(W2) + w_bytes);
+    const int tid = threadIdx.x;
+    const int nt = blockDim.x;   // the largest tile's lines, at most NT
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    uint32_t phase = 0;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, phase ^= 1u) {
+        const MultiTile tl = tiles[t];
+        const MultiSeg& sg = prm.seg[tl.seg];
+        const int q = sg.q;
+        const int q3 = q * q * q;
+        uint32_t tx = 0;
+        if (tid == 0) fence_proxy_async();
+        const S* us = stage_issue<S>(ustage, u + sg.uoff + tl.e_first * q3, tl.ne * q3, bar, tx, tid, nt);
+        const S* gs = stage_issue<S>(gstage, G + sg.goff + tl.e_first * 6 * q3, tl.ne * 6 * q3, bar, tx, tid, nt);
+        if (tid == 0) mbar_arrive_expect_tx(bar, tx);
+        if (batch_wait_failed(bar, phase, ctx, tid)) return;
+        S* vb = v + sg.uoff + tl.e_first * q3;
+        const S* mb = (mass != nullptr) ? mass + sg.uoff + tl.e_first * q3 : nullptr;
+        switch (q) {
+#define BK_MULTI_EO_CASE(QQ)                                                                                    \
+    case QQ:                                                                                                    \
+        bk5_sweep_batch<Eng, QQ, 6, 2, true>(nullptr, prm.eo.template at<QQ>().eo, prm.eo.template at<QQ>().eot, \
+                                             us, gs, W0, W1, W2, tl.ne, tid, nt, vb, mb, lambda);               \
+        break;
+            BK_MULTI_EO_CASE(3)
+            BK_MULTI_EO_CASE(4)
+            BK_MULTI_EO_CASE(5)
+            BK_MULTI_EO_CASE(6)
+            BK_MULTI_EO_CASE(7)
+            BK_MULTI_EO_CASE(8)
+            BK_MULTI_EO_CASE(9)
+#undef BK_MULTI_EO_CASE
+            default:
+                break;
+        }
+    }
 }
 
 }  // namespace bkg

@@ -5,7 +5,8 @@
 // q^3 values in the column layout), cut into tiles whose sizes per order
 // come from the caller (the autotuner of omp_bk_gb300.tune).  The apply
 // v = D^T G D u + lambda mass u is ONE persistent launch over the tile list
-// (bk5_multi.cuh).
+// (bk5_multi.cuh): the even-odd sweep body when every D is
+// centro-antisymmetric (GLL), the column body otherwise or on request.
 //
 // The solver is conjugate gradients in mixed precision with FP64 residual
 // refinement: the outer loop forms the FP64 residual r = f - A x with the
@@ -91,6 +92,79 @@ struct MultiLaunch {
         if (grid < 1) return BK_OK;
         kern<<<grid, kNT, total, s>>>(prm, tiles, ntiles, static_cast<const S*>(u), static_cast<const S*>(G),
                                       static_cast<const S*>(mass), lambda, static_cast<S*>(v), st, cb, dev_ctx());
+        return cudaGetLastError() == cudaSuccess ? BK_OK : BK_ERR_CUDA;
+    }
+};
+
+// The even-odd sweep launch: blockDim = the largest tile's lines (eb q^2),
+// rounded up to whole warps; MAXT threads at most, MINB blocks per SM asked
+// of the register allocator.
+template <class Eng, int MAXT, int MINB>
+struct MultiEOLaunch {
+    static int threads(const MultiSeg* seg, int nseg)
+    {
+        int nt = 64;
+        for (int s = 0; s < nseg; ++s) {
+            const int l = (seg[s].eb * seg[s].q * seg[s].q + 31) / 32 * 32;
+            nt = l > nt ? l : nt;
+        }
+        return nt;
+    }
+    static int smem(const PMultiEO<typename Eng::C>& prm, int& ub, int& gb, int& wb)
+    {
+        int total = 0;
+        multi_eo_smem<Eng>(prm.seg, prm.nseg, ub, gb, wb, total);
+        return total;
+    }
+    static int prepare(int total, int nt)
+    {
+        auto kern = bk5_multi_eo_kernel<Eng, MAXT, MINB>;
+        static int set[kMaxDevices] = {0};
+        static int occ_of[kMaxDevices][3] = {{0, 0, 0}};
+        const int dev = current_device();
+        if (dev < 0 || dev >= kMaxDevices) return 0;
+        if (!set[dev]) {
+            if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448) != cudaSuccess) {
+                cudaGetLastError();
+                return 0;
+            }
+            set[dev] = 1;
+        }
+        if (occ_of[dev][0] != total || occ_of[dev][1] != nt) {
+            int occ = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, nt, total) != cudaSuccess) {
+                cudaGetLastError();
+                return 0;
+            }
+            occ_of[dev][0] = total;
+            occ_of[dev][1] = nt;
+            occ_of[dev][2] = occ;
+        }
+        return occ_of[dev][2];
+    }
+    static int prepare(const PMultiEO<typename Eng::C>& prm)
+    {
+        int ub = 0, gb = 0, wb = 0;
+        const int total = smem(prm, ub, gb, wb);
+        if (total > 232448) return 0;
+        return prepare(total, threads(prm.seg, prm.nseg));
+    }
+    static int run(const PMultiEO<typename Eng::C>& prm, const MultiTile* tiles, int ntiles, const void* u,
+                   const void* G, const void* mass, double lambda, void* v, cudaStream_t s)
+    {
+        using S = typename Eng::S;
+        int ub = 0, gb = 0, wb = 0;
+        const int total = smem(prm, ub, gb, wb);
+        const int nt = threads(prm.seg, prm.nseg);
+        if (total > 232448 || nt > MAXT) return BK_ERR_ARG;
+        auto kern = bk5_multi_eo_kernel<Eng, MAXT, MINB>;
+        const int occ = prepare(total, nt);
+        if (occ < 1) return BK_ERR_CUDA;
+        int grid = occ * sm_count();
+        if (grid > ntiles) grid = ntiles;
+        if (grid < 1) return BK_OK;
+        kern<<<grid, nt, total, s>>>(prm, tiles, ntiles, static_cast<const S*>(u), static_cast<const S*>(G),
+                                     static_cast<const S*>(mass), lambda, static_cast<S*>(v), ub, gb, wb, dev_ctx());
         return cudaGetLastError() == cudaSuccess ? BK_OK : BK_ERR_CUDA;
     }
 };
@@ -297,6 +371,12 @@ struct bk_hplan {
     PMulti<double> p_dfma;
     PMulti<ff> p_ff;
     PMulti<float> p_f32;
+    // the even-odd forms (valid when eo_ok)
+    PMultiEO<double> e_dfma;
+    PMultiEO<ff> e_ff;
+    PMultiEO<float> e_f32;
+    bool eo_ok;
+    int kernel;         // BK_KERNEL_SWEEP (even-odd) or BK_KERNEL_COLUMN
     // solver state
     double* r64;
     float* r32;
@@ -326,6 +406,19 @@ void fill_params(PMulti<C>& P, const bk_hplan& h, const double* const* Dq, C (*c
     P.nseg = h.nseg;
 }
 
+template <class C, class Conv>
+bool fill_eo_params(PMultiEO<C>& P, const bk_hplan& h, const double* const* Dq, Conv conv)
+{
+    std::memset(&P, 0, sizeof(P));
+    bool ok = true;
+    for (int s = 0; s < h.nseg; ++s) {
+        ok = multi_eo_fill(P.eo, h.seg[s].q, Dq[s], conv) && ok;
+        P.seg[s] = h.seg[s];
+    }
+    P.nseg = h.nseg;
+    return ok;
+}
+
 double conv_d(double x) { return x; }
 float conv_f(double x) { return float(x); }
 ff conv_ff(double x) { return EngFF::coef(x); }
@@ -333,6 +426,15 @@ ff conv_ff(double x) { return EngFF::coef(x); }
 int apply_plan(bk_hplan* h, int eng, const void* G, const void* mass, double lambda, const void* u, void* v,
                cudaStream_t s)
 {
+    if (h->kernel == BK_KERNEL_SWEEP) {
+        switch (eng) {
+            case 0: return MultiEOLaunch<EngDfma, 256, 2>::run(h->e_dfma, h->tiles, h->ntiles, u, G, mass, lambda, v, s);
+            case 1: return MultiEOLaunch<EngFF, 256, 2>::run(h->e_ff, h->tiles, h->ntiles, u, G, mass, lambda, v, s);
+            case 2: return MultiEOLaunch<EngF32, 256, 2>::run(h->e_f32, h->tiles, h->ntiles, u, G, mass, lambda, v, s);
+            default:
+                return MultiEOLaunch<EngMixed, 256, 2>::run(h->e_f32, h->tiles, h->ntiles, u, G, mass, lambda, v, s);
+        }
+    }
     switch (eng) {
         case 0: return MultiLaunch<EngDfma, 1>::run(h->p_dfma, h->tiles, h->ntiles, u, G, mass, lambda, v, s);
         case 1: return MultiLaunch<EngFF, 1>::run(h->p_ff, h->tiles, h->ntiles, u, G, mass, lambda, v, s);
@@ -359,8 +461,11 @@ int build_inner_graph(bk_hplan* h, const void* G32, const void* mass32, double l
     {
         // kernel attributes and occupancy outside the capture
         int st = 0, cb = 0;
-        if (MultiLaunch<EngMixed, 2>::prepare(MultiLaunch<EngMixed, 2>::smem(h->p_f32, st, cb)) < 1)
+        if (h->kernel == BK_KERNEL_SWEEP) {
+            if (MultiEOLaunch<EngMixed, 256, 2>::prepare(h->e_f32) < 1) return BK_ERR_CUDA;
+        } else if (MultiLaunch<EngMixed, 2>::prepare(MultiLaunch<EngMixed, 2>::smem(h->p_f32, st, cb)) < 1) {
             return BK_ERR_CUDA;
+        }
     }
     // the legacy default stream cannot be captured: capture on a private
     // stream (the graph is launched on the caller's stream)
@@ -474,7 +579,7 @@ int bk_hplan_create(bk_hplan_t* out, int norders, const bk_order_range* orders, 
         }
         const int q = p + 1;
         int eb = orders[s].elems_per_tile;
-        if (eb <= 0) eb = (kNT / (q * q)) > 0 ? kNT / (q * q) : 1;
+        if (eb <= 0) eb = (q * q >= 100) ? 1 : ((q * q >= 64) ? 2 : (128 + q * q - 1) / (q * q));
         if (eb * q * q > kNT || orders[s].E < 0 || !D[s]) {
             delete h;
             return orders[s].E < 0 ? BK_ERR_SIZE : BK_ERR_ARG;
@@ -508,6 +613,9 @@ int bk_hplan_create(bk_hplan_t* out, int norders, const bk_order_range* orders, 
     fill_params(h->p_dfma, *h, D, conv_d);
     fill_params(h->p_ff, *h, D, conv_ff);
     fill_params(h->p_f32, *h, D, conv_f);
+    h->eo_ok = fill_eo_params(h->e_dfma, *h, D, conv_d) && fill_eo_params(h->e_ff, *h, D, conv_ff) &&
+               fill_eo_params(h->e_f32, *h, D, conv_f);
+    h->kernel = h->eo_ok ? BK_KERNEL_SWEEP : BK_KERNEL_COLUMN;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     int rc = BK_OK;
     const size_t nb = size_t(h->n);
@@ -554,7 +662,23 @@ long long bk_hplan_size(bk_hplan_t h, int what)
     if (what == 0) return h->n;
     if (what == 1) return h->ng;
     if (what == 2) return h->ntiles;
+    if (what == 3) return h->kernel;
     return -1;
+}
+
+int bk_hplan_set_kernel(bk_hplan_t h, int kernel)
+{
+    if (!h) return BK_ERR_NULL;
+    int k;
+    if (kernel == BK_KERNEL_AUTO) k = h->eo_ok ? BK_KERNEL_SWEEP : BK_KERNEL_COLUMN;
+    else if (kernel == BK_KERNEL_COLUMN) k = BK_KERNEL_COLUMN;
+    else if (kernel == BK_KERNEL_SWEEP && h->eo_ok) k = BK_KERNEL_SWEEP;
+    else return BK_ERR_ARG;
+    if (k != h->kernel) {
+        free_graph(h);
+        h->kernel = k;
+    }
+    return BK_OK;
 }
 
 int bk_hplan_apply(bk_hplan_t h, const void* G, const void* mass, double lambda, const void* u, void* v, int prec,

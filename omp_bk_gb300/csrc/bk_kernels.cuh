@@ -237,6 +237,107 @@ __device__ __forceinline__ void sweep_eo(const typename Eng::V* in, typename Eng
     }
 }
 
+// Even-odd form of a rectangular NO x NI matrix with M(NO-1-o, NI-1-n) =
+// SIGN M(o, n): the interpolation matrix between point sets symmetric about 0
+// (SIGN = +1) and the derivative matrix (SIGN = -1), or their transposes.
+// With HI = NI/2, HO = NO/2, e(n) = x(n) + x(NI-1-n), d(n) = x(n) - x(NI-1-n):
+//   a(o) = sum_n A(o,n) e(n) + c(o) x(HI),   b(o) = sum_n B(o,n) d(n),
+//   out(o) = a(o) + b(o),   out(NO-1-o) = SIGN (a(o) - b(o)),
+// and for odd NO the middle row out(HO) = sum_n r(n) e(n) + rm x(HI) (SIGN
+// +1) or sum_n r(n) d(n) (SIGN -1); x(HI) exists for odd NI only.
+template <class C, int NO, int NI>
+struct EORMat {
+    static constexpr int HO = NO / 2;
+    static constexpr int HI = NI / 2;
+    C A[HO * HI > 0 ? HO * HI : 1];
+    C B[HO * HI > 0 ? HO * HI : 1];
+    C c[HO > 0 ? HO : 1];
+    C r[HI > 0 ? HI : 1];
+    C rm;
+};
+
+// Host side: the even-odd form of M(o, n) = m[o*ld + n] (trans: m[n*ld + o]);
+// true if M(NO-1-o, NI-1-n) = sign M(o, n) to within 1e-13 of its largest
+// entry.
+template <class C, int NO, int NI, class Conv>
+inline bool make_eor(const double* m, int ld, bool trans, int sign, EORMat<C, NO, NI>& out, Conv conv)
+{
+    constexpr int HO = NO / 2, HI = NI / 2;
+    auto M = [&](int o, int n) { return trans ? m[n * ld + o] : m[o * ld + n]; };
+    auto fab = [](double x) { return x < 0 ? -x : x; };
+    double big = 0, dev = 0;
+    for (int o = 0; o < NO; ++o)
+        for (int n = 0; n < NI; ++n) {
+            big = big > fab(M(o, n)) ? big : fab(M(o, n));
+            const double a = M(NO - 1 - o, NI - 1 - n) - sign * M(o, n);
+            dev = dev > fab(a) ? dev : fab(a);
+        }
+    for (int o = 0; o < HO; ++o) {
+        for (int n = 0; n < HI; ++n) {
+            out.A[o * HI + n] = conv(0.5 * (M(o, n) + M(o, NI - 1 - n)));
+            out.B[o * HI + n] = conv(0.5 * (M(o, n) - M(o, NI - 1 - n)));
+        }
+        out.c[o] = conv((NI & 1) ? M(o, HI) : 0.0);
+    }
+    for (int n = 0; n < HI; ++n) out.r[n] = conv((NO & 1) ? M(HO, n) : 0.0);
+    out.rm = conv(((NO & 1) && (NI & 1)) ? M(HO, HI) : 0.0);
+    return dev <= 1e-13 * big;
+}
+
+// Even-odd sweep of direction DIR of the (X, Y, Z) box into extent NO along
+// DIR (see EORMat; in == out allowed).
+template <class Eng, class WB, int DIR, int X, int Y, int Z, int NO, int SIGN, class EM>
+__device__ __forceinline__ void sweep_eor(const typename Eng::V* in, typename Eng::V* out, int ne, const EM& m,
+                                          int tid, int nt)
+{
+    using V = typename Eng::V;
+    using A = typename Eng::A;
+    constexpr int NI = DIR == 0 ? X : (DIR == 1 ? Y : Z);
+    constexpr int HI = NI / 2, HO = NO / 2;
+    constexpr int LB = DIR == 2 ? Y : Z;
+    constexpr int L = (X * Y * Z) / NI;
+    constexpr int SD = DIR == 0 ? WB::PS : (DIR == 1 ? WB::ZP : 1);
+    for (int w = tid; w < ne * L; w += nt) {
+        const int e = w / L;
+        const int l = w - e * L;
+        const int a = l / LB;
+        const int b = l - a * LB;
+        int base = (DIR == 0) ? a * WB::ZP + b : (DIR == 1 ? a * WB::PS + b : a * WB::PS + b * WB::ZP);
+        base += e * WB::size;
+        V x[NI];
+#pragma unroll
+        for (int n = 0; n < NI; ++n) x[n] = in[base + n * SD];
+        V ev[HI > 0 ? HI : 1], dv[HI > 0 ? HI : 1];
+#pragma unroll
+        for (int n = 0; n < HI; ++n) {
+            ev[n] = Eng::vadd(x[n], x[NI - 1 - n]);
+            dv[n] = Eng::vsub(x[n], x[NI - 1 - n]);
+        }
+        V mid_out;
+        if constexpr ((NO & 1) != 0) {
+            A t = Eng::zero();
+#pragma unroll
+            for (int n = 0; n < HI; ++n) Eng::madd(t, m.r[n], SIGN > 0 ? ev[n] : dv[n]);
+            if constexpr (SIGN > 0 && (NI & 1) != 0) Eng::madd(t, m.rm, x[HI]);
+            mid_out = Eng::result(t);
+        }
+#pragma unroll
+        for (int o = 0; o < HO; ++o) {
+            A aa = Eng::zero(), bb = Eng::zero();
+#pragma unroll
+            for (int n = 0; n < HI; ++n) {
+                Eng::madd(aa, m.A[o * HI + n], ev[n]);
+                Eng::madd(bb, m.B[o * HI + n], dv[n]);
+            }
+            if constexpr ((NI & 1) != 0) Eng::madd(aa, m.c[o], x[HI]);
+            const V av = Eng::result(aa), bv = Eng::result(bb);
+            out[base + o * SD] = Eng::vadd(av, bv);
+            out[base + (NO - 1 - o) * SD] = SIGN > 0 ? Eng::vsub(av, bv) : Eng::vsub(bv, av);
+        }
+        if constexpr ((NO & 1) != 0) out[base + HO * SD] = mid_out;
+    }
+}
+
 // Dense (X, Y, Z) slice of S values of `ne` elements (element stride estride)
 // -> padded work box, converted to the working type.
 template <class Eng, class WB, int X, int Y, int Z>
@@ -272,12 +373,6 @@ __device__ __forceinline__ void store_box(const typename Eng::V* src, typename E
     }
 }
 
-template <class S>
-__device__ __forceinline__ void store_out(const S* src, S* dst, int n, int tid, int nt)
-{
-    for (int i = tid; i < n; i += nt) dst[i] = src[i];
-}
-
 // Waits (bounded) for the batch's staged copies; the block agrees on the
 // outcome with one barrier.  On a timeout the status word records
 // BK_ERR_TIMEOUT, every thread waits once more (bounded) so that copies still
@@ -307,7 +402,26 @@ template <class C, int Q>
 struct P13 {
     C B[(Q - 1) * Q];   // B(i, p) = B[i*Q + p]
     C D[Q * Q];         // BK3: D(n, p) = D[n*Q + p]
+    // even-odd forms (used when the kernel's EO is set): interpolation
+    // M(p, i) = B(i, p) and its transpose, gradient M(p, n) = D(n, p) and its
+    // transpose
+    EORMat<C, Q, Q - 1> bi;
+    EORMat<C, Q - 1, Q> bb;
+    EORMat<C, Q, Q> dg;
+    EORMat<C, Q, Q> dtr;
 };
+
+// Host: the even-odd forms of P13; true if B is centro-symmetric and D
+// centro-antisymmetric (point sets symmetric about 0).
+template <class C, int Q, class Conv>
+inline bool make_p13_eo(P13<C, Q>& p, const double* B, const double* D, Conv conv)
+{
+    bool ok = make_eor<C, Q, Q - 1>(B, Q, true, +1, p.bi, conv);
+    ok = make_eor<C, Q - 1, Q>(B, Q, false, +1, p.bb, conv) && ok;
+    ok = make_eor<C, Q, Q>(D, Q, true, -1, p.dg, conv) && ok;
+    ok = make_eor<C, Q, Q>(D, Q, false, -1, p.dtr, conv) && ok;
+    return ok;
+}
 
 // ---- BK5 -----------------------------------------------------------------------
 
@@ -321,8 +435,10 @@ __device__ __forceinline__ int g_index(int i, int j, int f, int k)
 
 // GD: G read from global memory in the pointwise stage (coalesced in every
 // layout: points are walked in G's own order) instead of staged by TMA, which
-// leaves the block's shared memory to u and the work boxes.
-template <class Eng, int Q, int EB, int F, int LAYOUT, bool GD = false>
+// leaves the block's shared memory to u and the work boxes.  NBUF: stage
+// buffers (2: the block's next batch is copied while it computes the
+// current one).
+template <class Eng, int Q, int EB, int F, int LAYOUT, bool GD = false, int NBUF = 1>
 struct BK5Cfg {
     using S = typename Eng::S;
     using V = typename Eng::V;
@@ -331,160 +447,222 @@ struct BK5Cfg {
     static constexpr int NT = ((EB * Q * Q + 31) / 32) * 32 < 64 ? 64 : ((EB * Q * Q + 31) / 32) * 32;
     static constexpr int U_BYTES = stage_bytes<S>(EB * Q3);
     static constexpr int G_BYTES = GD ? 0 : stage_bytes<S>(EB * F * Q3);
+    static constexpr int STAGE_BYTES = U_BYTES + G_BYTES;
     static constexpr int W_BYTES = 3 * EB * WB::size * int(sizeof(V));
-    static constexpr int SMEM = U_BYTES + G_BYTES + W_BYTES + 16;
+    static constexpr int SMEM = NBUF * STAGE_BYTES + W_BYTES + 16 * NBUF;
 };
 
-template <class Eng, int Q, int EB, int F, int LAYOUT, bool EO = false, bool GD = false>
-__global__ void __launch_bounds__(BK5Cfg<Eng, Q, EB, F, LAYOUT, GD>::NT)
+// One batch of ne elements of order Q whose u (us) and G (gs, in LAYOUT) are
+// staged densely in shared memory (gs may also point to global memory).
+// Dp: D(i, n) in parameter space; eo, eot: the even-odd forms of D and D^T
+// (used when EO).  W0..W2: three padded work boxes of at least ne elements.
+// v is written at vb (global), the mass term read at mb (global, may be
+// NULL).  Ends with a block barrier (after which the stages may be reused).
+template <class Eng, int Q, int F, int LAYOUT, bool EO>
+__device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restrict__ Dp,
+                                                const EOMat<typename Eng::C, Q>& eo,
+                                                const EOMat<typename Eng::C, Q>& eot, const typename Eng::S* us,
+                                                const typename Eng::S* gs, typename Eng::V* W0, typename Eng::V* W1,
+                                                typename Eng::V* W2, int ne, int tid, int nt,
+                                                typename Eng::S* __restrict__ vb,
+                                                const typename Eng::S* __restrict__ mb, double lambda)
+{
+    using S = typename Eng::S;
+    using V = typename Eng::V;
+    using A = typename Eng::A;
+    using WB = WBox<Q, V>;
+    constexpr int Q3 = Q * Q * Q;
+    const Mat<typename Eng::C, Q, false> Dm{Dp};   // D(i, n)
+    const Mat<typename Eng::C, Q, true> Dt{Dp};    // D(n, i)
+    const S lam = S(lambda);
+    // 2. u -> W2 (working type, padded)
+    load_box<Eng, WB, Q, Q, Q>(us, Q3, W2, ne, tid, nt);
+    __syncthreads();
+    // 3. gradient: qr -> W0 (along i), qs -> W1 (along j); qt along k
+    //    in place into W2 after the other two have read it
+    if constexpr (EO) {
+        sweep_eo<Eng, WB, 0, Q>(W2, W0, ne, eo, tid, nt);
+        sweep_eo<Eng, WB, 1, Q>(W2, W1, ne, eo, tid, nt);
+        __syncthreads();
+        sweep_eo<Eng, WB, 2, Q>(W2, W2, ne, eo, tid, nt);
+    } else {
+        sweep<Eng, WB, 0, Q, Q, Q, Q>(W2, W0, ne, Dm, tid, nt);
+        sweep<Eng, WB, 1, Q, Q, Q, Q>(W2, W1, ne, Dm, tid, nt);
+        __syncthreads();
+        sweep<Eng, WB, 2, Q, Q, Q, Q>(W2, W2, ne, Dm, tid, nt);
+    }
+    __syncthreads();
+    // 4. fluxes with the symmetric (F = 6) or full (F = 9) factors
+    for (int w = tid; w < ne * Q3; w += nt) {
+        const int e = w / Q3;
+        const int x = w - e * Q3;
+        int i, j, k;
+        if (LAYOUT == 2) {   // walk points in G's (k, i, j) order
+            k = x / (Q * Q);
+            i = (x / Q) % Q;
+            j = x % Q;
+        } else {
+            i = x / (Q * Q);
+            j = (x / Q) % Q;
+            k = x % Q;
+        }
+        const int wi = e * WB::size + WB::at(i, j, k);
+        const V qr = W0[wi], qs = W1[wi], qt = W2[wi];
+        const S* ge = gs + e * F * Q3;
+        auto g = [&](int f) { return Eng::load(ge[g_index<Eng, Q, F, LAYOUT>(i, j, f, k)]); };
+        A r0 = Eng::zero(), r1 = Eng::zero(), r2 = Eng::zero();
+        if (F == 6) {
+            const V g0 = g(0), g1 = g(1), g2 = g(2), g3 = g(3), g4 = g(4), g5 = g(5);
+            Eng::vmadd(r0, g0, qr); Eng::vmadd(r0, g1, qs); Eng::vmadd(r0, g2, qt);
+            Eng::vmadd(r1, g1, qr); Eng::vmadd(r1, g3, qs); Eng::vmadd(r1, g4, qt);
+            Eng::vmadd(r2, g2, qr); Eng::vmadd(r2, g4, qs); Eng::vmadd(r2, g5, qt);
+        } else {
+            Eng::vmadd(r0, g(0), qr); Eng::vmadd(r0, g(1), qs); Eng::vmadd(r0, g(2), qt);
+            Eng::vmadd(r1, g(3), qr); Eng::vmadd(r1, g(4), qs); Eng::vmadd(r1, g(5), qt);
+            Eng::vmadd(r2, g(6), qr); Eng::vmadd(r2, g(7), qs); Eng::vmadd(r2, g(8), qt);
+        }
+        W0[wi] = Eng::result(r0);
+        W1[wi] = Eng::result(r1);
+        W2[wi] = Eng::result(r2);
+    }
+    __syncthreads();
+    // 5. transposed derivatives: along i in place on W0, along j on W1
+    if constexpr (EO) {
+        sweep_eo<Eng, WB, 0, Q>(W0, W0, ne, eot, tid, nt);
+        sweep_eo<Eng, WB, 1, Q>(W1, W1, ne, eot, tid, nt);
+        __syncthreads();
+        sweep_eo<Eng, WB, 2, Q>(W2, W2, ne, eot, tid, nt);
+    } else {
+        sweep<Eng, WB, 0, Q, Q, Q, Q>(W0, W0, ne, Dt, tid, nt);
+        sweep<Eng, WB, 1, Q, Q, Q, Q>(W1, W1, ne, Dt, tid, nt);
+    }
+    __syncthreads();
+    // 6. along k on W2 (already contracted when EO), plus the other two
+    //    terms, back into W2 (each line is read completely before it is
+    //    written; lines are disjoint)
+    {
+        constexpr int L = Q * Q;
+        for (int w = tid; w < ne * L; w += nt) {
+            const int e = w / L;
+            const int l = w - e * L;
+            const int i = l / Q;
+            const int j = l - i * Q;
+            const int base = e * WB::size + WB::at(i, j, 0);
+            V x[Q];
+#pragma unroll
+            for (int n = 0; n < Q; ++n) x[n] = W2[base + n];
+#pragma unroll
+            for (int o = 0; o < Q; ++o) {
+                A acc = Eng::zero();
+                if constexpr (EO) {
+                    Eng::add(acc, x[o]);
+                } else {
+#pragma unroll
+                    for (int n = 0; n < Q; ++n) Eng::madd(acc, Dt(o, n), x[n]);
+                }
+                V res;
+                if constexpr (HasSum3<Eng>::value) {
+                    res = Eng::sum3(Eng::result(acc), W0[base + o], W1[base + o]);
+                } else {
+                    Eng::add(acc, W0[base + o]);
+                    Eng::add(acc, W1[base + o]);
+                    res = Eng::result(acc);
+                }
+                W2[base + o] = res;
+            }
+        }
+    }
+    __syncthreads();
+    // 7. padded box -> v in global memory (coalesced), with the Helmholtz
+    //    mass term lambda * mass * u in the storage type's arithmetic
+    //    (double for the FP64 engines)
+    for (int w = tid; w < ne * Q3; w += nt) {
+        const int e = w / Q3;
+        const int x = w - e * Q3;
+        const int i = x / (Q * Q);
+        const int j = (x / Q) % Q;
+        const int k = x % Q;
+        S out = Eng::store(W2[e * WB::size + WB::at(i, j, k)]);
+        if (mb != nullptr) out += lam * mb[w] * us[w];
+        vb[w] = out;
+    }
+    __syncthreads();
+}
+
+template <class Eng, int Q, int EB, int F, int LAYOUT, bool EO = false, bool GD = false, int NBUF = 1>
+__global__ void __launch_bounds__(BK5Cfg<Eng, Q, EB, F, LAYOUT, GD, NBUF>::NT)
     bk5_kernel(const __grid_constant__ P5<typename Eng::C, Q> prm, const long long E,
                const typename Eng::S* __restrict__ u, const typename Eng::S* __restrict__ G,
                const typename Eng::S* __restrict__ mass, const double lambda, typename Eng::S* __restrict__ v,
                const DevCtx ctx)
 {
-    using Cfg = BK5Cfg<Eng, Q, EB, F, LAYOUT, GD>;
+    static_assert(NBUF == 1 || NBUF == 2, "one or two stage buffers");
+    using Cfg = BK5Cfg<Eng, Q, EB, F, LAYOUT, GD, NBUF>;
     using S = typename Eng::S;
     using V = typename Eng::V;
-    using A = typename Eng::A;
     using WB = typename Cfg::WB;
     constexpr int Q3 = Cfg::Q3;
     extern __shared__ __align__(16) unsigned char smem[];
-    unsigned char* ustage = smem;
-    unsigned char* gstage = ustage + Cfg::U_BYTES;
-    V* W0 = reinterpret_cast<V*>(gstage + Cfg::G_BYTES);
+    V* W0 = reinterpret_cast<V*>(smem + NBUF * Cfg::STAGE_BYTES);
     V* W1 = W0 + EB * WB::size;
     V* W2 = W1 + EB * WB::size;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(reinterpret_cast<unsigned char*>(W2 + EB * WB::size));
+    uint64_t* bars = reinterpret_cast<uint64_t*>(reinterpret_cast<unsigned char*>(W2 + EB * WB::size));
     const int tid = threadIdx.x;
     const int nt = Cfg::NT;
-    const Mat<typename Eng::C, Q, false> Dm{prm.D};   // D(i, n)
-    const Mat<typename Eng::C, Q, true> Dt{prm.D};    // D(n, i)
 
     if (tid == 0) {
-        mbar_init(bar, 1);
+        for (int b = 0; b < NBUF; ++b) mbar_init(&bars[b], 1);
         fence_mbar_init();
     }
     __syncthreads();
-    uint32_t phase = 0;
     const long long nbatch = (E + EB - 1) / EB;
-    for (long long bt = blockIdx.x; bt < nbatch; bt += gridDim.x, phase ^= 1u) {
+    // where the batch of each stage buffer landed
+    const S* us0 = nullptr;
+    const S* gs0 = nullptr;
+    const S* us1 = nullptr;
+    const S* gs1 = nullptr;
+    // 1. stage u and G of batch bt into buffer b
+    auto issue = [&](long long bt, int b) {
         const long long e0 = bt * EB;
         const int ne = int((E - e0) < EB ? (E - e0) : EB);
-        // 1. stage u and G of the batch
+        unsigned char* st = smem + b * Cfg::STAGE_BYTES;
         uint32_t tx = 0;
         if (tid == 0) fence_proxy_async();
-        const S* us = stage_issue<S>(ustage, u + e0 * Q3, ne * Q3, bar, tx, tid, nt);
-        const S* gs = GD ? G + e0 * F * Q3 : stage_issue<S>(gstage, G + e0 * F * Q3, ne * F * Q3, bar, tx, tid, nt);
-        if (tid == 0) mbar_arrive_expect_tx(bar, tx);
-        if (batch_wait_failed(bar, phase, ctx, tid)) return;
-        // 2. u -> W2 (working type, padded)
-        load_box<Eng, WB, Q, Q, Q>(us, Q3, W2, ne, tid, nt);
-        __syncthreads();
-        // 3. gradient: qr -> W0 (along i), qs -> W1 (along j); qt along k
-        //    in place into W2 after the other two have read it
-        if constexpr (EO) {
-            sweep_eo<Eng, WB, 0, Q>(W2, W0, ne, prm.eo, tid, nt);
-            sweep_eo<Eng, WB, 1, Q>(W2, W1, ne, prm.eo, tid, nt);
-            __syncthreads();
-            sweep_eo<Eng, WB, 2, Q>(W2, W2, ne, prm.eo, tid, nt);
+        const S* us = stage_issue<S>(st, u + e0 * Q3, ne * Q3, &bars[b], tx, tid, nt);
+        const S* gs = GD ? G + e0 * F * Q3
+                         : stage_issue<S>(st + Cfg::U_BYTES, G + e0 * F * Q3, ne * F * Q3, &bars[b], tx, tid, nt);
+        if (tid == 0) mbar_arrive_expect_tx(&bars[b], tx);
+        if (b == 0) {
+            us0 = us;
+            gs0 = gs;
         } else {
-            sweep<Eng, WB, 0, Q, Q, Q, Q>(W2, W0, ne, Dm, tid, nt);
-            sweep<Eng, WB, 1, Q, Q, Q, Q>(W2, W1, ne, Dm, tid, nt);
-            __syncthreads();
-            sweep<Eng, WB, 2, Q, Q, Q, Q>(W2, W2, ne, Dm, tid, nt);
+            us1 = us;
+            gs1 = gs;
         }
-        __syncthreads();
-        // 4. fluxes with the symmetric (F = 6) or full (F = 9) factors
-        for (int w = tid; w < ne * Q3; w += nt) {
-            const int e = w / Q3;
-            const int x = w - e * Q3;
-            int i, j, k;
-            if (LAYOUT == 2) {   // walk points in G's (k, i, j) order
-                k = x / (Q * Q);
-                i = (x / Q) % Q;
-                j = x % Q;
-            } else {
-                i = x / (Q * Q);
-                j = (x / Q) % Q;
-                k = x % Q;
-            }
-            const int wi = e * WB::size + WB::at(i, j, k);
-            const V qr = W0[wi], qs = W1[wi], qt = W2[wi];
-            const S* ge = gs + e * F * Q3;
-            auto g = [&](int f) { return Eng::load(ge[g_index<Eng, Q, F, LAYOUT>(i, j, f, k)]); };
-            A r0 = Eng::zero(), r1 = Eng::zero(), r2 = Eng::zero();
-            if (F == 6) {
-                const V g0 = g(0), g1 = g(1), g2 = g(2), g3 = g(3), g4 = g(4), g5 = g(5);
-                Eng::vmadd(r0, g0, qr); Eng::vmadd(r0, g1, qs); Eng::vmadd(r0, g2, qt);
-                Eng::vmadd(r1, g1, qr); Eng::vmadd(r1, g3, qs); Eng::vmadd(r1, g4, qt);
-                Eng::vmadd(r2, g2, qr); Eng::vmadd(r2, g4, qs); Eng::vmadd(r2, g5, qt);
-            } else {
-                Eng::vmadd(r0, g(0), qr); Eng::vmadd(r0, g(1), qs); Eng::vmadd(r0, g(2), qt);
-                Eng::vmadd(r1, g(3), qr); Eng::vmadd(r1, g(4), qs); Eng::vmadd(r1, g(5), qt);
-                Eng::vmadd(r2, g(6), qr); Eng::vmadd(r2, g(7), qs); Eng::vmadd(r2, g(8), qt);
-            }
-            W0[wi] = Eng::result(r0);
-            W1[wi] = Eng::result(r1);
-            W2[wi] = Eng::result(r2);
+    };
+    if (NBUF == 2 && blockIdx.x < nbatch) issue(blockIdx.x, 0);
+    unsigned it = 0;
+    for (long long bt = blockIdx.x; bt < nbatch; bt += gridDim.x, ++it) {
+        const int b = (NBUF == 2) ? int(it & 1u) : 0;
+        const uint32_t parity = (NBUF == 2) ? ((it >> 1) & 1u) : (it & 1u);
+        bool next = false;
+        if (NBUF == 1) {
+            issue(bt, 0);
+        } else if (bt + gridDim.x < nbatch) {
+            // the other buffer was released by the previous batch's final barrier
+            issue(bt + gridDim.x, b ^ 1);
+            next = true;
         }
-        __syncthreads();
-        // 5. transposed derivatives: along i in place on W0, along j on W1
-        if constexpr (EO) {
-            sweep_eo<Eng, WB, 0, Q>(W0, W0, ne, prm.eot, tid, nt);
-            sweep_eo<Eng, WB, 1, Q>(W1, W1, ne, prm.eot, tid, nt);
-            __syncthreads();
-            sweep_eo<Eng, WB, 2, Q>(W2, W2, ne, prm.eot, tid, nt);
-        } else {
-            sweep<Eng, WB, 0, Q, Q, Q, Q>(W0, W0, ne, Dt, tid, nt);
-            sweep<Eng, WB, 1, Q, Q, Q, Q>(W1, W1, ne, Dt, tid, nt);
+        if (batch_wait_failed(&bars[b], parity, ctx, tid)) {
+            // a copy into the other buffer may still be in flight: let it land
+            if (next) mbar_wait_bounded(&bars[b ^ 1], ((it + 1) >> 1) & 1u, ctx.wait_limit);
+            return;
         }
-        __syncthreads();
-        // 6. along k on W2 (already contracted when EO), plus the other two
-        //    terms (and the Helmholtz mass term), written densely into the u
-        //    staging area
-        S* vs = const_cast<S*>(us);
-        {
-            constexpr int L = Q * Q;
-            for (int w = tid; w < ne * L; w += nt) {
-                const int e = w / L;
-                const int l = w - e * L;
-                const int i = l / Q;
-                const int j = l - i * Q;
-                const int base = e * WB::size + WB::at(i, j, 0);
-                V x[Q];
-#pragma unroll
-                for (int n = 0; n < Q; ++n) x[n] = W2[base + n];
-#pragma unroll
-                for (int o = 0; o < Q; ++o) {
-                    A acc = Eng::zero();
-                    if constexpr (EO) {
-                        Eng::add(acc, x[o]);
-                    } else {
-#pragma unroll
-                        for (int n = 0; n < Q; ++n) Eng::madd(acc, Dt(o, n), x[n]);
-                    }
-                    V res;
-                    if constexpr (HasSum3<Eng>::value) {
-                        res = Eng::sum3(Eng::result(acc), W0[base + o], W1[base + o]);
-                    } else {
-                        Eng::add(acc, W0[base + o]);
-                        Eng::add(acc, W1[base + o]);
-                        res = Eng::result(acc);
-                    }
-                    const int xo = e * Q3 + (i * Q + j) * Q + o;
-                    S out = Eng::store(res);
-                    if (mass != nullptr) {
-                        // lambda * mass * u at the point, in the storage type's
-                        // arithmetic (double for the FP64 engines)
-                        out += S(lambda) * mass[(e0 + e) * Q3 + (i * Q + j) * Q + o] * us[xo];
-                    }
-                    vs[xo] = out;
-                }
-            }
-        }
-        __syncthreads();
-        store_out<S>(vs, v + e0 * Q3, ne * Q3, tid, nt);
-        __syncthreads();
+        const long long e0 = bt * EB;
+        const int ne = int((E - e0) < EB ? (E - e0) : EB);
+        bk5_sweep_batch<Eng, Q, F, LAYOUT, EO>(prm.D, prm.eo, prm.eot, b == 0 ? us0 : us1, b == 0 ? gs0 : gs1, W0, W1,
+                                               W2, ne, tid, nt, v + e0 * Q3,
+                                               (mass != nullptr) ? mass + e0 * Q3 : nullptr, lambda);
     }
 }
 
@@ -567,10 +745,8 @@ __global__ void __launch_bounds__(BK1Cfg<Eng, Q, EB>::NT)
         __syncthreads();
         sweep<Eng, WB, 0, Q, P, P, P>(W1, W0, ne, Bb, tid, nt);   // (P,P,P)
         __syncthreads();
-        S* vs = const_cast<S*>(us);
-        store_box<Eng, WB, P, P, P>(W0, vs, P3, ne, tid, nt);
-        __syncthreads();
-        store_out<S>(vs, v + e0 * P3, ne * P3, tid, nt);
+        // padded box -> v (consecutive threads, consecutive values)
+        store_box<Eng, WB, P, P, P>(W0, v + e0 * P3, P3, ne, tid, nt);
         __syncthreads();
     }
 }
@@ -593,7 +769,7 @@ struct BK3Cfg {
     static constexpr int SMEM = U_BYTES + G_BYTES + K_BYTES + W_BYTES + 16;
 };
 
-template <class Eng, int Q, int EB>
+template <class Eng, int Q, int EB, bool EO = false>
 __global__ void __launch_bounds__(BK3Cfg<Eng, Q, EB>::NT)
     bk3_kernel(const __grid_constant__ P13<typename Eng::C, Q> prm, const long long E,
                const typename Eng::S* __restrict__ u, const typename Eng::S* __restrict__ G,
@@ -640,15 +816,27 @@ __global__ void __launch_bounds__(BK3Cfg<Eng, Q, EB>::NT)
         if (batch_wait_failed(bar, phase, ctx, tid)) return;
         load_box<Eng, WB, P, P, P>(us, P3, W0, ne, tid, nt);
         __syncthreads();
-        sweep<Eng, WB, 0, P, P, P, Q>(W0, W1, ne, Bi, tid, nt);   // (Q,P,P)
-        __syncthreads();
-        sweep<Eng, WB, 1, Q, P, P, Q>(W1, W0, ne, Bi, tid, nt);   // (Q,Q,P)
-        __syncthreads();
-        sweep<Eng, WB, 2, Q, Q, P, Q>(W0, W2, ne, Bi, tid, nt);   // u at the points: W2
-        __syncthreads();
-        sweep<Eng, WB, 0, Q, Q, Q, Q>(W2, W0, ne, Dg, tid, nt);   // qr
-        sweep<Eng, WB, 1, Q, Q, Q, Q>(W2, W1, ne, Dg, tid, nt);   // qs
-        sweep<Eng, WB, 2, Q, Q, Q, Q>(W2, W3, ne, Dg, tid, nt);   // qt
+        if constexpr (EO) {
+            sweep_eor<Eng, WB, 0, P, P, P, Q, +1>(W0, W1, ne, prm.bi, tid, nt);   // (Q,P,P)
+            __syncthreads();
+            sweep_eor<Eng, WB, 1, Q, P, P, Q, +1>(W1, W0, ne, prm.bi, tid, nt);   // (Q,Q,P)
+            __syncthreads();
+            sweep_eor<Eng, WB, 2, Q, Q, P, Q, +1>(W0, W2, ne, prm.bi, tid, nt);   // u at the points: W2
+            __syncthreads();
+            sweep_eor<Eng, WB, 0, Q, Q, Q, Q, -1>(W2, W0, ne, prm.dg, tid, nt);   // qr
+            sweep_eor<Eng, WB, 1, Q, Q, Q, Q, -1>(W2, W1, ne, prm.dg, tid, nt);   // qs
+            sweep_eor<Eng, WB, 2, Q, Q, Q, Q, -1>(W2, W3, ne, prm.dg, tid, nt);   // qt
+        } else {
+            sweep<Eng, WB, 0, P, P, P, Q>(W0, W1, ne, Bi, tid, nt);   // (Q,P,P)
+            __syncthreads();
+            sweep<Eng, WB, 1, Q, P, P, Q>(W1, W0, ne, Bi, tid, nt);   // (Q,Q,P)
+            __syncthreads();
+            sweep<Eng, WB, 2, Q, Q, P, Q>(W0, W2, ne, Bi, tid, nt);   // u at the points: W2
+            __syncthreads();
+            sweep<Eng, WB, 0, Q, Q, Q, Q>(W2, W0, ne, Dg, tid, nt);   // qr
+            sweep<Eng, WB, 1, Q, Q, Q, Q>(W2, W1, ne, Dg, tid, nt);   // qs
+            sweep<Eng, WB, 2, Q, Q, Q, Q>(W2, W3, ne, Dg, tid, nt);   // qt
+        }
         __syncthreads();
         for (int w = tid; w < ne * Q3; w += nt) {
             const int e = w / Q3;
@@ -674,10 +862,17 @@ __global__ void __launch_bounds__(BK3Cfg<Eng, Q, EB>::NT)
             W3[wi] = Eng::result(r2);
         }
         __syncthreads();
-        sweep<Eng, WB, 0, Q, Q, Q, Q>(W0, W0, ne, Dtr, tid, nt);
-        sweep<Eng, WB, 1, Q, Q, Q, Q>(W1, W1, ne, Dtr, tid, nt);
+        if constexpr (EO) {
+            sweep_eor<Eng, WB, 0, Q, Q, Q, Q, -1>(W0, W0, ne, prm.dtr, tid, nt);
+            sweep_eor<Eng, WB, 1, Q, Q, Q, Q, -1>(W1, W1, ne, prm.dtr, tid, nt);
+            sweep_eor<Eng, WB, 2, Q, Q, Q, Q, -1>(W3, W3, ne, prm.dtr, tid, nt);
+        } else {
+            sweep<Eng, WB, 0, Q, Q, Q, Q>(W0, W0, ne, Dtr, tid, nt);
+            sweep<Eng, WB, 1, Q, Q, Q, Q>(W1, W1, ne, Dtr, tid, nt);
+        }
         __syncthreads();
-        // along r on W3, plus the two other terms -> W2
+        // along r on W3 (already contracted when EO), plus the two other
+        // terms -> W2
         {
             constexpr int L = Q * Q;
             for (int w = tid; w < ne * L; w += nt) {
@@ -692,8 +887,12 @@ __global__ void __launch_bounds__(BK3Cfg<Eng, Q, EB>::NT)
 #pragma unroll
                 for (int o = 0; o < Q; ++o) {
                     A acc = Eng::zero();
+                    if constexpr (EO) {
+                        Eng::add(acc, x[o]);
+                    } else {
 #pragma unroll
-                    for (int n = 0; n < Q; ++n) Eng::madd(acc, Dtr(o, n), x[n]);
+                        for (int n = 0; n < Q; ++n) Eng::madd(acc, Dtr(o, n), x[n]);
+                    }
                     if constexpr (HasSum3<Eng>::value) {
                         W2[base + o] = Eng::sum3(Eng::result(acc), W0[base + o], W1[base + o]);
                     } else {
@@ -705,16 +904,22 @@ __global__ void __launch_bounds__(BK3Cfg<Eng, Q, EB>::NT)
             }
         }
         __syncthreads();
-        sweep<Eng, WB, 2, Q, Q, Q, P>(W2, W0, ne, Bb, tid, nt);   // (Q,Q,P)
+        if constexpr (EO) {
+            sweep_eor<Eng, WB, 2, Q, Q, Q, P, +1>(W2, W0, ne, prm.bb, tid, nt);   // (Q,Q,P)
+            __syncthreads();
+            sweep_eor<Eng, WB, 1, Q, Q, P, P, +1>(W0, W1, ne, prm.bb, tid, nt);   // (Q,P,P)
+            __syncthreads();
+            sweep_eor<Eng, WB, 0, Q, P, P, P, +1>(W1, W0, ne, prm.bb, tid, nt);   // (P,P,P)
+        } else {
+            sweep<Eng, WB, 2, Q, Q, Q, P>(W2, W0, ne, Bb, tid, nt);   // (Q,Q,P)
+            __syncthreads();
+            sweep<Eng, WB, 1, Q, Q, P, P>(W0, W1, ne, Bb, tid, nt);   // (Q,P,P)
+            __syncthreads();
+            sweep<Eng, WB, 0, Q, P, P, P>(W1, W0, ne, Bb, tid, nt);   // (P,P,P)
+        }
         __syncthreads();
-        sweep<Eng, WB, 1, Q, Q, P, P>(W0, W1, ne, Bb, tid, nt);   // (Q,P,P)
-        __syncthreads();
-        sweep<Eng, WB, 0, Q, P, P, P>(W1, W0, ne, Bb, tid, nt);   // (P,P,P)
-        __syncthreads();
-        S* vs = const_cast<S*>(us);
-        store_box<Eng, WB, P, P, P>(W0, vs, P3, ne, tid, nt);
-        __syncthreads();
-        store_out<S>(vs, v + e0 * P3, ne * P3, tid, nt);
+        // padded box -> v (consecutive threads, consecutive values)
+        store_box<Eng, WB, P, P, P>(W0, v + e0 * P3, P3, ne, tid, nt);
         __syncthreads();
     }
 }

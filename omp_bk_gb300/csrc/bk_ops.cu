@@ -55,9 +55,36 @@ namespace BK_TU_NS {
 // Elements per block: about 128 lines per sweep (Q^2 lines per element).
 constexpr int default_eb(int q) { return (q * q >= 100) ? 1 : ((q * q >= 64) ? 2 : (128 + q * q - 1) / (q * q)); }
 
+// Elements per block of the BK5 and BK3 sweep kernels (even-odd path), the
+// fastest of EB = 1..16 measured per engine and q on GB300 (about 2^24 DoFs
+// per apply).  Small orders want many elements per block (short lines, small
+// boxes); from q = 8 one element per block, whose smaller shared-memory
+// footprint keeps more blocks resident, wins for the FP32-pipe engines.
+constexpr bool eng_is_dfma() { return Eng::kId == BK_ENGINE_DFMA; }
+constexpr bool eng_is_ff() { return Eng::kId == BK_ENGINE_FF; }
+constexpr int sweep_eb5(int q)
+{
+    if (q <= 3) return eng_is_ff() || eng_is_dfma() ? 16 : 12;
+    if (q == 4) return 8;
+    if (eng_is_dfma()) return q == 5 ? 6 : q == 6 ? 4 : q == 7 ? 3 : q == 8 ? 2 : 3;
+    if (eng_is_ff()) return q == 5 ? 4 : q == 6 ? 3 : q == 7 ? 4 : 1;
+    return q == 5 ? 4 : q == 6 ? 3 : q == 7 ? 2 : 1;
+}
+constexpr int sweep_eb3(int q)
+{
+    if (q <= 3) return eng_is_ff() ? 12 : 16;
+    if (q == 4) return 8;
+    if (eng_is_dfma()) return q == 5 ? 6 : q == 6 ? 4 : q == 7 ? 3 : q == 8 ? 2 : q == 9 ? 3 : 1;
+    if (eng_is_ff()) return q == 5 ? 8 : q <= 7 ? 3 : 1;
+    return q == 5 ? 6 : q == 6 ? 4 : q == 7 ? 3 : 1;
+}
+
 // Sets the dynamic shared-memory size of a kernel on the current device once
 // and returns its resident blocks per SM (0 if it cannot run).  Tag makes the
 // cache one per kernel instantiation (kernels of one signature share K).
+template <class Cfg, bool EO>
+struct EoTag {};
+
 template <class Tag, class K>
 int prepare(K kern, int smem, int nt)
 {
@@ -84,7 +111,11 @@ template <int Q, int EB, int F, int LAYOUT, bool GD>
 int bk5_q(const double* D, long long E, const void* u, const void* G, const void* mass, double lambda, void* v,
           cudaStream_t s)
 {
-    using Cfg = BK5Cfg<Eng, Q, EB, F, LAYOUT, GD>;
+    // one stage buffer: double buffering (NB = 2) measured no faster than
+    // the overlap of the blocks resident on an SM, which one buffer keeps
+    // more of
+    constexpr int NB = 1;
+    using Cfg = BK5Cfg<Eng, Q, EB, F, LAYOUT, GD, NB>;
     using S = typename Eng::S;
     static_assert(Cfg::SMEM <= 232448, "BK5 block exceeds the shared memory of an SM");
     P5<typename Eng::C, Q> prm;
@@ -93,8 +124,8 @@ int bk5_q(const double* D, long long E, const void* u, const void* G, const void
     // instantiated for the symmetric 6-factor G only
     const bool eo = (F == 6) && make_eo<typename Eng::C, Q>(D, false, prm.eo, &Eng::coef) &&
                     make_eo<typename Eng::C, Q>(D, true, prm.eot, &Eng::coef);
-    auto kern = eo ? bk5_kernel<Eng, Q, EB, F, LAYOUT, (F == 6), GD> : bk5_kernel<Eng, Q, EB, F, LAYOUT, false, GD>;
-    const int occ = eo ? prepare<BK5Cfg<Eng, Q, EB, F, LAYOUT + 8, GD>>(kern, Cfg::SMEM, Cfg::NT)
+    auto kern = eo ? bk5_kernel<Eng, Q, EB, F, LAYOUT, (F == 6), GD, NB> : bk5_kernel<Eng, Q, EB, F, LAYOUT, false, GD, NB>;
+    const int occ = eo ? prepare<EoTag<Cfg, true>>(kern, Cfg::SMEM, Cfg::NT)
                        : prepare<Cfg>(kern, Cfg::SMEM, Cfg::NT);
     if (occ <= 0) return BK_ERR_CUDA;
     const int grid = grid_for((E + EB - 1) / EB, occ);
@@ -103,15 +134,24 @@ int bk5_q(const double* D, long long E, const void* u, const void* G, const void
     return cudaGetLastError() == cudaSuccess ? BK_OK : BK_ERR_CUDA;
 }
 
+// the largest EB <= EB0 whose block fits an SM's shared memory
+template <int Q, int F, int EB0>
+constexpr int fit_eb5()
+{
+    if constexpr (EB0 > 1 && BK5Cfg<Eng, Q, EB0, F, BK_LAYOUT_TU>::SMEM > 232448)
+        return fit_eb5<Q, F, EB0 - 1>();
+    else
+        return EB0;
+}
+
 template <int Q>
 int bk5_sweep_q(int F, int gd, const double* D, long long E, const void* u, const void* G, const void* mass,
                 double lambda, void* v, cudaStream_t s)
 {
-    constexpr int EB = default_eb(Q);
     constexpr int L = BK_LAYOUT_TU;
     (void)gd;
-    if (F == 6) return bk5_q<Q, EB, 6, L, false>(D, E, u, G, mass, lambda, v, s);
-    if (F == 9) return bk5_q<Q, EB, 9, L, false>(D, E, u, G, mass, lambda, v, s);
+    if (F == 6) return bk5_q<Q, fit_eb5<Q, 6, sweep_eb5(Q)>(), 6, L, false>(D, E, u, G, mass, lambda, v, s);
+    if (F == 9) return bk5_q<Q, fit_eb5<Q, 9, sweep_eb5(Q)>(), 9, L, false>(D, E, u, G, mass, lambda, v, s);
     return BK_ERR_PREC;
 }
 #endif  // BK_OP_TU == 5
@@ -186,8 +226,11 @@ int bk3_q(const double* B, const double* D, long long E, const void* G, const vo
     P13<typename Eng::C, Q> prm;
     for (int i = 0; i < (Q - 1) * Q; ++i) prm.B[i] = Eng::coef(B[i]);
     for (int i = 0; i < Q * Q; ++i) prm.D[i] = Eng::coef(D[i]);
-    auto kern = bk3_kernel<Eng, Q, EB>;
-    const int occ = prepare<Cfg>(kern, Cfg::SMEM, Cfg::NT);
+    // the even-odd contractions when B is centro-symmetric and D
+    // centro-antisymmetric (GLL nodes, Gauss points)
+    const bool eo = make_p13_eo<typename Eng::C, Q>(prm, B, D, &Eng::coef);
+    auto kern = eo ? bk3_kernel<Eng, Q, EB, true> : bk3_kernel<Eng, Q, EB, false>;
+    const int occ = eo ? prepare<EoTag<Cfg, true>>(kern, Cfg::SMEM, Cfg::NT) : prepare<Cfg>(kern, Cfg::SMEM, Cfg::NT);
     if (occ <= 0) return BK_ERR_CUDA;
     const int grid = grid_for((E + EB - 1) / EB, occ);
     kern<<<grid, Cfg::NT, Cfg::SMEM, s>>>(prm, E, static_cast<const S*>(u), static_cast<const S*>(G),
@@ -290,14 +333,14 @@ int BK_CAT(launch_bk3, BK_SFX)(int p, long long E, const double* B, const double
 {
     (void)eb;
     switch (p + 2) {
-        case 3: return bk3_q<3, default_eb(3)>(B, D, E, G, k, u, v, s);
-        case 4: return bk3_q<4, default_eb(4)>(B, D, E, G, k, u, v, s);
-        case 5: return bk3_q<5, default_eb(5)>(B, D, E, G, k, u, v, s);
-        case 6: return bk3_q<6, default_eb(6)>(B, D, E, G, k, u, v, s);
-        case 7: return bk3_q<7, default_eb(7)>(B, D, E, G, k, u, v, s);
-        case 8: return bk3_q<8, default_eb(8)>(B, D, E, G, k, u, v, s);
-        case 9: return bk3_q<9, default_eb(9)>(B, D, E, G, k, u, v, s);
-        case 10: return bk3_q<10, default_eb(10)>(B, D, E, G, k, u, v, s);
+        case 3: return bk3_q<3, sweep_eb3(3)>(B, D, E, G, k, u, v, s);
+        case 4: return bk3_q<4, sweep_eb3(4)>(B, D, E, G, k, u, v, s);
+        case 5: return bk3_q<5, sweep_eb3(5)>(B, D, E, G, k, u, v, s);
+        case 6: return bk3_q<6, sweep_eb3(6)>(B, D, E, G, k, u, v, s);
+        case 7: return bk3_q<7, sweep_eb3(7)>(B, D, E, G, k, u, v, s);
+        case 8: return bk3_q<8, sweep_eb3(8)>(B, D, E, G, k, u, v, s);
+        case 9: return bk3_q<9, sweep_eb3(9)>(B, D, E, G, k, u, v, s);
+        case 10: return bk3_q<10, sweep_eb3(10)>(B, D, E, G, k, u, v, s);
         default: return BK_ERR_ORDER;
     }
 }

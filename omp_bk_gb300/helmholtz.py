@@ -45,15 +45,18 @@ def _declare():
                                  C.c_int, C.c_void_p]
     L.bk_hplan_cg.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_void_p,
                               C.c_void_p, C.POINTER(CGOptions), C.POINTER(CGStats), C.c_void_p]
-    for f in ("bk_hplan_create", "bk_hplan_destroy", "bk_hplan_apply", "bk_hplan_cg"):
+    L.bk_hplan_set_kernel.argtypes = [C.c_void_p, C.c_int]
+    for f in ("bk_hplan_create", "bk_hplan_destroy", "bk_hplan_apply", "bk_hplan_cg", "bk_hplan_set_kernel"):
         getattr(L, f).restype = C.c_int
     L._hplan_declared = True
     return L
 
 
 def default_tiles(p: int) -> int:
-    """Elements per tile when no tuning is given: 256 threads / (p+1)^2."""
-    return max(1, 256 // (p + 1) ** 2)
+    """Elements per tile when no tuning is given (the library's own default):
+    about 128 lines of (p+1) points, at least one element."""
+    q2 = (p + 1) ** 2
+    return 1 if q2 >= 100 else (2 if q2 >= 64 else (128 + q2 - 1) // q2)
 
 
 class HelmholtzPlan:
@@ -81,6 +84,15 @@ class HelmholtzPlan:
             self.goff.append(go)
             uo += E * (p + 1) ** 3
             go += 6 * E * (p + 1) ** 3
+
+    @property
+    def kernel(self) -> int:
+        """The body of the persistent launch: KERNEL_SWEEP (even-odd line
+        sweeps) or KERNEL_COLUMN."""
+        return int(_declare().bk_hplan_size(self.h, 3))
+
+    def set_kernel(self, kernel: int):
+        check(_declare().bk_hplan_set_kernel(self.h, int(kernel)), "bk_hplan_set_kernel")
 
     def close(self):
         if self.h:

@@ -39,10 +39,14 @@ def small_plan(bklib):
     plan.close()
 
 
+@pytest.mark.parametrize("kernel", ["sweep", "column"])
 @pytest.mark.parametrize("prec", ["ff", "dfma", "mixed", "fp32"])
-def test_multi_apply_matches_per_order(bklib, small_plan, prec):
+def test_multi_apply_matches_per_order(bklib, small_plan, prec, kernel):
     bk = bklib
     plan, G, M, u = small_plan
+    assert plan.kernel == bk.KERNEL_SWEEP   # GLL derivatives: even-odd body by default
+    plan.set_kernel(bk.KERNEL_SWEEP if kernel == "sweep" else bk.KERNEL_COLUMN)
+    assert plan.kernel == (bk.KERNEL_SWEEP if kernel == "sweep" else bk.KERNEL_COLUMN)
     lam = 1.0 if prec != "dfma" else 0.75
     if prec in ("ff", "dfma"):
         pr, eng, dt, tol = bk.PREC_FP64, (bk.ENGINE_FF if prec == "ff" else bk.ENGINE_DFMA), torch.float64, 1e-12
@@ -67,6 +71,29 @@ def test_multi_apply_matches_per_order(bklib, small_plan, prec):
         ref = oracle.bk5(q, plan.E[k], D, _col_to_interleaved(f(Gd[sg]), plan.E[k], q), f(ud[su]),
                          mass=f(Md[su]), lam=lam)
         assert oracle.rel_maxdiff(host(v[su]), ref) < tol, p
+    plan.set_kernel(bk.KERNEL_AUTO)
+
+
+def test_sweep_needs_centro_antisymmetric_D(bklib):
+    """A D that is not centro-antisymmetric keeps the column body."""
+    import ctypes as C
+    from omp_bk_gb300.helmholtz import HelmholtzPlan, OrderRange, _declare
+    plan = HelmholtzPlan([(3, 4)])
+    assert plan.kernel == bklib.KERNEL_SWEEP
+    plan.close()
+    L = _declare()
+    D = np.arange(16, dtype=np.float64) / 7.0
+    rng = (OrderRange * 1)(OrderRange(3, 4, 0))
+    dp = (C.POINTER(C.c_double) * 1)(D.ctypes.data_as(C.POINTER(C.c_double)))
+    h = C.c_void_p()
+    assert L.bk_hplan_create(C.byref(h), 1, rng, dp, None) == bklib.BK_OK
+    try:
+        assert L.bk_hplan_size(h, 3) == bklib.KERNEL_COLUMN
+        assert L.bk_hplan_set_kernel(h, bklib.KERNEL_SWEEP) == bklib.BK_ERR_ARG
+        assert L.bk_hplan_set_kernel(h, bklib.KERNEL_AUTO) == bklib.BK_OK
+        assert L.bk_hplan_size(h, 3) == bklib.KERNEL_COLUMN
+    finally:
+        L.bk_hplan_destroy(h)
 
 
 def test_cg_converges(bklib, small_plan):

@@ -239,3 +239,32 @@ def test_bk5_gll_even_odd(bklib, p, engine):
         ref = oracle.bk5(nq, E, D, f(g), f(u))
         tol = TOL32
     assert oracle.rel_maxdiff(out, ref) < tol
+
+
+@pytest.mark.parametrize("p", P_ALL)
+@pytest.mark.parametrize("engine", ["dfma", "ff", "fp32", "mixed"])
+@pytest.mark.parametrize("coef", [False, True])
+def test_bk3_gll_gauss_even_odd(bklib, p, engine, coef):
+    """With GLL nodes and Gauss points (B centro-symmetric, D
+    centro-antisymmetric) BK3 takes the even-odd contractions, rectangular
+    for the interpolation; same operator as the oracle's plain sums."""
+    E = 9
+    B, D, _, _, _ = bklib.bk1_bk3_matrices(p)
+    nq = p + 2
+    rng = np.random.default_rng(200 + p)
+    u = rng.uniform(-1, 1, E * (nq - 1) ** 3)
+    g = rng.uniform(0.5, 1.5, E * 6 * nq ** 3)
+    k = np.exp(rng.normal(0, 0.5, E * nq ** 3)) if coef else None
+    if engine in ("dfma", "ff"):
+        eng = bklib.ENGINE_DFMA if engine == "dfma" else bklib.ENGINE_FF
+        out = gpu_apply(bklib, 3, p, E, B, D, g, u, bklib.PREC_FP64, engine=eng, k=k)
+        ref = oracle.bk3(nq, E, B, D, g, u, k=k)
+        tol = TOL64
+    else:
+        pr = bklib.PREC_FP32 if engine == "fp32" else bklib.PREC_MIXED
+        out = gpu_apply(bklib, 3, p, E, B, D, g, u, pr, k=k)
+        f = lambda a: None if a is None else a.astype(np.float32).astype(np.float64)
+        ref = oracle.bk3(nq, E, B, D, f(g), f(u), k=f(k))
+        tol = TOL32
+    assert np.all(np.isfinite(out))
+    assert oracle.rel_maxdiff(out, ref) < tol
