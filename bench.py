@@ -59,7 +59,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--elements", type=int, default=E_FULL, help="override E (profiling a smaller case)")
+    ap.add_argument("--elements", type=int, default=None,
+                    help="override E (profiling a smaller case); helmholtz: E_p = 2^(8-p) * elements / 64")
     ap.add_argument("--engine", default="ff", choices=["ff", "dfma"])
     ap.add_argument("--prec", default="fp64", choices=["fp64", "mixed", "fp32"],
                     help="form timed in the main loop (profiling; the headline is fp64)")
@@ -288,7 +289,7 @@ def run_bk1(args):
     import torch
 
     import omp_bk_gb300 as bk
-    p, E = 3, 4096
+    p, E = 3, args.elements or 4096
     P, Q = p + 1, p + 2
     B, _, xq, wq, _ = bk.bk1_bk3_matrices(p)
     qd = torch.empty(E * Q ** 3, dtype=torch.float64, device="cuda")
@@ -327,7 +328,7 @@ def run_bk3(args):
     import torch
 
     import omp_bk_gb300 as bk
-    p, E = 6, 131072
+    p, E = 6, args.elements or 131072
     P, Q = p + 1, p + 2
     B, D, xq, wq, xn = bk.bk1_bk3_matrices(p)
     G = torch.empty(E * 6 * Q ** 3, dtype=torch.float64, device="cuda")
@@ -379,7 +380,7 @@ def run_adjoint(args):
     import torch
 
     import omp_bk_gb300 as bk
-    p, E = 4, 65536
+    p, E = 4, args.elements or 65536
     P, Q = p + 1, p + 2
     B, D, xq, wq, _ = bk.bk1_bk3_matrices(p)
     G = torch.empty(E * 6 * Q ** 3, dtype=torch.float64, device="cuda")
@@ -439,6 +440,8 @@ def run_helmholtz(args):
     from omp_bk_gb300 import helmholtz as hz
     from omp_bk_gb300 import tune
     orders = hz.config_orders()
+    if args.elements:
+        orders = [(p, max(1, (2 ** (8 - p)) * args.elements // 64)) for p, _ in orders]
     best = tune.tune(orders)
     plan = hz.HelmholtzPlan([(p, E, best[p]) for p, E in orders])
     G, M = plan.geometry(seed=11)
@@ -480,7 +483,7 @@ def run_helmholtz(args):
     torch.cuda.synchronize()
     solve_s = time.perf_counter() - t
     err = float(torch.linalg.norm(x - ustar) / torch.linalg.norm(ustar))
-    _line(args, f"mixed-order Helmholtz p=2..8, E_p=2^(8-p)*4096 ({plan.n} DoFs), one persistent launch",
+    _line(args, f"mixed-order Helmholtz p=2..8, E_p=2^(8-p)*{orders[-1][1]} ({plan.n} DoFs), one persistent launch",
           plan.n / m_multi / 1e6, m_multi, "f32",
           {"helmholtz": {"dofs": plan.n, "tiles": plan.ntiles, "tile_elems": best,
                          "kernel": {bk.KERNEL_SWEEP: "sweep (even-odd)", bk.KERNEL_COLUMN: "column"}[plan.kernel],
@@ -504,7 +507,7 @@ def main():
     rank, world, local = dist_setup(args.gpus)
     torch.cuda.set_device(local)
     stream = torch.cuda.current_stream()
-    E = args.elements
+    E = args.elements or E_FULL
     Q = P_ORDER + 1
     dofs = E * Q ** 3
     D, u, G = make_inputs(bk, E, torch, args.layout)
@@ -545,21 +548,28 @@ def main():
                                 f"bytes = 8 B x (u + v + 6 G) per DoF"},
            "clocks": clk.summary()}
 
-    # end to end through the C ABI: pinned host u -> device, apply, v -> pinned host
+    # end to end through the C ABI on HOST arrays (bk5_apply_host): pinned
+    # host u -> device -> apply -> pinned host v every step, the elements cut
+    # into 8 chunks whose copies in and out (two copy streams) overlap the
+    # applies of the neighbouring chunks
     if not args.no_e2e:
         uh = torch.empty(u.numel(), dtype=u.dtype, pin_memory=True)
         vh = torch.empty_like(uh)
         uh.copy_(u)
+        hp = bk.HostPlan(5, P_ORDER, E, prec=prec)
 
-        def e2e():
-            u.copy_(uh, non_blocking=True)
-            apply()
-            vh.copy_(v, non_blocking=True)
+        def step_e2e():
+            hp.apply(uh, vh, G=G, D=D, engine=engine, layout=args.layout, kernel=kernel, stream=stream)
 
-        te = max_over_ranks(time_loop(e2e, max(3, steps // 10), 2, world, stream, torch), world)
+        te = max_over_ranks(time_loop(step_e2e, max(3, steps // 10), 2, world, stream, torch), world)
+        torch.cuda.synchronize()
+        e2e_err = float((vh.to(v.device) - v).abs().max())
+        hp.close()
         out["e2e"] = {"value": world * dofs / te / 1e9, "unit": UNIT, "h2d_bytes_per_step": u.element_size() * dofs,
                       "d2h_bytes_per_step": u.element_size() * dofs, "ms_per_step": te * 1e3,
-                      "note": "G (6.4 GB) resident on the device; u in, v out every step"}
+                      "max_abs_diff_vs_device_apply": e2e_err,
+                      "note": "bk5_apply_host: G (6.4 GB) resident on the device; u in, v out every step "
+                              "from/to pinned host memory in 8 element chunks, copies overlapping the applies"}
 
     # the forms side by side, with their error against the FP64 result
     if not args.no_forms and rank == 0 and prec == bk.PREC_FP64:

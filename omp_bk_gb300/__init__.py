@@ -45,6 +45,7 @@ EXPORTS = [
     "bk3_adjoint", "bk_stream_kernel", "bk_dot_workspace_bytes", "bk_dot", "bk_axpby",
     "bk_hplan_create", "bk_hplan_destroy", "bk_hplan_size", "bk_hplan_set_kernel", "bk_hplan_apply", "bk_hplan_cg",
     "bk_dot_noalloc",
+    "bk_host_plan_create", "bk_host_plan_destroy", "bk1_apply_host", "bk3_apply_host", "bk5_apply_host",
 ]
 
 
@@ -367,3 +368,58 @@ def axpby(a, x, b, y, stream=None):
     check(lib().bk_axpby(x.numel(), float(a), _ptr(x), float(b), _ptr(y), int(y.dtype == torch.float64),
                          _stream(stream)), "bk_axpby")
     return y
+
+
+# ---- applies on host arrays (include/bk_host.h) ------------------------------------
+
+class HostPlan:
+    """Applies of operator `op` (1, 3, 5) at order p over E elements whose u
+    and v live in HOST memory (pinned for overlap): element chunks go
+    host -> device -> apply -> host on three streams.  G/qdata/k stay on the
+    device.  apply() is asynchronous on `stream`; synchronize it before
+    reading v."""
+
+    def __init__(self, op, p, E, prec=PREC_FP64, chunk_elems=0):
+        L = lib()
+        if not getattr(L, "_host_declared", False):
+            L.bk_host_plan_create.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_int64, C.c_int, C.c_int64]
+            L.bk_host_plan_destroy.argtypes = [C.c_void_p]
+            L.bk1_apply_host.argtypes = [C.c_void_p, _dp, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                         C.c_void_p]
+            L.bk3_apply_host.argtypes = [C.c_void_p, _dp, _dp, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                         C.c_void_p, C.c_void_p]
+            L.bk5_apply_host.argtypes = [C.c_void_p, _dp, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                         C.c_void_p]
+            L._host_declared = True
+        self.op, self.p, self.E, self.prec = int(op), int(p), int(E), prec
+        h = C.c_void_p()
+        check(L.bk_host_plan_create(C.byref(h), self.op, self.p, self.E, prec, int(chunk_elems)),
+              "bk_host_plan_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().bk_host_plan_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def apply(self, u_host, v_host, G=None, B=None, D=None, k=None, engine=ENGINE_AUTO,
+              layout=LAYOUT_INTERLEAVED, nfactors=6, kernel=KERNEL_AUTO, stream=None):
+        """v_host = A u_host (torch CPU tensors or numpy arrays); G: qdata
+        (BK1) or the geometric factors (BK3, BK5) on the device."""
+        o = ApplyOptions(prec=self.prec, engine=engine, layout=layout, nfactors=nfactors, kernel=kernel).c()
+        uptr = u_host.data_ptr() if hasattr(u_host, "data_ptr") else u_host.ctypes.data
+        vptr = v_host.data_ptr() if hasattr(v_host, "data_ptr") else v_host.ctypes.data
+        L = lib()
+        if self.op == 1:
+            Bh, Bp = _host(B)
+            rc = L.bk1_apply_host(self.h, Bp, _ptr(G), uptr, vptr, C.byref(o), _stream(stream))
+        elif self.op == 3:
+            Bh, Bp = _host(B)
+            Dh, Dp = _host(D)
+            rc = L.bk3_apply_host(self.h, Bp, Dp, _ptr(G), _ptr(k), uptr, vptr, C.byref(o), _stream(stream))
+        else:
+            Dh, Dp = _host(D)
+            rc = L.bk5_apply_host(self.h, Dp, _ptr(G), uptr, vptr, C.byref(o), _stream(stream))
+        check(rc, f"bk{self.op}_apply_host")

@@ -234,8 +234,9 @@ inline int multi_wbox_bytes(int q, int eb, int vbytes)
     return eb * q * box_ps(q, vbytes) * vbytes;
 }
 
-// Shared memory of the even-odd launch: u stage, G stage, three work boxes
-// (each the largest tile's), one mbarrier.
+// Shared memory of the even-odd launch: u stage (followed by the mass stage,
+// of the same size), G stage, three work boxes (each the largest tile's), one
+// mbarrier.
 template <class Eng>
 inline void multi_eo_smem(const MultiSeg* seg, int nseg, int& u_bytes, int& g_bytes, int& w_bytes, int& total)
 {
@@ -252,7 +253,7 @@ inline void multi_eo_smem(const MultiSeg* seg, int nseg, int& u_bytes, int& g_by
         g_bytes = gb > g_bytes ? gb : g_bytes;
         w_bytes = wb > w_bytes ? wb : w_bytes;
     }
-    total = u_bytes + g_bytes + 3 * w_bytes + 16;
+    total = 2 * u_bytes + g_bytes + 3 * w_bytes + 16;
 }
 
 template <class Eng, int NT, int MINB>
@@ -261,13 +262,14 @@ __global__ void __launch_bounds__(NT, MINB)
                         const int ntiles, const typename Eng::S* __restrict__ u, const typename Eng::S* __restrict__ G,
                         const typename Eng::S* __restrict__ mass, const double lambda,
                         typename Eng::S* __restrict__ v, const int u_bytes, const int g_bytes, const int w_bytes,
-                        const DevCtx ctx)
+                        double* __restrict__ dot_part, const DevCtx ctx)
 {
     using S = typename Eng::S;
     using V = typename Eng::V;
     extern __shared__ __align__(16) unsigned char smem[];
     unsigned char* ustage = smem;
-    unsigned char* gstage = smem + u_bytes;
+    unsigned char* mstage = smem + u_bytes;
+    unsigned char* gstage = mstage + u_bytes;
     V* W0 = reinterpret_cast<V*>(gstage + g_bytes);
     V* W1 = reinterpret_cast<V*>(reinterpret_cast<unsigned char*>(W0) + w_bytes);
     V* W2 = reinterpret_cast<V*>(reinterpret_cast<unsigned char*>(W1) + w_bytes);
@@ -280,6 +282,8 @@ __global__ void __launch_bounds__(NT, MINB)
     }
     __syncthreads();
     uint32_t phase = 0;
+    double dacc = 0.0;   // u . A u over the block's points (dot_part only)
+    double* dp = dot_part != nullptr ? &dacc : nullptr;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, phase ^= 1u) {
         const MultiTile tl = tiles[t];
         const MultiSeg& sg = prm.seg[tl.seg];
@@ -289,15 +293,19 @@ __global__ void __launch_bounds__(NT, MINB)
         if (tid == 0) fence_proxy_async();
         const S* us = stage_issue<S>(ustage, u + sg.uoff + tl.e_first * q3, tl.ne * q3, bar, tx, tid, nt);
         const S* gs = stage_issue<S>(gstage, G + sg.goff + tl.e_first * 6 * q3, tl.ne * 6 * q3, bar, tx, tid, nt);
+        // the mass term's diagonal, staged too: read in the last pass, where
+        // a global load per point would stall every warp on its latency
+        const S* mb = (mass != nullptr)
+                          ? stage_issue<S>(mstage, mass + sg.uoff + tl.e_first * q3, tl.ne * q3, bar, tx, tid, nt)
+                          : nullptr;
         if (tid == 0) mbar_arrive_expect_tx(bar, tx);
         if (batch_wait_failed(bar, phase, ctx, tid)) return;
         S* vb = v + sg.uoff + tl.e_first * q3;
-        const S* mb = (mass != nullptr) ? mass + sg.uoff + tl.e_first * q3 : nullptr;
         switch (q) {
 #define BK_MULTI_EO_CASE(QQ)                                                                                    \
     case QQ:                                                                                                    \
         bk5_sweep_batch<Eng, QQ, 6, 2, true>(nullptr, prm.eo.template at<QQ>().eo, prm.eo.template at<QQ>().eot, \
-                                             us, gs, W0, W1, W2, tl.ne, tid, nt, vb, mb, lambda);               \
+                                             us, gs, W0, W1, W2, nullptr, tl.ne, tid, nt, vb, mb, lambda, dp);  \
         break;
             BK_MULTI_EO_CASE(3)
             BK_MULTI_EO_CASE(4)
@@ -309,6 +317,21 @@ __global__ void __launch_bounds__(NT, MINB)
 #undef BK_MULTI_EO_CASE
             default:
                 break;
+        }
+    }
+    if (dot_part != nullptr) {
+        // block sum of the threads' partial dot products, one value per block
+        // (the work boxes are free after the last tile; no static shared
+        // memory, which would shrink the dynamic limit)
+        double* wsum = reinterpret_cast<double*>(W0);
+        double s = dacc;
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if ((tid & 31) == 0) wsum[tid >> 5] = s;
+        __syncthreads();
+        if (tid == 0) {
+            double b = 0.0;
+            for (int w = 0; w < (nt + 31) / 32; ++w) b += wsum[w];
+            dot_part[blockIdx.x] = b;
         }
     }
 }

@@ -33,30 +33,46 @@ struct BK3AdjCfg {
 };
 
 // u (P^3, dense S) -> gradient components at the Q^3 points in (gr, gs, gt);
-// tmp is a scratch box.  gt also serves as the interpolation target.
-template <class Eng, class WB, int Q>
+// tmp is a scratch box.  gt also serves as the interpolation target.  EO:
+// the even-odd contractions of prm.bi (interpolation, centro-symmetric) and
+// prm.dg (derivative, centro-antisymmetric).
+template <class Eng, class WB, int Q, bool EO>
 __device__ __forceinline__ void grad_at_points(const typename Eng::S* src, typename Eng::V* tmp, typename Eng::V* gr,
                                                typename Eng::V* gs, typename Eng::V* gt, int ne,
-                                               const Mat<typename Eng::C, Q, true>& Bi,
-                                               const Mat<typename Eng::C, Q, true>& Dg, int tid, int nt)
+                                               const P13<typename Eng::C, Q>& prm, int tid, int nt)
 {
     constexpr int P = Q - 1;
+    const Mat<typename Eng::C, Q, true> Bi{prm.B};   // interpolation: M(p, i) = B[i*Q + p]
+    const Mat<typename Eng::C, Q, true> Dg{prm.D};   // derivative: q(p) = sum_n w(n) D(n, p)
     load_box<Eng, WB, P, P, P>(src, P * P * P, tmp, ne, tid, nt);
     __syncthreads();
-    sweep<Eng, WB, 0, P, P, P, Q>(tmp, gr, ne, Bi, tid, nt);   // (Q,P,P)
-    __syncthreads();
-    sweep<Eng, WB, 1, Q, P, P, Q>(gr, tmp, ne, Bi, tid, nt);   // (Q,Q,P)
-    __syncthreads();
-    sweep<Eng, WB, 2, Q, Q, P, Q>(tmp, gt, ne, Bi, tid, nt);   // w at the points
-    __syncthreads();
-    sweep<Eng, WB, 0, Q, Q, Q, Q>(gt, gr, ne, Dg, tid, nt);
-    sweep<Eng, WB, 1, Q, Q, Q, Q>(gt, gs, ne, Dg, tid, nt);
-    __syncthreads();
-    sweep<Eng, WB, 2, Q, Q, Q, Q>(gt, gt, ne, Dg, tid, nt);
+    if constexpr (EO) {
+        sweep_eor<Eng, WB, 0, P, P, P, Q, +1>(tmp, gr, ne, prm.bi, tid, nt);   // (Q,P,P)
+        __syncthreads();
+        sweep_eor<Eng, WB, 1, Q, P, P, Q, +1>(gr, tmp, ne, prm.bi, tid, nt);   // (Q,Q,P)
+        __syncthreads();
+        sweep_eor<Eng, WB, 2, Q, Q, P, Q, +1>(tmp, gt, ne, prm.bi, tid, nt);   // w at the points
+        __syncthreads();
+        sweep_eor<Eng, WB, 0, Q, Q, Q, Q, -1>(gt, gr, ne, prm.dg, tid, nt);
+        sweep_eor<Eng, WB, 1, Q, Q, Q, Q, -1>(gt, gs, ne, prm.dg, tid, nt);
+        __syncthreads();
+        sweep_eor<Eng, WB, 2, Q, Q, Q, Q, -1>(gt, gt, ne, prm.dg, tid, nt);
+    } else {
+        sweep<Eng, WB, 0, P, P, P, Q>(tmp, gr, ne, Bi, tid, nt);   // (Q,P,P)
+        __syncthreads();
+        sweep<Eng, WB, 1, Q, P, P, Q>(gr, tmp, ne, Bi, tid, nt);   // (Q,Q,P)
+        __syncthreads();
+        sweep<Eng, WB, 2, Q, Q, P, Q>(tmp, gt, ne, Bi, tid, nt);   // w at the points
+        __syncthreads();
+        sweep<Eng, WB, 0, Q, Q, Q, Q>(gt, gr, ne, Dg, tid, nt);
+        sweep<Eng, WB, 1, Q, Q, Q, Q>(gt, gs, ne, Dg, tid, nt);
+        __syncthreads();
+        sweep<Eng, WB, 2, Q, Q, Q, Q>(gt, gt, ne, Dg, tid, nt);
+    }
     __syncthreads();
 }
 
-template <class Eng, int Q, int EB>
+template <class Eng, int Q, int EB, bool EO = false>
 __global__ void __launch_bounds__(BK3AdjCfg<Eng, Q, EB>::NT)
     bk3_adjoint_kernel(const __grid_constant__ P13<typename Eng::C, Q> prm, const long long E,
                        const typename Eng::S* __restrict__ u, const typename Eng::S* __restrict__ res,
@@ -84,8 +100,6 @@ __global__ void __launch_bounds__(BK3AdjCfg<Eng, Q, EB>::NT)
     uint64_t* bar = reinterpret_cast<uint64_t*>(reinterpret_cast<unsigned char*>(W5 + EB * WB::size));
     const int tid = threadIdx.x;
     const int nt = Cfg::NT;
-    const Mat<typename Eng::C, Q, true> Bi{prm.B};   // interpolation: M(p, i) = B[i*Q + p]
-    const Mat<typename Eng::C, Q, true> Dg{prm.D};   // derivative: q(p) = sum_n w(n) D(n, p)
 
     if (tid == 0) {
         mbar_init(bar, 1);
@@ -106,8 +120,8 @@ __global__ void __launch_bounds__(BK3AdjCfg<Eng, Q, EB>::NT)
         if (tid == 0) mbar_arrive_expect_tx(bar, tx);
         if (batch_wait_failed(bar, phase, ctx, tid)) return;
         // g_u -> (W1, W2, W3) with W0 as scratch; g_res -> (W4, W5, W0) with W0 last
-        grad_at_points<Eng, WB, Q>(us, W0, W1, W2, W3, ne, Bi, Dg, tid, nt);
-        grad_at_points<Eng, WB, Q>(rs, W0, W4, W5, W0, ne, Bi, Dg, tid, nt);
+        grad_at_points<Eng, WB, Q, EO>(us, W0, W1, W2, W3, ne, prm, tid, nt);
+        grad_at_points<Eng, WB, Q, EO>(rs, W0, W4, W5, W0, ne, prm, tid, nt);
         for (int w = tid; w < ne * Q3; w += nt) {
             const int e = w / Q3;
             const int x = w - e * Q3;

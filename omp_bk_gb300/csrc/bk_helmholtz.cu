@@ -34,7 +34,8 @@ namespace bkg {
 namespace {
 
 constexpr int kNT = 256;   // threads per block of the persistent kernel
-constexpr int kRedBlocks = 608;
+constexpr int kRedBlocks = 1216;   // 8 blocks of 256 threads per SM
+constexpr int kMaxDotParts = 4864;  // blocks of the persistent launch at most (32 per SM)
 constexpr int kRedThreads = 256;
 
 enum Scalar { S_RR = 0, S_RR0, S_PAP, S_IT, S_TOL2, S_MAXIT, S_NORM, S_INV, S_RN2, S_FN2, S_NSCAL };
@@ -149,8 +150,11 @@ struct MultiEOLaunch {
         if (total > 232448) return 0;
         return prepare(total, threads(prm.seg, prm.nseg));
     }
+    // dot_part (optional): one partial sum of u . v per block, their count in
+    // *nparts
     static int run(const PMultiEO<typename Eng::C>& prm, const MultiTile* tiles, int ntiles, const void* u,
-                   const void* G, const void* mass, double lambda, void* v, cudaStream_t s)
+                   const void* G, const void* mass, double lambda, void* v, cudaStream_t s,
+                   double* dot_part = nullptr, int* nparts = nullptr)
     {
         using S = typename Eng::S;
         int ub = 0, gb = 0, wb = 0;
@@ -162,9 +166,12 @@ struct MultiEOLaunch {
         if (occ < 1) return BK_ERR_CUDA;
         int grid = occ * sm_count();
         if (grid > ntiles) grid = ntiles;
+        if (grid > kMaxDotParts) grid = kMaxDotParts;
+        if (nparts) *nparts = grid;
         if (grid < 1) return BK_OK;
         kern<<<grid, nt, total, s>>>(prm, tiles, ntiles, static_cast<const S*>(u), static_cast<const S*>(G),
-                                     static_cast<const S*>(mass), lambda, static_cast<S*>(v), ub, gb, wb, dev_ctx());
+                                     static_cast<const S*>(mass), lambda, static_cast<S*>(v), ub, gb, wb, dot_part,
+                                     dev_ctx());
         return cudaGetLastError() == cudaSuccess ? BK_OK : BK_ERR_CUDA;
     }
 };
@@ -183,21 +190,42 @@ __global__ void cg_start_kernel(long long n, const double* __restrict__ r64, con
     }
 }
 
-// partial sums of x.y (FP64) per block
-__global__ void __launch_bounds__(kRedThreads) red_dot_kernel(long long n, const float* __restrict__ x,
-                                                              const float* __restrict__ y, double* __restrict__ part)
+// The FP32 vectors of the inner CG are 16-byte aligned allocations: their
+// loops run over float4 groups (one 16-byte load per vector and thread and
+// iteration, enough bytes in flight for HBM) and a scalar tail of n % 4.
+
+__device__ __forceinline__ double block_reduce(double s)
 {
     __shared__ double sh[kRedThreads];
-    double s = 0.0;
-    for (long long i = blockIdx.x * (long long)kRedThreads + threadIdx.x; i < n; i += (long long)gridDim.x * kRedThreads)
-        s = fma(double(x[i]), double(y[i]), s);
     sh[threadIdx.x] = s;
     __syncthreads();
     for (int w = kRedThreads / 2; w > 0; w >>= 1) {
         if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
         __syncthreads();
     }
-    if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+    return sh[0];
+}
+
+// partial sums of x.y (FP64) per block
+__global__ void __launch_bounds__(kRedThreads) red_dot_kernel(long long n, const float* __restrict__ x,
+                                                              const float* __restrict__ y, double* __restrict__ part)
+{
+    const long long n4 = n / 4;
+    const long long stride = (long long)gridDim.x * kRedThreads;
+    const float4* x4 = reinterpret_cast<const float4*>(x);
+    const float4* y4 = reinterpret_cast<const float4*>(y);
+    double s = 0.0;
+    for (long long i = blockIdx.x * (long long)kRedThreads + threadIdx.x; i < n4; i += stride) {
+        const float4 a = x4[i], b = y4[i];
+        s = fma(double(a.x), double(b.x), s);
+        s = fma(double(a.y), double(b.y), s);
+        s = fma(double(a.z), double(b.z), s);
+        s = fma(double(a.w), double(b.w), s);
+    }
+    for (long long i = 4 * n4 + blockIdx.x * (long long)kRedThreads + threadIdx.x; i < n; i += stride)
+        s = fma(double(x[i]), double(y[i]), s);
+    const double t = block_reduce(s);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
 }
 
 __device__ __forceinline__ double block_sum(const double* __restrict__ part, int nb)
@@ -239,23 +267,39 @@ __global__ void __launch_bounds__(kRedThreads) cg_update_kernel(long long n, con
                                                                 const float* __restrict__ Ap, float* __restrict__ d,
                                                                 float* __restrict__ r, double* __restrict__ part)
 {
-    __shared__ double sh[kRedThreads];
     const double pap = sc[S_PAP];
     const float alpha = float(pap != 0.0 ? sc[S_RR] / pap : 0.0);
+    const long long n4 = n / 4;
+    const long long stride = (long long)gridDim.x * kRedThreads;
     double s = 0.0;
-    for (long long i = blockIdx.x * (long long)kRedThreads + threadIdx.x; i < n; i += (long long)gridDim.x * kRedThreads) {
+    for (long long i = blockIdx.x * (long long)kRedThreads + threadIdx.x; i < n4; i += stride) {
+        const float4 pp = reinterpret_cast<const float4*>(p)[i];
+        const float4 aa = reinterpret_cast<const float4*>(Ap)[i];
+        float4 dd = reinterpret_cast<float4*>(d)[i];
+        float4 rr = reinterpret_cast<float4*>(r)[i];
+        dd.x = fmaf(alpha, pp.x, dd.x);
+        dd.y = fmaf(alpha, pp.y, dd.y);
+        dd.z = fmaf(alpha, pp.z, dd.z);
+        dd.w = fmaf(alpha, pp.w, dd.w);
+        rr.x = fmaf(-alpha, aa.x, rr.x);
+        rr.y = fmaf(-alpha, aa.y, rr.y);
+        rr.z = fmaf(-alpha, aa.z, rr.z);
+        rr.w = fmaf(-alpha, aa.w, rr.w);
+        reinterpret_cast<float4*>(d)[i] = dd;
+        reinterpret_cast<float4*>(r)[i] = rr;
+        s = fma(double(rr.x), double(rr.x), s);
+        s = fma(double(rr.y), double(rr.y), s);
+        s = fma(double(rr.z), double(rr.z), s);
+        s = fma(double(rr.w), double(rr.w), s);
+    }
+    for (long long i = 4 * n4 + blockIdx.x * (long long)kRedThreads + threadIdx.x; i < n; i += stride) {
         d[i] = fmaf(alpha, p[i], d[i]);
         const float ri = fmaf(-alpha, Ap[i], r[i]);
         r[i] = ri;
         s = fma(double(ri), double(ri), s);
     }
-    sh[threadIdx.x] = s;
-    __syncthreads();
-    for (int w = kRedThreads / 2; w > 0; w >>= 1) {
-        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+    const double t = block_reduce(s);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
 }
 
 // rr_new, beta, iteration count and the loop condition
@@ -279,10 +323,20 @@ __global__ void cg_dir_kernel(long long n, const double* __restrict__ beta_in, c
                               float* __restrict__ p)
 {
     const float beta = float(beta_in[0]);
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    const long long n4 = n / 4;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4; i += stride) {
+        const float4 rr = reinterpret_cast<const float4*>(r)[i];
+        float4 pp = reinterpret_cast<float4*>(p)[i];
+        pp.x = fmaf(beta, pp.x, rr.x);
+        pp.y = fmaf(beta, pp.y, rr.y);
+        pp.z = fmaf(beta, pp.z, rr.z);
+        pp.w = fmaf(beta, pp.w, rr.w);
+        reinterpret_cast<float4*>(p)[i] = pp;
+    }
+    for (long long i = 4 * n4 + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride)
         p[i] = fmaf(beta, p[i], r[i]);
 }
-
 // x += |r| d (FP64), the norm from the scalars
 __global__ void cg_correct_kernel(long long n, const double* __restrict__ sc, const float* __restrict__ d,
                                   double* __restrict__ x)
@@ -530,9 +584,18 @@ int build_inner_graph(bk_hplan* h, const void* G32, const void* mass32, double l
                 cudaSuccess) {
                 rc = BK_ERR_CUDA;
             } else {
-                int arc = apply_plan(h, 3, G32, mass32, lambda, h->p32, h->Ap32, s);
-                red_dot_kernel<<<kRedBlocks, kRedThreads, 0, s>>>(n, h->p32, h->Ap32, h->part);
-                cg_pap_kernel<<<1, kRedThreads, 0, s>>>(h->part, kRedBlocks, h->sc);
+                int arc;
+                if (h->kernel == BK_KERNEL_SWEEP) {
+                    // p . Ap summed by the apply itself (one partial per block)
+                    int nparts = 0;
+                    arc = MultiEOLaunch<EngMixed, 256, 2>::run(h->e_f32, h->tiles, h->ntiles, h->p32, G32, mass32,
+                                                                lambda, h->Ap32, s, h->part, &nparts);
+                    cg_pap_kernel<<<1, kRedThreads, 0, s>>>(h->part, nparts, h->sc);
+                } else {
+                    arc = apply_plan(h, 3, G32, mass32, lambda, h->p32, h->Ap32, s);
+                    red_dot_kernel<<<kRedBlocks, kRedThreads, 0, s>>>(n, h->p32, h->Ap32, h->part);
+                    cg_pap_kernel<<<1, kRedThreads, 0, s>>>(h->part, kRedBlocks, h->sc);
+                }
                 cg_update_kernel<<<kRedBlocks, kRedThreads, 0, s>>>(n, h->sc, h->p32, h->Ap32, h->d32, h->r32,
                                                                     h->part);
                 cg_step_kernel<<<1, kRedThreads, 0, s>>>(h->part, kRedBlocks, h->sc, h->beta, handle);
@@ -625,7 +688,7 @@ int bk_hplan_create(bk_hplan_t* out, int norders, const bk_order_range* orders, 
     rc |= ck(cudaMalloc(&h->p32, 4 * (nb + 4)));
     rc |= ck(cudaMalloc(&h->Ap32, 4 * (nb + 4)));
     rc |= ck(cudaMalloc(&h->d32, 4 * (nb + 4)));
-    rc |= ck(cudaMalloc(&h->part, 8 * kRedBlocks));
+    rc |= ck(cudaMalloc(&h->part, 8 * (kRedBlocks > kMaxDotParts ? kRedBlocks : kMaxDotParts)));
     rc |= ck(cudaMalloc(&h->sc, 8 * S_NSCAL));
     rc |= ck(cudaMalloc(&h->beta, 8 * 2));
     if (rc == BK_OK && h->ntiles > 0)

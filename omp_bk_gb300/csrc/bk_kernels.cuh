@@ -237,6 +237,58 @@ __device__ __forceinline__ void sweep_eo(const typename Eng::V* in, typename Eng
     }
 }
 
+// sweep_eo with the direction dir (0, 1, 2) given at run time: the line's
+// strides are computed, not constants, so that one code body serves all
+// three directions.
+template <class Eng, class WB, int Q, class EM>
+__device__ __forceinline__ void sweep_eo_dyn(const typename Eng::V* in, typename Eng::V* out, int ne, const EM& m,
+                                             int tid, int nt, int dir)
+{
+    using V = typename Eng::V;
+    using A = typename Eng::A;
+    constexpr int H = Q / 2;
+    constexpr int L = Q * Q;
+    const int SD = dir == 0 ? WB::PS : (dir == 1 ? WB::ZP : 1);
+    const int SA = dir == 0 ? WB::ZP : WB::PS;   // stride of the line's first index
+    const int SB = dir == 2 ? WB::ZP : 1;        // stride of its second index
+    for (int w = tid; w < ne * L; w += nt) {
+        const int e = w / L;
+        const int l = w - e * L;
+        const int a = l / Q;
+        const int b = l - a * Q;
+        const V* pi = in + e * WB::size + a * SA + b * SB;
+        V* po = out + e * WB::size + a * SA + b * SB;
+        V x[Q];
+#pragma unroll
+        for (int n = 0; n < Q; ++n) x[n] = pi[n * SD];
+        V ev[H > 0 ? H : 1], dv[H > 0 ? H : 1];
+#pragma unroll
+        for (int n = 0; n < H; ++n) {
+            ev[n] = Eng::vadd(x[n], x[Q - 1 - n]);
+            dv[n] = Eng::vsub(x[n], x[Q - 1 - n]);
+        }
+#pragma unroll
+        for (int o = 0; o < H; ++o) {
+            A aa = Eng::zero(), bb = Eng::zero();
+#pragma unroll
+            for (int n = 0; n < H; ++n) {
+                Eng::madd(aa, m.A[o * H + n], ev[n]);
+                Eng::madd(bb, m.B[o * H + n], dv[n]);
+            }
+            if (Q & 1) Eng::madd(aa, m.c[o], x[H]);
+            const V av = Eng::result(aa), bv = Eng::result(bb);
+            po[o * SD] = Eng::vadd(bv, av);
+            po[(Q - 1 - o) * SD] = Eng::vsub(bv, av);
+        }
+        if (Q & 1) {
+            A t = Eng::zero();
+#pragma unroll
+            for (int n = 0; n < H; ++n) Eng::madd(t, m.r[n], dv[n]);
+            po[H * SD] = Eng::result(t);
+        }
+    }
+}
+
 // Even-odd form of a rectangular NO x NI matrix with M(NO-1-o, NI-1-n) =
 // SIGN M(o, n): the interpolation matrix between point sets symmetric about 0
 // (SIGN = +1) and the derivative matrix (SIGN = -1), or their transposes.
@@ -438,35 +490,52 @@ __device__ __forceinline__ int g_index(int i, int j, int f, int k)
 // leaves the block's shared memory to u and the work boxes.  NBUF: stage
 // buffers (2: the block's next batch is copied while it computes the
 // current one).
-template <class Eng, int Q, int EB, int F, int LAYOUT, bool GD = false, int NBUF = 1>
+// DPAR != 0: three thread groups, one direction each (bk5_sweep_batch), and
+// a fourth work box.
+template <class Eng, int Q, int EB, int F, int LAYOUT, bool GD = false, int NBUF = 1, int DPAR = 0>
 struct BK5Cfg {
     using S = typename Eng::S;
     using V = typename Eng::V;
     using WB = WBox<Q, V>;
     static constexpr int Q3 = Q * Q * Q;
-    static constexpr int NT = ((EB * Q * Q + 31) / 32) * 32 < 64 ? 64 : ((EB * Q * Q + 31) / 32) * 32;
+    static constexpr int LINES = ((EB * Q * Q + 31) / 32) * 32;   // one direction, whole warps
+    static constexpr int NT = DPAR ? 3 * LINES : (LINES < 64 ? 64 : LINES);
+    static constexpr int NBOX = DPAR ? 4 : 3;
     static constexpr int U_BYTES = stage_bytes<S>(EB * Q3);
     static constexpr int G_BYTES = GD ? 0 : stage_bytes<S>(EB * F * Q3);
     static constexpr int STAGE_BYTES = U_BYTES + G_BYTES;
-    static constexpr int W_BYTES = 3 * EB * WB::size * int(sizeof(V));
+    static constexpr int W_BYTES = NBOX * EB * WB::size * int(sizeof(V));
     static constexpr int SMEM = NBUF * STAGE_BYTES + W_BYTES + 16 * NBUF;
 };
 
-// One batch of ne elements of order Q whose u (us) and G (gs, in LAYOUT) are
-// staged densely in shared memory (gs may also point to global memory).
-// Dp: D(i, n) in parameter space; eo, eot: the even-odd forms of D and D^T
-// (used when EO).  W0..W2: three padded work boxes of at least ne elements.
-// v is written at vb (global), the mass term read at mb (global, may be
-// NULL).  Ends with a block barrier (after which the stages may be reused).
-template <class Eng, int Q, int F, int LAYOUT, bool EO>
+// One batch of ne elements of order Q whose u (us, dense; shared or global
+// memory) and G (gs, in LAYOUT; shared or global memory) are given.  Dp:
+// D(i, n) in parameter space; eo, eot: the even-odd forms of D and D^T (used
+// when EO).  W0..W3: padded work boxes of at least ne elements (W3 only
+// when DPAR).  v is written at vb (global), the mass term read at mb (global
+// or shared, may be NULL) with u at us.  dot (optional): the thread's
+// running sum of u . v over its points (FP64).  Ends with a block barrier
+// (after which the stages may be reused).
+//
+// DPAR (even-odd only): the three sweeps of a stage run at the same time on
+// three thread groups of nt/3 threads, one direction per group (warp-uniform
+// branches when nt/3 is a multiple of 32); qt goes to the fourth box.  Three
+// times the threads per element at the same shared memory per element: the
+// latency-bound float-float arithmetic gets more warps per SM.  DPAR = 1:
+// one code body per direction (strides known at compile time); DPAR = 2: one
+// body for all three, the direction's strides in registers (a third of the
+// instruction footprint of the stage).
+template <class Eng, int Q, int F, int LAYOUT, bool EO, int DPAR = 0>
 __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restrict__ Dp,
                                                 const EOMat<typename Eng::C, Q>& eo,
                                                 const EOMat<typename Eng::C, Q>& eot, const typename Eng::S* us,
                                                 const typename Eng::S* gs, typename Eng::V* W0, typename Eng::V* W1,
-                                                typename Eng::V* W2, int ne, int tid, int nt,
+                                                typename Eng::V* W2, typename Eng::V* W3, int ne, int tid, int nt,
                                                 typename Eng::S* __restrict__ vb,
-                                                const typename Eng::S* __restrict__ mb, double lambda)
+                                                const typename Eng::S* __restrict__ mb, double lambda,
+                                                double* dot = nullptr)
 {
+    static_assert(!DPAR || EO, "direction-parallel sweeps need the even-odd form");
     using S = typename Eng::S;
     using V = typename Eng::V;
     using A = typename Eng::A;
@@ -475,12 +544,23 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
     const Mat<typename Eng::C, Q, false> Dm{Dp};   // D(i, n)
     const Mat<typename Eng::C, Q, true> Dt{Dp};    // D(n, i)
     const S lam = S(lambda);
+    // thread group of the direction-parallel stages
+    const int ntd = DPAR ? nt / 3 : nt;
+    const int grp = DPAR ? tid / ntd : 0;
+    const int tg = tid - grp * ntd;
+    V* QT = DPAR ? W3 : W2;   // qt, and the third transposed term
     // 2. u -> W2 (working type, padded)
     load_box<Eng, WB, Q, Q, Q>(us, Q3, W2, ne, tid, nt);
     __syncthreads();
-    // 3. gradient: qr -> W0 (along i), qs -> W1 (along j); qt along k
-    //    in place into W2 after the other two have read it
-    if constexpr (EO) {
+    // 3. gradient: qr -> W0 (along i), qs -> W1 (along j), qt (along k) ->
+    //    QT (in place into W2 after the other two have read it unless DPAR)
+    if constexpr (DPAR == 2) {
+        if (grp < 3) sweep_eo_dyn<Eng, WB, Q>(W2, grp == 0 ? W0 : (grp == 1 ? W1 : W3), ne, eo, tg, ntd, grp);
+    } else if constexpr (DPAR == 1) {
+        if (grp == 0) sweep_eo<Eng, WB, 0, Q>(W2, W0, ne, eo, tg, ntd);
+        else if (grp == 1) sweep_eo<Eng, WB, 1, Q>(W2, W1, ne, eo, tg, ntd);
+        else if (grp == 2) sweep_eo<Eng, WB, 2, Q>(W2, W3, ne, eo, tg, ntd);
+    } else if constexpr (EO) {
         sweep_eo<Eng, WB, 0, Q>(W2, W0, ne, eo, tid, nt);
         sweep_eo<Eng, WB, 1, Q>(W2, W1, ne, eo, tid, nt);
         __syncthreads();
@@ -507,7 +587,7 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
             k = x % Q;
         }
         const int wi = e * WB::size + WB::at(i, j, k);
-        const V qr = W0[wi], qs = W1[wi], qt = W2[wi];
+        const V qr = W0[wi], qs = W1[wi], qt = QT[wi];
         const S* ge = gs + e * F * Q3;
         auto g = [&](int f) { return Eng::load(ge[g_index<Eng, Q, F, LAYOUT>(i, j, f, k)]); };
         A r0 = Eng::zero(), r1 = Eng::zero(), r2 = Eng::zero();
@@ -523,11 +603,21 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
         }
         W0[wi] = Eng::result(r0);
         W1[wi] = Eng::result(r1);
-        W2[wi] = Eng::result(r2);
+        QT[wi] = Eng::result(r2);
     }
     __syncthreads();
-    // 5. transposed derivatives: along i in place on W0, along j on W1
-    if constexpr (EO) {
+    // 5. transposed derivatives, in place: along i on W0, along j on W1 and
+    //    (even-odd) along k on QT
+    if constexpr (DPAR == 2) {
+        if (grp < 3) {
+            V* Wg = grp == 0 ? W0 : (grp == 1 ? W1 : W3);
+            sweep_eo_dyn<Eng, WB, Q>(Wg, Wg, ne, eot, tg, ntd, grp);
+        }
+    } else if constexpr (DPAR == 1) {
+        if (grp == 0) sweep_eo<Eng, WB, 0, Q>(W0, W0, ne, eot, tg, ntd);
+        else if (grp == 1) sweep_eo<Eng, WB, 1, Q>(W1, W1, ne, eot, tg, ntd);
+        else if (grp == 2) sweep_eo<Eng, WB, 2, Q>(W3, W3, ne, eot, tg, ntd);
+    } else if constexpr (EO) {
         sweep_eo<Eng, WB, 0, Q>(W0, W0, ne, eot, tid, nt);
         sweep_eo<Eng, WB, 1, Q>(W1, W1, ne, eot, tid, nt);
         __syncthreads();
@@ -537,10 +627,9 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
         sweep<Eng, WB, 1, Q, Q, Q, Q>(W1, W1, ne, Dt, tid, nt);
     }
     __syncthreads();
-    // 6. along k on W2 (already contracted when EO), plus the other two
-    //    terms, back into W2 (each line is read completely before it is
-    //    written; lines are disjoint)
-    {
+    if constexpr (!EO) {
+        // 6. along k on W2 plus the other two terms, back into W2 (each line
+        //    is read completely before it is written; lines are disjoint)
         constexpr int L = Q * Q;
         for (int w = tid; w < ne * L; w += nt) {
             const int e = w / L;
@@ -554,12 +643,8 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
 #pragma unroll
             for (int o = 0; o < Q; ++o) {
                 A acc = Eng::zero();
-                if constexpr (EO) {
-                    Eng::add(acc, x[o]);
-                } else {
 #pragma unroll
-                    for (int n = 0; n < Q; ++n) Eng::madd(acc, Dt(o, n), x[n]);
-                }
+                for (int n = 0; n < Q; ++n) Eng::madd(acc, Dt(o, n), x[n]);
                 V res;
                 if constexpr (HasSum3<Eng>::value) {
                     res = Eng::sum3(Eng::result(acc), W0[base + o], W1[base + o]);
@@ -571,33 +656,51 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
                 W2[base + o] = res;
             }
         }
+        __syncthreads();
     }
-    __syncthreads();
-    // 7. padded box -> v in global memory (coalesced), with the Helmholtz
-    //    mass term lambda * mass * u in the storage type's arithmetic
-    //    (double for the FP64 engines)
+    // 7. -> v in global memory (consecutive threads, consecutive values):
+    //    the sum of the three terms (even-odd: here; otherwise already in W2)
+    //    and the Helmholtz mass term lambda * mass * u in the storage type's
+    //    arithmetic (double for the FP64 engines)
     for (int w = tid; w < ne * Q3; w += nt) {
         const int e = w / Q3;
         const int x = w - e * Q3;
         const int i = x / (Q * Q);
         const int j = (x / Q) % Q;
         const int k = x % Q;
-        S out = Eng::store(W2[e * WB::size + WB::at(i, j, k)]);
+        const int wi = e * WB::size + WB::at(i, j, k);
+        V res;
+        if constexpr (EO) {
+            if constexpr (HasSum3<Eng>::value) {
+                res = Eng::sum3(QT[wi], W0[wi], W1[wi]);
+            } else {
+                A acc = Eng::zero();
+                Eng::add(acc, QT[wi]);
+                Eng::add(acc, W0[wi]);
+                Eng::add(acc, W1[wi]);
+                res = Eng::result(acc);
+            }
+        } else {
+            res = W2[wi];
+        }
+        S out = Eng::store(res);
         if (mb != nullptr) out += lam * mb[w] * us[w];
         vb[w] = out;
+        if (dot != nullptr) *dot = fma(double(us[w]), double(out), *dot);   // u . A u, for CG
     }
     __syncthreads();
 }
 
-template <class Eng, int Q, int EB, int F, int LAYOUT, bool EO = false, bool GD = false, int NBUF = 1>
-__global__ void __launch_bounds__(BK5Cfg<Eng, Q, EB, F, LAYOUT, GD, NBUF>::NT)
+template <class Eng, int Q, int EB, int F, int LAYOUT, bool EO = false, bool GD = false, int NBUF = 1,
+          int DPAR = 0>
+__global__ void __launch_bounds__(BK5Cfg<Eng, Q, EB, F, LAYOUT, GD, NBUF, DPAR>::NT)
     bk5_kernel(const __grid_constant__ P5<typename Eng::C, Q> prm, const long long E,
                const typename Eng::S* __restrict__ u, const typename Eng::S* __restrict__ G,
                const typename Eng::S* __restrict__ mass, const double lambda, typename Eng::S* __restrict__ v,
                const DevCtx ctx)
 {
     static_assert(NBUF == 1 || NBUF == 2, "one or two stage buffers");
-    using Cfg = BK5Cfg<Eng, Q, EB, F, LAYOUT, GD, NBUF>;
+    using Cfg = BK5Cfg<Eng, Q, EB, F, LAYOUT, GD, NBUF, DPAR>;
     using S = typename Eng::S;
     using V = typename Eng::V;
     using WB = typename Cfg::WB;
@@ -606,7 +709,8 @@ __global__ void __launch_bounds__(BK5Cfg<Eng, Q, EB, F, LAYOUT, GD, NBUF>::NT)
     V* W0 = reinterpret_cast<V*>(smem + NBUF * Cfg::STAGE_BYTES);
     V* W1 = W0 + EB * WB::size;
     V* W2 = W1 + EB * WB::size;
-    uint64_t* bars = reinterpret_cast<uint64_t*>(reinterpret_cast<unsigned char*>(W2 + EB * WB::size));
+    V* W3 = DPAR ? W2 + EB * WB::size : nullptr;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(reinterpret_cast<unsigned char*>(W0 + Cfg::NBOX * EB * WB::size));
     const int tid = threadIdx.x;
     const int nt = Cfg::NT;
 
@@ -660,9 +764,9 @@ __global__ void __launch_bounds__(BK5Cfg<Eng, Q, EB, F, LAYOUT, GD, NBUF>::NT)
         }
         const long long e0 = bt * EB;
         const int ne = int((E - e0) < EB ? (E - e0) : EB);
-        bk5_sweep_batch<Eng, Q, F, LAYOUT, EO>(prm.D, prm.eo, prm.eot, b == 0 ? us0 : us1, b == 0 ? gs0 : gs1, W0, W1,
-                                               W2, ne, tid, nt, v + e0 * Q3,
-                                               (mass != nullptr) ? mass + e0 * Q3 : nullptr, lambda);
+        bk5_sweep_batch<Eng, Q, F, LAYOUT, EO, DPAR>(prm.D, prm.eo, prm.eot, b == 0 ? us0 : us1, b == 0 ? gs0 : gs1,
+                                                     W0, W1, W2, W3, ne, tid, nt, v + e0 * Q3,
+                                                     (mass != nullptr) ? mass + e0 * Q3 : nullptr, lambda);
     }
 }
 
@@ -753,7 +857,10 @@ __global__ void __launch_bounds__(BK1Cfg<Eng, Q, EB>::NT)
 
 // ---- BK3 -----------------------------------------------------------------------
 
-template <class Eng, int Q, int EB>
+// DPAR != 0: three thread groups run the three gradient sweeps and the three
+// transposed ones at the same time (one shared code body); the other stages
+// use all threads.
+template <class Eng, int Q, int EB, int DPAR = 0>
 struct BK3Cfg {
     using S = typename Eng::S;
     using V = typename Eng::V;
@@ -761,7 +868,8 @@ struct BK3Cfg {
     static constexpr int P = Q - 1;
     static constexpr int Q3 = Q * Q * Q;
     static constexpr int P3 = P * P * P;
-    static constexpr int NT = ((EB * Q * Q + 31) / 32) * 32 < 64 ? 64 : ((EB * Q * Q + 31) / 32) * 32;
+    static constexpr int LINES = ((EB * Q * Q + 31) / 32) * 32;
+    static constexpr int NT = DPAR ? 3 * LINES : (LINES < 64 ? 64 : LINES);
     static constexpr int U_BYTES = stage_bytes<S>(EB * P3);
     static constexpr int G_BYTES = stage_bytes<S>(EB * 6 * Q3);
     static constexpr int K_BYTES = stage_bytes<S>(EB * Q3);
@@ -769,13 +877,14 @@ struct BK3Cfg {
     static constexpr int SMEM = U_BYTES + G_BYTES + K_BYTES + W_BYTES + 16;
 };
 
-template <class Eng, int Q, int EB, bool EO = false>
-__global__ void __launch_bounds__(BK3Cfg<Eng, Q, EB>::NT)
+template <class Eng, int Q, int EB, bool EO = false, int DPAR = 0>
+__global__ void __launch_bounds__(BK3Cfg<Eng, Q, EB, DPAR>::NT)
     bk3_kernel(const __grid_constant__ P13<typename Eng::C, Q> prm, const long long E,
                const typename Eng::S* __restrict__ u, const typename Eng::S* __restrict__ G,
                const typename Eng::S* __restrict__ kq, typename Eng::S* __restrict__ v, const DevCtx ctx)
 {
-    using Cfg = BK3Cfg<Eng, Q, EB>;
+    static_assert(!DPAR || EO, "direction-parallel sweeps need the even-odd form");
+    using Cfg = BK3Cfg<Eng, Q, EB, DPAR>;
     using S = typename Eng::S;
     using V = typename Eng::V;
     using A = typename Eng::A;
@@ -823,9 +932,16 @@ __global__ void __launch_bounds__(BK3Cfg<Eng, Q, EB>::NT)
             __syncthreads();
             sweep_eor<Eng, WB, 2, Q, Q, P, Q, +1>(W0, W2, ne, prm.bi, tid, nt);   // u at the points: W2
             __syncthreads();
-            sweep_eor<Eng, WB, 0, Q, Q, Q, Q, -1>(W2, W0, ne, prm.dg, tid, nt);   // qr
-            sweep_eor<Eng, WB, 1, Q, Q, Q, Q, -1>(W2, W1, ne, prm.dg, tid, nt);   // qs
-            sweep_eor<Eng, WB, 2, Q, Q, Q, Q, -1>(W2, W3, ne, prm.dg, tid, nt);   // qt
+            if constexpr (DPAR) {
+                const int grp = tid / Cfg::LINES;
+                if (grp < 3)
+                    sweep_eo_dyn<Eng, WB, Q>(W2, grp == 0 ? W0 : (grp == 1 ? W1 : W3), ne, prm.dg,
+                                             tid - grp * Cfg::LINES, Cfg::LINES, grp);   // qr, qs, qt
+            } else {
+                sweep_eor<Eng, WB, 0, Q, Q, Q, Q, -1>(W2, W0, ne, prm.dg, tid, nt);   // qr
+                sweep_eor<Eng, WB, 1, Q, Q, Q, Q, -1>(W2, W1, ne, prm.dg, tid, nt);   // qs
+                sweep_eor<Eng, WB, 2, Q, Q, Q, Q, -1>(W2, W3, ne, prm.dg, tid, nt);   // qt
+            }
         } else {
             sweep<Eng, WB, 0, P, P, P, Q>(W0, W1, ne, Bi, tid, nt);   // (Q,P,P)
             __syncthreads();
@@ -862,7 +978,13 @@ __global__ void __launch_bounds__(BK3Cfg<Eng, Q, EB>::NT)
             W3[wi] = Eng::result(r2);
         }
         __syncthreads();
-        if constexpr (EO) {
+        if constexpr (DPAR) {
+            const int grp = tid / Cfg::LINES;
+            if (grp < 3) {
+                V* Wg = grp == 0 ? W0 : (grp == 1 ? W1 : W3);
+                sweep_eo_dyn<Eng, WB, Q>(Wg, Wg, ne, prm.dtr, tid - grp * Cfg::LINES, Cfg::LINES, grp);
+            }
+        } else if constexpr (EO) {
             sweep_eor<Eng, WB, 0, Q, Q, Q, Q, -1>(W0, W0, ne, prm.dtr, tid, nt);
             sweep_eor<Eng, WB, 1, Q, Q, Q, Q, -1>(W1, W1, ne, prm.dtr, tid, nt);
             sweep_eor<Eng, WB, 2, Q, Q, Q, Q, -1>(W3, W3, ne, prm.dtr, tid, nt);

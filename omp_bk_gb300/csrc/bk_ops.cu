@@ -107,26 +107,18 @@ int grid_for(long long nbatch, int occ)
 }
 
 #if BK_OP_TU == 5
-template <int Q, int EB, int F, int LAYOUT, bool GD>
-int bk5_q(const double* D, long long E, const void* u, const void* G, const void* mass, double lambda, void* v,
-          cudaStream_t s)
+// One launch of bk5_kernel with the given shape.  One stage buffer: double
+// buffering (NBUF = 2) measured no faster than the overlap of the blocks
+// resident on an SM, which one buffer keeps more of.
+template <int Q, int EB, int F, int LAYOUT, bool EO, int DPAR>
+int bk5_launch(const P5<typename Eng::C, Q>& prm, long long E, const void* u, const void* G, const void* mass,
+               double lambda, void* v, cudaStream_t s)
 {
-    // one stage buffer: double buffering (NB = 2) measured no faster than
-    // the overlap of the blocks resident on an SM, which one buffer keeps
-    // more of
-    constexpr int NB = 1;
-    using Cfg = BK5Cfg<Eng, Q, EB, F, LAYOUT, GD, NB>;
+    using Cfg = BK5Cfg<Eng, Q, EB, F, LAYOUT, false, 1, DPAR>;
     using S = typename Eng::S;
     static_assert(Cfg::SMEM <= 232448, "BK5 block exceeds the shared memory of an SM");
-    P5<typename Eng::C, Q> prm;
-    for (int i = 0; i < Q * Q; ++i) prm.D[i] = Eng::coef(D[i]);
-    // the even-odd contractions when D is centro-antisymmetric (GLL points);
-    // instantiated for the symmetric 6-factor G only
-    const bool eo = (F == 6) && make_eo<typename Eng::C, Q>(D, false, prm.eo, &Eng::coef) &&
-                    make_eo<typename Eng::C, Q>(D, true, prm.eot, &Eng::coef);
-    auto kern = eo ? bk5_kernel<Eng, Q, EB, F, LAYOUT, (F == 6), GD, NB> : bk5_kernel<Eng, Q, EB, F, LAYOUT, false, GD, NB>;
-    const int occ = eo ? prepare<EoTag<Cfg, true>>(kern, Cfg::SMEM, Cfg::NT)
-                       : prepare<Cfg>(kern, Cfg::SMEM, Cfg::NT);
+    auto kern = bk5_kernel<Eng, Q, EB, F, LAYOUT, EO, false, 1, DPAR>;
+    const int occ = prepare<EoTag<Cfg, EO>>(kern, Cfg::SMEM, Cfg::NT);
     if (occ <= 0) return BK_ERR_CUDA;
     const int grid = grid_for((E + EB - 1) / EB, occ);
     kern<<<grid, Cfg::NT, Cfg::SMEM, s>>>(prm, E, static_cast<const S*>(u), static_cast<const S*>(G),
@@ -135,14 +127,21 @@ int bk5_q(const double* D, long long E, const void* u, const void* G, const void
 }
 
 // the largest EB <= EB0 whose block fits an SM's shared memory
-template <int Q, int F, int EB0>
+template <int Q, int F, int EB0, int DPAR = 0>
 constexpr int fit_eb5()
 {
-    if constexpr (EB0 > 1 && BK5Cfg<Eng, Q, EB0, F, BK_LAYOUT_TU>::SMEM > 232448)
-        return fit_eb5<Q, F, EB0 - 1>();
+    if constexpr (EB0 > 1 && BK5Cfg<Eng, Q, EB0, F, BK_LAYOUT_TU, false, 1, DPAR>::SMEM > 232448)
+        return fit_eb5<Q, F, EB0 - 1, DPAR>();
     else
         return EB0;
 }
+
+// The direction-parallel even-odd shape (three thread groups, one direction
+// each, one shared code body: DPAR = 2) for the float-float engine where it
+// measured faster on GB300: q = 6 (EB 4), 7 (EB 2), 8 and 9 (EB 1), 2-26 %
+// over one thread per line (q = 8: 31.5 against 24.9 GDoF/s).
+constexpr bool sweep_dpar5(int q) { return eng_is_ff() && q >= 6 && q <= 9; }
+constexpr int sweep_eb5_dpar(int q) { return q == 6 ? 4 : q == 7 ? 2 : 1; }
 
 template <int Q>
 int bk5_sweep_q(int F, int gd, const double* D, long long E, const void* u, const void* G, const void* mass,
@@ -150,8 +149,19 @@ int bk5_sweep_q(int F, int gd, const double* D, long long E, const void* u, cons
 {
     constexpr int L = BK_LAYOUT_TU;
     (void)gd;
-    if (F == 6) return bk5_q<Q, fit_eb5<Q, 6, sweep_eb5(Q)>(), 6, L, false>(D, E, u, G, mass, lambda, v, s);
-    if (F == 9) return bk5_q<Q, fit_eb5<Q, 9, sweep_eb5(Q)>(), 9, L, false>(D, E, u, G, mass, lambda, v, s);
+    P5<typename Eng::C, Q> prm;
+    for (int i = 0; i < Q * Q; ++i) prm.D[i] = Eng::coef(D[i]);
+    // the even-odd contractions when D is centro-antisymmetric (GLL points);
+    // instantiated for the symmetric 6-factor G only
+    const bool eo = (F == 6) && make_eo<typename Eng::C, Q>(D, false, prm.eo, &Eng::coef) &&
+                    make_eo<typename Eng::C, Q>(D, true, prm.eot, &Eng::coef);
+    if (eo) {
+        constexpr int DP = sweep_dpar5(Q) ? 2 : 0;
+        constexpr int EB = fit_eb5<Q, 6, DP ? sweep_eb5_dpar(Q) : sweep_eb5(Q), DP>();
+        return bk5_launch<Q, EB, 6, L, true, DP>(prm, E, u, G, mass, lambda, v, s);
+    }
+    if (F == 6) return bk5_launch<Q, fit_eb5<Q, 6, sweep_eb5(Q)>(), 6, L, false, 0>(prm, E, u, G, mass, lambda, v, s);
+    if (F == 9) return bk5_launch<Q, fit_eb5<Q, 9, sweep_eb5(Q)>(), 9, L, false, 0>(prm, E, u, G, mass, lambda, v, s);
     return BK_ERR_PREC;
 }
 #endif  // BK_OP_TU == 5
@@ -216,26 +226,41 @@ int bk1_q(const double* B, long long E, const void* jxw, const void* u, void* v,
 #endif  // BK_OP_TU == 1
 
 #if BK_OP_TU == 3
+template <int Q, int EB, bool EO, int DPAR>
+int bk3_launch(const P13<typename Eng::C, Q>& prm, long long E, const void* G, const void* k, const void* u, void* v,
+               cudaStream_t s)
+{
+    using Cfg = BK3Cfg<Eng, Q, EB, DPAR>;
+    using S = typename Eng::S;
+    static_assert(Cfg::SMEM <= 232448, "BK3 block exceeds the shared memory of an SM");
+    auto kern = bk3_kernel<Eng, Q, EB, EO, DPAR>;
+    const int occ = prepare<EoTag<Cfg, EO>>(kern, Cfg::SMEM, Cfg::NT);
+    if (occ <= 0) return BK_ERR_CUDA;
+    const int grid = grid_for((E + EB - 1) / EB, occ);
+    kern<<<grid, Cfg::NT, Cfg::SMEM, s>>>(prm, E, static_cast<const S*>(u), static_cast<const S*>(G),
+                                          static_cast<const S*>(k), static_cast<S*>(v), dev_ctx());
+    return cudaGetLastError() == cudaSuccess ? BK_OK : BK_ERR_CUDA;
+}
+
+// direction-parallel gradient stages for the float-float engine from q = 7
+// (one element per block)
+constexpr bool sweep_dpar3(int q) { return eng_is_ff() && q >= 7; }
+
 template <int Q, int EB>
 int bk3_q(const double* B, const double* D, long long E, const void* G, const void* k, const void* u, void* v,
           cudaStream_t s)
 {
-    using Cfg = BK3Cfg<Eng, Q, EB>;
-    using S = typename Eng::S;
-    static_assert(Cfg::SMEM <= 232448, "BK3 block exceeds the shared memory of an SM");
     P13<typename Eng::C, Q> prm;
     for (int i = 0; i < (Q - 1) * Q; ++i) prm.B[i] = Eng::coef(B[i]);
     for (int i = 0; i < Q * Q; ++i) prm.D[i] = Eng::coef(D[i]);
     // the even-odd contractions when B is centro-symmetric and D
     // centro-antisymmetric (GLL nodes, Gauss points)
     const bool eo = make_p13_eo<typename Eng::C, Q>(prm, B, D, &Eng::coef);
-    auto kern = eo ? bk3_kernel<Eng, Q, EB, true> : bk3_kernel<Eng, Q, EB, false>;
-    const int occ = eo ? prepare<EoTag<Cfg, true>>(kern, Cfg::SMEM, Cfg::NT) : prepare<Cfg>(kern, Cfg::SMEM, Cfg::NT);
-    if (occ <= 0) return BK_ERR_CUDA;
-    const int grid = grid_for((E + EB - 1) / EB, occ);
-    kern<<<grid, Cfg::NT, Cfg::SMEM, s>>>(prm, E, static_cast<const S*>(u), static_cast<const S*>(G),
-                                          static_cast<const S*>(k), static_cast<S*>(v), dev_ctx());
-    return cudaGetLastError() == cudaSuccess ? BK_OK : BK_ERR_CUDA;
+    if (eo) {
+        constexpr int DP = sweep_dpar3(Q) ? 2 : 0;
+        return bk3_launch<Q, DP ? 1 : EB, true, DP>(prm, E, G, k, u, v, s);
+    }
+    return bk3_launch<Q, EB, false, 0>(prm, E, G, k, u, v, s);
 }
 
 #endif  // BK_OP_TU == 3
@@ -252,8 +277,9 @@ int bk3adj_q(const double* B, const double* D, long long E, const void* G, const
     P13<typename Eng::C, Q> prm;
     for (int i = 0; i < (Q - 1) * Q; ++i) prm.B[i] = Eng::coef(B[i]);
     for (int i = 0; i < Q * Q; ++i) prm.D[i] = Eng::coef(D[i]);
-    auto kern = bk3_adjoint_kernel<Eng, Q, EB>;
-    const int occ = prepare<Cfg>(kern, Cfg::SMEM, Cfg::NT);
+    const bool eo = make_p13_eo<typename Eng::C, Q>(prm, B, D, &Eng::coef);
+    auto kern = eo ? bk3_adjoint_kernel<Eng, Q, EB, true> : bk3_adjoint_kernel<Eng, Q, EB, false>;
+    const int occ = eo ? prepare<EoTag<Cfg, true>>(kern, Cfg::SMEM, Cfg::NT) : prepare<Cfg>(kern, Cfg::SMEM, Cfg::NT);
     if (occ <= 0) return BK_ERR_CUDA;
     const int grid = grid_for((E + EB - 1) / EB, occ);
     kern<<<grid, Cfg::NT, Cfg::SMEM, s>>>(prm, E, static_cast<const S*>(u), static_cast<const S*>(res),

@@ -51,6 +51,26 @@ def test_adjoint_vs_host_gradient(bklib, p, engine):
     assert oracle.rel_maxdiff(host(dG), rG) < 1e-12
 
 
+@pytest.mark.parametrize("p", [2, 5])
+def test_adjoint_general_bases(bklib, p):
+    """Bases without the point symmetry (the plain sweeps, not the even-odd
+    ones) against the oracle's host gradient."""
+    from gpu_util import random_case
+    bk = bklib
+    E = 7
+    nq, B, D, g, u = random_case(3, p, E)
+    rng = np.random.default_rng(50 + p)
+    k = np.exp(rng.normal(0, 0.5, E * nq ** 3))
+    res = rng.uniform(-1, 1, E * (nq - 1) ** 3)
+    dk = torch.full((E * nq ** 3,), float("nan"), dtype=torch.float64, device="cuda")
+    dG = torch.full((E * 6 * nq ** 3,), float("nan"), dtype=torch.float64, device="cuda")
+    bk.bk3_adjoint(p, E, B, D, dev(g, "f64"), dev(k, "f64"), dev(u, "f64"), dev(res, "f64"), dk, dG)
+    torch.cuda.synchronize()
+    rk, rG = oracle.bk3_adjoint(nq, E, B, D, g, k, u, res)
+    assert oracle.rel_maxdiff(host(dk), rk) < 1e-12
+    assert oracle.rel_maxdiff(host(dG), rG) < 1e-12
+
+
 def test_adjoint_finite_differences_full(bklib):
     """Configuration: BK3 adjoint, FP64, p = 4 (P = 5, Q = 6), E = 65536."""
     bk = bklib
