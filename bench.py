@@ -194,10 +194,11 @@ def time_loop(fn, steps, warmup, world, stream, torch):
     return t0.elapsed_time(t1) / 1e3 / steps   # seconds per step
 
 
-def cpu_baseline_run(sample_E, reps):
+def cpu_baseline_run(sample_E, steps, warmup=1, best=True):
     """The oracle's restatement of the reference's BK5 kernel in double, OpenMP
-    over the host cores, on `sample_E` elements of the workload; min time over
-    `reps` (bk::time_min, include/bk_common.h:182-192)."""
+    over the host cores, on `sample_E` elements of the workload: `warmup`
+    untimed applies, then `steps` timed ones; the rate from the best
+    (bk::time_min, include/bk_common.h:182-192) or the mean time."""
     import numpy as np
 
     import oracle
@@ -207,14 +208,19 @@ def cpu_baseline_run(sample_E, reps):
     u = rng.uniform(-1, 1, sample_E * Q ** 3)
     G = rng.uniform(0.5, 1.5, sample_E * 6 * Q ** 3)
     oracle.lib(fast=True)
-    best = float("inf")
-    for _ in range(reps):
+    for _ in range(warmup):
+        oracle.bk5(Q, sample_E, D, G, u, fast=True)
+    times = []
+    for _ in range(steps):
         t = time.perf_counter()
         oracle.bk5(Q, sample_E, D, G, u, fast=True)
-        best = min(best, time.perf_counter() - t)
+        times.append(time.perf_counter() - t)
+    sec = min(times) if best else sum(times) / len(times)
     cores = os.cpu_count()
-    return {"value": sample_E * Q ** 3 / best / 1e9, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"BK5 p=7 FP64, {sample_E} of the {E_FULL} elements (random u, G), min of {reps} applies, "
+    how = f"min of {steps} applies" if best else f"mean of {steps} applies after {warmup} warm-up"
+    return {"value": sample_E * Q ** 3 / sec / 1e9, "unit": UNIT, "cores": cores, "kind": "port",
+            "ms_per_step": sec * 1e3,
+            "sample": f"BK5 p=7 FP64, {sample_E} of the {E_FULL} elements (random u, G), {how}, "
                       f"OMP over {cores} host threads (oracle/bk_oracle.c, -O3)"}
 
 
@@ -238,13 +244,17 @@ def measured_peak():
 
 
 def run_reference(args):
+    """The reference arm: the reference's BK5 p=7 FP64 kernel restated in C
+    (the oracle port; the reference's own build is CMake-only and does not
+    travel to the Arm machine) on the host cores, each step one apply of a
+    32768-element sample of the workload, `--warmup` untimed steps first."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    reps = max(1, min(args.steps, 5))
-    cb = cpu_baseline_run(32768, reps)
+    steps, warmup = max(1, args.steps), max(0, args.warmup)
+    cb = cpu_baseline_run(32768, steps, warmup, best=False)
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
-            "steps": reps, "warmup": 0, "ms_per_step": 32768 * 512 / cb["value"] / 1e6, "higher_is_better": True,
+            "steps": steps, "warmup": warmup, "ms_per_step": cb["ms_per_step"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": "BK5 p=7 FP64 apply, E=262144 (134M DoFs), CPU sample of 32768 elements",
                        "p": P_ORDER, "elements": E_FULL},
@@ -550,7 +560,7 @@ def main():
 
     # end to end through the C ABI on HOST arrays (bk5_apply_host): pinned
     # host u -> device -> apply -> pinned host v every step, the elements cut
-    # into 8 chunks whose copies in and out (two copy streams) overlap the
+    # into 16 chunks whose copies in and out (two copy streams) overlap the
     # applies of the neighbouring chunks
     if not args.no_e2e:
         uh = torch.empty(u.numel(), dtype=u.dtype, pin_memory=True)
@@ -569,7 +579,7 @@ def main():
                       "d2h_bytes_per_step": u.element_size() * dofs, "ms_per_step": te * 1e3,
                       "max_abs_diff_vs_device_apply": e2e_err,
                       "note": "bk5_apply_host: G (6.4 GB) resident on the device; u in, v out every step "
-                              "from/to pinned host memory in 8 element chunks, copies overlapping the applies"}
+                              "from/to pinned host memory in 16 element chunks, copies overlapping the applies"}
 
     # the forms side by side, with their error against the FP64 result
     if not args.no_forms and rank == 0 and prec == bk.PREC_FP64:

@@ -5,8 +5,8 @@
  * openmp/bk3_sumfact.h:17-24, openmp/BK5.cpp:18-24 with the `map` clauses of
  * openmp/offload/bk5_offload.cpp).  The operator data (qdata or G, and k)
  * stay resident on the device; u comes from host memory and v goes back to
- * host memory in element chunks: chunk c's copy in, chunk c-1's apply and
- * chunk c-2's copy out run at the same time on two copy streams and the
+ * host memory in element chunks: chunk c+1's copy in, chunk c's apply and
+ * chunk c-1's copy out run at the same time on two copy streams and the
  * caller's stream.  Host arrays should be pinned (cudaHostAlloc or
  * cudaHostRegister) for the copies to overlap; pageable memory works but
  * copies synchronously.  Return values are bk_status codes (bk_gpu.h). */
@@ -22,10 +22,10 @@ extern "C" {
 typedef struct bk_host_plan* bk_host_plan_t;
 
 /* A plan for operator `op` (1, 3 or 5) at order p over E elements with
- * storage precision prec: three device slots of chunk_elems elements each
- * for u and for v (chunk_elems 0: E / 8 rounded up, at least 1), two copy
- * streams and their events, on the current device.  The applies allocate
- * nothing. */
+ * storage precision prec: device buffers for u and v (E elements each), two
+ * copy streams and one event per chunk, on the current device; chunks of
+ * chunk_elems elements (0: E / 16 rounded up; at most 64 chunks; rounded up
+ * to keep chunk offsets 16-byte aligned).  The applies allocate nothing. */
 int bk_host_plan_create(bk_host_plan_t* plan, int op, int p, int64_t E, int prec, int64_t chunk_elems);
 int bk_host_plan_destroy(bk_host_plan_t plan);
 

@@ -16,7 +16,9 @@
 
 namespace bkg {
 
-template <class Eng, int Q, int EB>
+// DPAR != 0: the three gradient sweeps of each field run at the same time on
+// three thread groups (one shared code body), with a seventh work box.
+template <class Eng, int Q, int EB, int DPAR = 0>
 struct BK3AdjCfg {
     using S = typename Eng::S;
     using V = typename Eng::V;
@@ -24,29 +26,45 @@ struct BK3AdjCfg {
     static constexpr int P = Q - 1;
     static constexpr int Q3 = Q * Q * Q;
     static constexpr int P3 = P * P * P;
-    static constexpr int NT = ((EB * Q * Q + 31) / 32) * 32 < 64 ? 64 : ((EB * Q * Q + 31) / 32) * 32;
+    static constexpr int LINES = ((EB * Q * Q + 31) / 32) * 32;
+    static constexpr int NT = DPAR ? 3 * LINES : (LINES < 64 ? 64 : LINES);
+    static constexpr int NBOX = DPAR ? 7 : 6;
     static constexpr int U_BYTES = stage_bytes<S>(EB * P3);
     static constexpr int G_BYTES = stage_bytes<S>(EB * 6 * Q3);
     static constexpr int K_BYTES = stage_bytes<S>(EB * Q3);
-    static constexpr int W_BYTES = 6 * EB * WB::size * int(sizeof(V));
+    static constexpr int W_BYTES = NBOX * EB * WB::size * int(sizeof(V));
     static constexpr int SMEM = 2 * U_BYTES + G_BYTES + K_BYTES + W_BYTES + 16;
 };
 
 // u (P^3, dense S) -> gradient components at the Q^3 points in (gr, gs, gt);
-// tmp is a scratch box.  gt also serves as the interpolation target.  EO:
-// the even-odd contractions of prm.bi (interpolation, centro-symmetric) and
-// prm.dg (derivative, centro-antisymmetric).
-template <class Eng, class WB, int Q, bool EO>
+// tmp is a scratch box.  gt also serves as the interpolation target unless
+// DPAR.  EO: the even-odd contractions of prm.bi (interpolation,
+// centro-symmetric) and prm.dg (derivative, centro-antisymmetric).  DPAR:
+// the three derivative sweeps at once on three thread groups of `lines`
+// threads, reading the interpolant from tmp.
+template <class Eng, class WB, int Q, bool EO, int DPAR = 0>
 __device__ __forceinline__ void grad_at_points(const typename Eng::S* src, typename Eng::V* tmp, typename Eng::V* gr,
                                                typename Eng::V* gs, typename Eng::V* gt, int ne,
-                                               const P13<typename Eng::C, Q>& prm, int tid, int nt)
+                                               const P13<typename Eng::C, Q>& prm, int tid, int nt, int lines = 0)
 {
     constexpr int P = Q - 1;
     const Mat<typename Eng::C, Q, true> Bi{prm.B};   // interpolation: M(p, i) = B[i*Q + p]
     const Mat<typename Eng::C, Q, true> Dg{prm.D};   // derivative: q(p) = sum_n w(n) D(n, p)
     load_box<Eng, WB, P, P, P>(src, P * P * P, tmp, ne, tid, nt);
     __syncthreads();
-    if constexpr (EO) {
+    if constexpr (DPAR) {
+        static_assert(EO, "direction-parallel sweeps need the even-odd form");
+        sweep_eor<Eng, WB, 0, P, P, P, Q, +1>(tmp, gr, ne, prm.bi, tid, nt);   // (Q,P,P)
+        __syncthreads();
+        sweep_eor<Eng, WB, 1, Q, P, P, Q, +1>(gr, gs, ne, prm.bi, tid, nt);    // (Q,Q,P)
+        __syncthreads();
+        sweep_eor<Eng, WB, 2, Q, Q, P, Q, +1>(gs, tmp, ne, prm.bi, tid, nt);   // w at the points
+        __syncthreads();
+        const int grp = tid / lines;
+        if (grp < 3)
+            sweep_eo_dyn<Eng, WB, Q>(tmp, grp == 0 ? gr : (grp == 1 ? gs : gt), ne, prm.dg, tid - grp * lines, lines,
+                                     grp);
+    } else if constexpr (EO) {
         sweep_eor<Eng, WB, 0, P, P, P, Q, +1>(tmp, gr, ne, prm.bi, tid, nt);   // (Q,P,P)
         __syncthreads();
         sweep_eor<Eng, WB, 1, Q, P, P, Q, +1>(gr, tmp, ne, prm.bi, tid, nt);   // (Q,Q,P)
@@ -72,14 +90,14 @@ __device__ __forceinline__ void grad_at_points(const typename Eng::S* src, typen
     __syncthreads();
 }
 
-template <class Eng, int Q, int EB, bool EO = false>
-__global__ void __launch_bounds__(BK3AdjCfg<Eng, Q, EB>::NT)
+template <class Eng, int Q, int EB, bool EO = false, int DPAR = 0>
+__global__ void __launch_bounds__(BK3AdjCfg<Eng, Q, EB, DPAR>::NT)
     bk3_adjoint_kernel(const __grid_constant__ P13<typename Eng::C, Q> prm, const long long E,
                        const typename Eng::S* __restrict__ u, const typename Eng::S* __restrict__ res,
                        const typename Eng::S* __restrict__ G, const typename Eng::S* __restrict__ kq,
                        typename Eng::S* __restrict__ dk, typename Eng::S* __restrict__ dG, const DevCtx ctx)
 {
-    using Cfg = BK3AdjCfg<Eng, Q, EB>;
+    using Cfg = BK3AdjCfg<Eng, Q, EB, DPAR>;
     using S = typename Eng::S;
     using V = typename Eng::V;
     using A = typename Eng::A;
@@ -97,7 +115,8 @@ __global__ void __launch_bounds__(BK3AdjCfg<Eng, Q, EB>::NT)
     V* W3 = W2 + EB * WB::size;
     V* W4 = W3 + EB * WB::size;
     V* W5 = W4 + EB * WB::size;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(reinterpret_cast<unsigned char*>(W5 + EB * WB::size));
+    V* W6 = DPAR ? W5 + EB * WB::size : W0;   // the third component of g_res
+    uint64_t* bar = reinterpret_cast<uint64_t*>(reinterpret_cast<unsigned char*>(W0 + Cfg::NBOX * EB * WB::size));
     const int tid = threadIdx.x;
     const int nt = Cfg::NT;
 
@@ -119,16 +138,17 @@ __global__ void __launch_bounds__(BK3AdjCfg<Eng, Q, EB>::NT)
         const S* ks = stage_issue<S>(kstage, kq + e0 * Q3, ne * Q3, bar, tx, tid, nt);
         if (tid == 0) mbar_arrive_expect_tx(bar, tx);
         if (batch_wait_failed(bar, phase, ctx, tid)) return;
-        // g_u -> (W1, W2, W3) with W0 as scratch; g_res -> (W4, W5, W0) with W0 last
-        grad_at_points<Eng, WB, Q, EO>(us, W0, W1, W2, W3, ne, prm, tid, nt);
-        grad_at_points<Eng, WB, Q, EO>(rs, W0, W4, W5, W0, ne, prm, tid, nt);
+        // g_u -> (W1, W2, W3) with W0 as scratch; g_res -> (W4, W5, W6), W6 = W0
+        // (its last use) unless DPAR
+        grad_at_points<Eng, WB, Q, EO, DPAR>(us, W0, W1, W2, W3, ne, prm, tid, nt, Cfg::LINES);
+        grad_at_points<Eng, WB, Q, EO, DPAR>(rs, W0, W4, W5, W6, ne, prm, tid, nt, Cfg::LINES);
         for (int w = tid; w < ne * Q3; w += nt) {
             const int e = w / Q3;
             const int x = w - e * Q3;
             const int i = x / (Q * Q), j = (x / Q) % Q, k = x % Q;
             const int wi = e * WB::size + WB::at(i, j, k);
             const V ur = W1[wi], us_ = W2[wi], ut = W3[wi];
-            const V rr = W4[wi], rs_ = W5[wi], rt = W0[wi];
+            const V rr = W4[wi], rs_ = W5[wi], rt = W6[wi];
             const S* ge = gs + e * 6 * Q3 + x;   // factor-major
             const V g0 = Eng::load(ge[0]), g1 = Eng::load(ge[Q3]), g2 = Eng::load(ge[2 * Q3]);
             const V g3 = Eng::load(ge[3 * Q3]), g4 = Eng::load(ge[4 * Q3]), g5 = Eng::load(ge[5 * Q3]);

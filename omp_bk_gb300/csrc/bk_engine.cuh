@@ -33,6 +33,13 @@ struct EngDfma {
     __device__ static __forceinline__ V mul(V a, V b) { return a * b; }
     __device__ static __forceinline__ V vadd(V a, V b) { return a + b; }
     __device__ static __forceinline__ V vsub(V a, V b) { return a - b; }
+    __device__ static __forceinline__ V vadd_in(V a, V b) { return a + b; }
+    __device__ static __forceinline__ V vsub_in(V a, V b) { return a - b; }
+    __device__ static __forceinline__ void sum_diff(const A& a, const A& b, V& s, V& d)
+    {
+        s = a + b;
+        d = b - a;
+    }
     static C coef(double d) { return d; }
 };
 
@@ -52,6 +59,11 @@ struct EngFF {
     __device__ static __forceinline__ V mul(V a, V b) { return ff_mul(a, b); }
     __device__ static __forceinline__ V vadd(V a, V b) { return ff_add(a, b); }
     __device__ static __forceinline__ V vsub(V a, V b) { return ff_add(a, ff{-b.hi, -b.lo}); }
+    // operands of multiply-adds only: not renormalised
+    __device__ static __forceinline__ V vadd_in(V a, V b) { return ff_add_loose(a, b); }
+    __device__ static __forceinline__ V vsub_in(V a, V b) { return ff_add_loose(a, ff{-b.hi, -b.lo}); }
+    // a + b and b - a of two accumulators
+    __device__ static __forceinline__ void sum_diff(const A& a, const A& b, V& s, V& d) { acc_sum_diff(a, b, s, d); }
     static C coef(double d)
     {
         C c;
@@ -77,6 +89,13 @@ struct EngF32 {
     __device__ static __forceinline__ V mul(V a, V b) { return a * b; }
     __device__ static __forceinline__ V vadd(V a, V b) { return a + b; }
     __device__ static __forceinline__ V vsub(V a, V b) { return a - b; }
+    __device__ static __forceinline__ V vadd_in(V a, V b) { return a + b; }
+    __device__ static __forceinline__ V vsub_in(V a, V b) { return a - b; }
+    __device__ static __forceinline__ void sum_diff(const A& a, const A& b, V& s, V& d)
+    {
+        s = a + b;
+        d = b - a;
+    }
     static C coef(double d) { return static_cast<float>(d); }
 };
 

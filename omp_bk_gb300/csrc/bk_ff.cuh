@@ -116,6 +116,32 @@ __device__ __forceinline__ ff ff_mul(const ff a, const ff b)
     return r;
 }
 
+// a + b without the final renormalisation: hi = fl(a.hi + b.hi) and lo the
+// exact error of that sum plus the lo parts, so |lo| may reach a few ulp(hi).
+// For operands of multiply-adds, which use hi and lo separately (the sweeps'
+// even and odd combinations): 8 flops instead of 11.
+__device__ __forceinline__ ff ff_add_loose(const ff a, const ff b)
+{
+    float s, e;
+    two_sum(a.hi, b.hi, s, e);
+    return ff{s, __fadd_rn(e, __fadd_rn(a.lo, b.lo))};
+}
+
+// a + b and b - a from two compensated accumulators, each renormalised once
+// with TwoSum (safe after cancellation, where the compensation may exceed
+// the sum) instead of normalising a and b first and then adding them: 28
+// flops for the pair instead of 34.
+__device__ __forceinline__ void acc_sum_diff(const ffacc& a, const ffacc& b, ff& sum, ff& diff)
+{
+    float s, e, t, f;
+    two_sum(a.s, b.s, s, e);
+    two_sum(b.s, -a.s, t, f);
+    const float cs = __fadd_rn(e, __fadd_rn(a.c, b.c));
+    const float cd = __fadd_rn(f, __fsub_rn(b.c, a.c));
+    two_sum(s, cs, sum.hi, sum.lo);
+    two_sum(t, cd, diff.hi, diff.lo);
+}
+
 // a + b, both float-float, normalised (TwoSum of the hi parts, lo parts added).
 __device__ __forceinline__ ff ff_add(const ff a, const ff b)
 {

@@ -2,15 +2,16 @@
 //
 // The reference's kernels take host pointers and map `in` to the device and
 // `out` back on every call (openmp/offload/bk5_offload.cpp's `map` clauses).
-// Here the element range is cut into chunks and each chunk goes through
-// three stages on three streams: copy in (stream s_in), apply (the caller's
-// stream), copy out (stream s_out), chained by events.  Three device slots
-// per direction form a ring: chunk c uses slot c % 3, so chunk c's copy in
-// waits only for the apply of chunk c - 3 (the last reader of that u slot)
-// and chunk c's apply for the copy out of chunk c - 3 (the last reader of
-// that v slot).  The copy engines of both directions and the SMs then work
-// at the same time; the events persist in the plan, so consecutive calls
-// chain the same way.
+// Here the element range is cut into chunks, and a call is three passes over
+// them on three streams: every chunk's copy in (stream s_in), every chunk's
+// apply (the caller's stream, each after its own copy in), every chunk's
+// copy out (stream s_out, each after its own apply); the caller's stream
+// then waits for the last copy out, and the next call's copies wait for the
+// caller's stream (stream order).  Chunk c+1's copy in, chunk c's apply and
+// chunk c-1's copy out run at the same time.  u and v have device buffers of the full size:
+// with a ring of chunk slots the copies in had to wait for applies and, on
+// this part, the copy engines' queues then held the copies out behind them
+// (measured: the copies serialised, 15 ms per BK5 p=7 apply instead of 7.9).
 #include <cstdint>
 #include <cstring>
 
@@ -21,7 +22,7 @@
 
 namespace {
 
-constexpr int kSlots = 3;
+constexpr int kMaxChunks = 64;
 
 long long gcd_ll(long long a, long long b)
 {
@@ -52,11 +53,13 @@ long long align_elems(int vbytes, const long long* per_elem, int n)
 struct bk_host_plan {
     int op, p, prec, vbytes;
     long long E, chunk;
+    int nchunk;
     long long nin, nq;   // values per element of u/v and of one quadrature field
-    void* du[kSlots];
-    void* dv[kSlots];
+    void* du;
+    void* dv;
     cudaStream_t s_in, s_out;
-    cudaEvent_t ev_in[kSlots], ev_done[kSlots], ev_out[kSlots];
+    cudaEvent_t ev_start;
+    cudaEvent_t ev_in[kMaxChunks], ev_done[kMaxChunks], ev_out[kMaxChunks];
 };
 
 namespace {
@@ -72,35 +75,43 @@ int ck(cudaError_t e)
 template <class F>
 int run_chunks(bk_host_plan* h, const void* u_host, void* v_host, cudaStream_t s, F apply)
 {
+    if (h->E == 0) return BK_OK;
     const size_t eb = size_t(h->nin) * h->vbytes;   // bytes of u (and v) per element
     const char* uh = static_cast<const char*>(u_host);
     char* vh = static_cast<char*>(v_host);
-    int rc = BK_OK;
-    int last = -1;
-    for (long long e0 = 0, c = 0; e0 < h->E; e0 += h->chunk, ++c) {
+    char* du = static_cast<char*>(h->du);
+    char* dv = static_cast<char*>(h->dv);
+    int rc;
+    // stream order: the copies in start after the caller's earlier work on
+    // `s` (an earlier call included: its copies out may write the host
+    // array this call reads, and it still uses du and dv)
+    if ((rc = ck(cudaEventRecord(h->ev_start, s)))) return rc;
+    if ((rc = ck(cudaStreamWaitEvent(h->s_in, h->ev_start, 0)))) return rc;
+    for (int c = 0; c < h->nchunk; ++c) {
+        const long long e0 = c * h->chunk;
         const long long ne = (h->E - e0) < h->chunk ? (h->E - e0) : h->chunk;
-        const int k = int(c % kSlots);
-        const size_t bytes = size_t(ne) * eb;
-        // copy in, after the apply that last read this u slot
-        if ((rc = ck(cudaStreamWaitEvent(h->s_in, h->ev_done[k], 0)))) return rc;
-        if ((rc = ck(cudaMemcpyAsync(h->du[k], uh + size_t(e0) * eb, bytes, cudaMemcpyHostToDevice, h->s_in))))
-            return rc;
-        if ((rc = ck(cudaEventRecord(h->ev_in[k], h->s_in)))) return rc;
-        // apply, after the copy in and after the copy out that last read this v slot
-        if ((rc = ck(cudaStreamWaitEvent(s, h->ev_in[k], 0)))) return rc;
-        if ((rc = ck(cudaStreamWaitEvent(s, h->ev_out[k], 0)))) return rc;
-        if ((rc = apply(e0, ne, h->du[k], h->dv[k], s))) return rc;
-        if ((rc = ck(cudaEventRecord(h->ev_done[k], s)))) return rc;
-        // copy out
-        if ((rc = ck(cudaStreamWaitEvent(h->s_out, h->ev_done[k], 0)))) return rc;
-        if ((rc = ck(cudaMemcpyAsync(vh + size_t(e0) * eb, h->dv[k], bytes, cudaMemcpyDeviceToHost, h->s_out))))
-            return rc;
-        if ((rc = ck(cudaEventRecord(h->ev_out[k], h->s_out)))) return rc;
-        last = k;
+        const size_t off = size_t(e0) * eb, bytes = size_t(ne) * eb;
+        if ((rc = ck(cudaMemcpyAsync(du + off, uh + off, bytes, cudaMemcpyHostToDevice, h->s_in)))) return rc;
+        if ((rc = ck(cudaEventRecord(h->ev_in[c], h->s_in)))) return rc;
+    }
+    for (int c = 0; c < h->nchunk; ++c) {
+        const long long e0 = c * h->chunk;
+        const long long ne = (h->E - e0) < h->chunk ? (h->E - e0) : h->chunk;
+        const size_t off = size_t(e0) * eb;
+        if ((rc = ck(cudaStreamWaitEvent(s, h->ev_in[c], 0)))) return rc;
+        if ((rc = apply(e0, ne, du + off, dv + off, s))) return rc;
+        if ((rc = ck(cudaEventRecord(h->ev_done[c], s)))) return rc;
+    }
+    for (int c = 0; c < h->nchunk; ++c) {
+        const long long e0 = c * h->chunk;
+        const long long ne = (h->E - e0) < h->chunk ? (h->E - e0) : h->chunk;
+        const size_t off = size_t(e0) * eb, bytes = size_t(ne) * eb;
+        if ((rc = ck(cudaStreamWaitEvent(h->s_out, h->ev_done[c], 0)))) return rc;
+        if ((rc = ck(cudaMemcpyAsync(vh + off, dv + off, bytes, cudaMemcpyDeviceToHost, h->s_out)))) return rc;
+        if ((rc = ck(cudaEventRecord(h->ev_out[c], h->s_out)))) return rc;
     }
     // the caller's stream completes after the last copy out
-    if (last >= 0) rc = ck(cudaStreamWaitEvent(s, h->ev_out[last], 0));
-    return rc;
+    return ck(cudaStreamWaitEvent(s, h->ev_out[h->nchunk - 1], 0));
 }
 
 int check_plan(const bk_host_plan* h, int op, const void* u_host, void* v_host, const bk_options* opt)
@@ -138,16 +149,18 @@ int bk_host_plan_create(bk_host_plan_t* out, int op, int p, int64_t E, int prec,
     // u/v, qdata or G (up to 9 factors for BK5), k
     const long long per[4] = {h->nin, h->nq, 6 * h->nq, 9 * h->nq};
     const long long m = align_elems(h->vbytes, per, 4);
-    long long c = chunk_elems > 0 ? chunk_elems : (E + 7) / 8;
+    long long c = chunk_elems > 0 ? chunk_elems : (E + 15) / 16;
     if (c < 1) c = 1;
+    if ((E + c - 1) / c > kMaxChunks) c = (E + kMaxChunks - 1) / kMaxChunks;
     c = (c + m - 1) / m * m;
     h->chunk = c;
-    const size_t slot = size_t(c) * size_t(h->nin) * h->vbytes;
-    int rc = BK_OK;
-    for (int k = 0; k < kSlots && rc == BK_OK; ++k) {
-        rc = ck(cudaMalloc(&h->du[k], slot));
-        if (rc == BK_OK) rc = ck(cudaMalloc(&h->dv[k], slot));
-        if (rc == BK_OK) rc = ck(cudaEventCreateWithFlags(&h->ev_in[k], cudaEventDisableTiming));
+    h->nchunk = int((E + c - 1) / c);
+    const size_t bytes = size_t(E > 0 ? E : 1) * size_t(h->nin) * h->vbytes;
+    int rc = ck(cudaMalloc(&h->du, bytes));
+    if (rc == BK_OK) rc = ck(cudaMalloc(&h->dv, bytes));
+    if (rc == BK_OK) rc = ck(cudaEventCreateWithFlags(&h->ev_start, cudaEventDisableTiming));
+    for (int k = 0; k < h->nchunk && rc == BK_OK; ++k) {
+        rc = ck(cudaEventCreateWithFlags(&h->ev_in[k], cudaEventDisableTiming));
         if (rc == BK_OK) rc = ck(cudaEventCreateWithFlags(&h->ev_done[k], cudaEventDisableTiming));
         if (rc == BK_OK) rc = ck(cudaEventCreateWithFlags(&h->ev_out[k], cudaEventDisableTiming));
     }
@@ -166,16 +179,15 @@ int bk_host_plan_destroy(bk_host_plan_t h)
     if (!h) return BK_OK;
     if (h->s_in) cudaStreamSynchronize(h->s_in);
     if (h->s_out) cudaStreamSynchronize(h->s_out);
-    for (int k = 0; k < kSlots; ++k) {
-        if (h->ev_in[k]) cudaEventSynchronize(h->ev_in[k]);
+    for (int k = 0; k < kMaxChunks; ++k) {
         if (h->ev_done[k]) cudaEventSynchronize(h->ev_done[k]);
-        if (h->ev_out[k]) cudaEventSynchronize(h->ev_out[k]);
-        cudaFree(h->du[k]);
-        cudaFree(h->dv[k]);
         if (h->ev_in[k]) cudaEventDestroy(h->ev_in[k]);
         if (h->ev_done[k]) cudaEventDestroy(h->ev_done[k]);
         if (h->ev_out[k]) cudaEventDestroy(h->ev_out[k]);
     }
+    if (h->ev_start) cudaEventDestroy(h->ev_start);
+    cudaFree(h->du);
+    cudaFree(h->dv);
     if (h->s_in) cudaStreamDestroy(h->s_in);
     if (h->s_out) cudaStreamDestroy(h->s_out);
     delete h;

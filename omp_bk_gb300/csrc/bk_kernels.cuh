@@ -212,8 +212,8 @@ __device__ __forceinline__ void sweep_eo(const typename Eng::V* in, typename Eng
         V ev[H > 0 ? H : 1], dv[H > 0 ? H : 1];
 #pragma unroll
         for (int n = 0; n < H; ++n) {
-            ev[n] = Eng::vadd(x[n], x[Q - 1 - n]);
-            dv[n] = Eng::vsub(x[n], x[Q - 1 - n]);
+            ev[n] = Eng::vadd_in(x[n], x[Q - 1 - n]);
+            dv[n] = Eng::vsub_in(x[n], x[Q - 1 - n]);
         }
 #pragma unroll
         for (int o = 0; o < H; ++o) {
@@ -224,9 +224,10 @@ __device__ __forceinline__ void sweep_eo(const typename Eng::V* in, typename Eng
                 Eng::madd(bb, m.B[o * H + n], dv[n]);
             }
             if (Q & 1) Eng::madd(aa, m.c[o], x[H]);
-            const V av = Eng::result(aa), bv = Eng::result(bb);
-            out[base + o * SD] = Eng::vadd(bv, av);
-            out[base + (Q - 1 - o) * SD] = Eng::vsub(bv, av);
+            V s, d;
+            Eng::sum_diff(aa, bb, s, d);   // a + b, b - a
+            out[base + o * SD] = s;
+            out[base + (Q - 1 - o) * SD] = d;
         }
         if (Q & 1) {
             A t = Eng::zero();
@@ -264,8 +265,8 @@ __device__ __forceinline__ void sweep_eo_dyn(const typename Eng::V* in, typename
         V ev[H > 0 ? H : 1], dv[H > 0 ? H : 1];
 #pragma unroll
         for (int n = 0; n < H; ++n) {
-            ev[n] = Eng::vadd(x[n], x[Q - 1 - n]);
-            dv[n] = Eng::vsub(x[n], x[Q - 1 - n]);
+            ev[n] = Eng::vadd_in(x[n], x[Q - 1 - n]);
+            dv[n] = Eng::vsub_in(x[n], x[Q - 1 - n]);
         }
 #pragma unroll
         for (int o = 0; o < H; ++o) {
@@ -276,9 +277,10 @@ __device__ __forceinline__ void sweep_eo_dyn(const typename Eng::V* in, typename
                 Eng::madd(bb, m.B[o * H + n], dv[n]);
             }
             if (Q & 1) Eng::madd(aa, m.c[o], x[H]);
-            const V av = Eng::result(aa), bv = Eng::result(bb);
-            po[o * SD] = Eng::vadd(bv, av);
-            po[(Q - 1 - o) * SD] = Eng::vsub(bv, av);
+            V s, d;
+            Eng::sum_diff(aa, bb, s, d);   // a + b, b - a
+            po[o * SD] = s;
+            po[(Q - 1 - o) * SD] = d;
         }
         if (Q & 1) {
             A t = Eng::zero();
@@ -362,8 +364,8 @@ __device__ __forceinline__ void sweep_eor(const typename Eng::V* in, typename En
         V ev[HI > 0 ? HI : 1], dv[HI > 0 ? HI : 1];
 #pragma unroll
         for (int n = 0; n < HI; ++n) {
-            ev[n] = Eng::vadd(x[n], x[NI - 1 - n]);
-            dv[n] = Eng::vsub(x[n], x[NI - 1 - n]);
+            ev[n] = Eng::vadd_in(x[n], x[NI - 1 - n]);
+            dv[n] = Eng::vsub_in(x[n], x[NI - 1 - n]);
         }
         V mid_out;
         if constexpr ((NO & 1) != 0) {
@@ -382,9 +384,14 @@ __device__ __forceinline__ void sweep_eor(const typename Eng::V* in, typename En
                 Eng::madd(bb, m.B[o * HI + n], dv[n]);
             }
             if constexpr ((NI & 1) != 0) Eng::madd(aa, m.c[o], x[HI]);
-            const V av = Eng::result(aa), bv = Eng::result(bb);
-            out[base + o * SD] = Eng::vadd(av, bv);
-            out[base + (NO - 1 - o) * SD] = SIGN > 0 ? Eng::vsub(av, bv) : Eng::vsub(bv, av);
+            V s, d;
+            if constexpr (SIGN > 0) {
+                Eng::sum_diff(bb, aa, s, d);   // b + a, a - b
+            } else {
+                Eng::sum_diff(aa, bb, s, d);   // a + b, b - a
+            }
+            out[base + o * SD] = s;
+            out[base + (NO - 1 - o) * SD] = d;
         }
         if constexpr ((NO & 1) != 0) out[base + HO * SD] = mid_out;
     }
@@ -477,6 +484,7 @@ inline bool make_p13_eo(P13<C, Q>& p, const double* B, const double* D, Conv con
 
 // ---- BK5 -----------------------------------------------------------------------
 
+// Index of factor f at point (i, j, k) within an element's G.
 template <class Eng, int Q, int F, int LAYOUT>
 __device__ __forceinline__ int g_index(int i, int j, int f, int k)
 {
@@ -787,7 +795,7 @@ struct BK1Cfg {
     static constexpr int SMEM = U_BYTES + J_BYTES + W_BYTES + 16;
 };
 
-template <class Eng, int Q, int EB>
+template <class Eng, int Q, int EB, bool EO = false>
 __global__ void __launch_bounds__(BK1Cfg<Eng, Q, EB>::NT)
     bk1_kernel(const __grid_constant__ P13<typename Eng::C, Q> prm, const long long E,
                const typename Eng::S* __restrict__ u, const typename Eng::S* __restrict__ jxw,
@@ -829,11 +837,19 @@ __global__ void __launch_bounds__(BK1Cfg<Eng, Q, EB>::NT)
         if (batch_wait_failed(bar, phase, ctx, tid)) return;
         load_box<Eng, WB, P, P, P>(us, P3, W0, ne, tid, nt);
         __syncthreads();
-        sweep<Eng, WB, 0, P, P, P, Q>(W0, W1, ne, Bi, tid, nt);   // (Q,P,P)
-        __syncthreads();
-        sweep<Eng, WB, 1, Q, P, P, Q>(W1, W0, ne, Bi, tid, nt);   // (Q,Q,P)
-        __syncthreads();
-        sweep<Eng, WB, 2, Q, Q, P, Q>(W0, W1, ne, Bi, tid, nt);   // (Q,Q,Q)
+        if constexpr (EO) {   // B centro-symmetric (GLL nodes, Gauss points)
+            sweep_eor<Eng, WB, 0, P, P, P, Q, +1>(W0, W1, ne, prm.bi, tid, nt);   // (Q,P,P)
+            __syncthreads();
+            sweep_eor<Eng, WB, 1, Q, P, P, Q, +1>(W1, W0, ne, prm.bi, tid, nt);   // (Q,Q,P)
+            __syncthreads();
+            sweep_eor<Eng, WB, 2, Q, Q, P, Q, +1>(W0, W1, ne, prm.bi, tid, nt);   // (Q,Q,Q)
+        } else {
+            sweep<Eng, WB, 0, P, P, P, Q>(W0, W1, ne, Bi, tid, nt);   // (Q,P,P)
+            __syncthreads();
+            sweep<Eng, WB, 1, Q, P, P, Q>(W1, W0, ne, Bi, tid, nt);   // (Q,Q,P)
+            __syncthreads();
+            sweep<Eng, WB, 2, Q, Q, P, Q>(W0, W1, ne, Bi, tid, nt);   // (Q,Q,Q)
+        }
         __syncthreads();
         for (int w = tid; w < ne * Q3; w += nt) {
             const int e = w / Q3;
@@ -843,11 +859,19 @@ __global__ void __launch_bounds__(BK1Cfg<Eng, Q, EB>::NT)
             W1[wi] = Eng::mul(W1[wi], Eng::load(js[e * Q3 + x]));
         }
         __syncthreads();
-        sweep<Eng, WB, 2, Q, Q, Q, P>(W1, W0, ne, Bb, tid, nt);   // (Q,Q,P)
-        __syncthreads();
-        sweep<Eng, WB, 1, Q, Q, P, P>(W0, W1, ne, Bb, tid, nt);   // (Q,P,P)
-        __syncthreads();
-        sweep<Eng, WB, 0, Q, P, P, P>(W1, W0, ne, Bb, tid, nt);   // (P,P,P)
+        if constexpr (EO) {
+            sweep_eor<Eng, WB, 2, Q, Q, Q, P, +1>(W1, W0, ne, prm.bb, tid, nt);   // (Q,Q,P)
+            __syncthreads();
+            sweep_eor<Eng, WB, 1, Q, Q, P, P, +1>(W0, W1, ne, prm.bb, tid, nt);   // (Q,P,P)
+            __syncthreads();
+            sweep_eor<Eng, WB, 0, Q, P, P, P, +1>(W1, W0, ne, prm.bb, tid, nt);   // (P,P,P)
+        } else {
+            sweep<Eng, WB, 2, Q, Q, Q, P>(W1, W0, ne, Bb, tid, nt);   // (Q,Q,P)
+            __syncthreads();
+            sweep<Eng, WB, 1, Q, Q, P, P>(W0, W1, ne, Bb, tid, nt);   // (Q,P,P)
+            __syncthreads();
+            sweep<Eng, WB, 0, Q, P, P, P>(W1, W0, ne, Bb, tid, nt);   // (P,P,P)
+        }
         __syncthreads();
         // padded box -> v (consecutive threads, consecutive values)
         store_box<Eng, WB, P, P, P>(W0, v + e0 * P3, P3, ne, tid, nt);

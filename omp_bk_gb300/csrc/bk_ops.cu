@@ -214,8 +214,12 @@ int bk1_q(const double* B, long long E, const void* jxw, const void* u, void* v,
     P13<typename Eng::C, Q> prm;
     for (int i = 0; i < (Q - 1) * Q; ++i) prm.B[i] = Eng::coef(B[i]);
     for (int i = 0; i < Q * Q; ++i) prm.D[i] = Eng::coef(0.0);
-    auto kern = bk1_kernel<Eng, Q, EB>;
-    const int occ = prepare<Cfg>(kern, Cfg::SMEM, Cfg::NT);
+    // the even-odd interpolation when B is centro-symmetric (GLL nodes,
+    // Gauss points)
+    const bool eo = make_eor<typename Eng::C, Q, Q - 1>(B, Q, true, +1, prm.bi, &Eng::coef) &&
+                    make_eor<typename Eng::C, Q - 1, Q>(B, Q, false, +1, prm.bb, &Eng::coef);
+    auto kern = eo ? bk1_kernel<Eng, Q, EB, true> : bk1_kernel<Eng, Q, EB, false>;
+    const int occ = eo ? prepare<EoTag<Cfg, true>>(kern, Cfg::SMEM, Cfg::NT) : prepare<Cfg>(kern, Cfg::SMEM, Cfg::NT);
     if (occ <= 0) return BK_ERR_CUDA;
     const int grid = grid_for((E + EB - 1) / EB, occ);
     kern<<<grid, Cfg::NT, Cfg::SMEM, s>>>(prm, E, static_cast<const S*>(u), static_cast<const S*>(jxw),
@@ -268,26 +272,40 @@ int bk3_q(const double* B, const double* D, long long E, const void* G, const vo
 #endif  // BK_OP_TU == 3
 
 #if BK_OP_TU == 7
-template <int Q>
-int bk3adj_q(const double* B, const double* D, long long E, const void* G, const void* k, const void* u,
-             const void* res, void* dk, void* dG, cudaStream_t s)
+template <int Q, int EB, bool EO, int DPAR>
+int bk3adj_launch(const P13<typename Eng::C, Q>& prm, long long E, const void* G, const void* k, const void* u,
+                  const void* res, void* dk, void* dG, cudaStream_t s)
 {
-    constexpr int EB = default_eb(Q) / 2 > 0 ? default_eb(Q) / 2 : 1;
-    using Cfg = BK3AdjCfg<Eng, Q, EB>;
+    using Cfg = BK3AdjCfg<Eng, Q, EB, DPAR>;
     using S = typename Eng::S;
     static_assert(Cfg::SMEM <= 232448, "BK3 adjoint block exceeds the shared memory of an SM");
-    P13<typename Eng::C, Q> prm;
-    for (int i = 0; i < (Q - 1) * Q; ++i) prm.B[i] = Eng::coef(B[i]);
-    for (int i = 0; i < Q * Q; ++i) prm.D[i] = Eng::coef(D[i]);
-    const bool eo = make_p13_eo<typename Eng::C, Q>(prm, B, D, &Eng::coef);
-    auto kern = eo ? bk3_adjoint_kernel<Eng, Q, EB, true> : bk3_adjoint_kernel<Eng, Q, EB, false>;
-    const int occ = eo ? prepare<EoTag<Cfg, true>>(kern, Cfg::SMEM, Cfg::NT) : prepare<Cfg>(kern, Cfg::SMEM, Cfg::NT);
+    auto kern = bk3_adjoint_kernel<Eng, Q, EB, EO, DPAR>;
+    const int occ = prepare<EoTag<Cfg, EO>>(kern, Cfg::SMEM, Cfg::NT);
     if (occ <= 0) return BK_ERR_CUDA;
     const int grid = grid_for((E + EB - 1) / EB, occ);
     kern<<<grid, Cfg::NT, Cfg::SMEM, s>>>(prm, E, static_cast<const S*>(u), static_cast<const S*>(res),
                                           static_cast<const S*>(G), static_cast<const S*>(k), static_cast<S*>(dk),
                                           static_cast<S*>(dG), dev_ctx());
     return cudaGetLastError() == cudaSuccess ? BK_OK : BK_ERR_CUDA;
+}
+
+// the direction-parallel gradient sweeps for the float-float engine
+constexpr bool adj_dpar(int q) { return eng_is_ff() && q >= 6 && q <= 9; }
+constexpr int adj_eb_dpar(int q) { return q <= 6 ? 2 : 1; }
+
+template <int Q>
+int bk3adj_q(const double* B, const double* D, long long E, const void* G, const void* k, const void* u,
+             const void* res, void* dk, void* dG, cudaStream_t s)
+{
+    constexpr int EB = default_eb(Q) / 2 > 0 ? default_eb(Q) / 2 : 1;
+    P13<typename Eng::C, Q> prm;
+    for (int i = 0; i < (Q - 1) * Q; ++i) prm.B[i] = Eng::coef(B[i]);
+    for (int i = 0; i < Q * Q; ++i) prm.D[i] = Eng::coef(D[i]);
+    if (make_p13_eo<typename Eng::C, Q>(prm, B, D, &Eng::coef)) {
+        constexpr int DP = adj_dpar(Q) ? 2 : 0;
+        return bk3adj_launch<Q, DP ? adj_eb_dpar(Q) : EB, true, DP>(prm, E, G, k, u, res, dk, dG, s);
+    }
+    return bk3adj_launch<Q, EB, false, 0>(prm, E, G, k, u, res, dk, dG, s);
 }
 #endif  // BK_OP_TU == 7
 

@@ -268,3 +268,29 @@ def test_bk3_gll_gauss_even_odd(bklib, p, engine, coef):
         tol = TOL32
     assert np.all(np.isfinite(out))
     assert oracle.rel_maxdiff(out, ref) < tol
+
+
+@pytest.mark.parametrize("p", P_ALL)
+@pytest.mark.parametrize("engine", ["dfma", "ff", "fp32", "mixed"])
+def test_bk1_gll_gauss_even_odd(bklib, p, engine):
+    """With GLL nodes and Gauss points (B centro-symmetric) BK1 takes the
+    even-odd interpolation sweeps; same operator as the oracle's sums."""
+    E = 10
+    B, _, _, _, _ = bklib.bk1_bk3_matrices(p)
+    nq = p + 2
+    rng = np.random.default_rng(300 + p)
+    u = rng.uniform(-1, 1, E * (nq - 1) ** 3)
+    jxw = rng.uniform(0.5, 1.5, E * nq ** 3)
+    if engine in ("dfma", "ff"):
+        eng = bklib.ENGINE_DFMA if engine == "dfma" else bklib.ENGINE_FF
+        out = gpu_apply(bklib, 1, p, E, B, None, jxw, u, bklib.PREC_FP64, engine=eng)
+        ref = oracle.bk1(nq, E, B, jxw, u)
+        tol = TOL64
+    else:
+        pr = bklib.PREC_FP32 if engine == "fp32" else bklib.PREC_MIXED
+        out = gpu_apply(bklib, 1, p, E, B, None, jxw, u, pr)
+        f = lambda a: a.astype(np.float32).astype(np.float64)
+        ref = oracle.bk1(nq, E, B, f(jxw), f(u))
+        tol = TOL32
+    assert np.all(np.isfinite(out))
+    assert oracle.rel_maxdiff(out, ref) < tol
