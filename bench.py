@@ -76,14 +76,19 @@ def parse():
 
 # ---- distributed plumbing -------------------------------------------------------
 
-def dist_setup(n):
+def dist_setup(n, backend="nccl"):
+    """Rank, world size and local rank from the torchrun environment; the
+    process group (NCCL between GPUs; gloo for the CPU tests) when world > 1.
+    The apply has no exchange step: ranks only meet in the timing barrier and
+    the max-over-ranks reduction (replicas)."""
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
         import torch.distributed as dist
         os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
-        dist.init_process_group("nccl")
+        if not dist.is_initialized():
+            dist.init_process_group(backend)
     return rank, world, local
 
 
@@ -94,11 +99,13 @@ def barrier(world):
 
 
 def max_over_ranks(x, world):
+    """The largest of the ranks' values (the slowest rank's time)."""
     if world == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
