@@ -281,31 +281,62 @@ __global__ void __launch_bounds__(NT, MINB)
         fence_mbar_init();
     }
     __syncthreads();
-    uint32_t phase = 0;
     double dacc = 0.0;   // u . A u over the block's points (dot_part only)
     double* dp = dot_part != nullptr ? &dacc : nullptr;
+    // where the staged tile's u, G and mass landed
+    const S* us = nullptr;
+    const S* gs = nullptr;
+    const S* ms = nullptr;
+    // G of tile t (thread 0 adds its bytes to the phase without arriving),
+    // then u and the mass diagonal (thread 0 arrives): the next tile's G is
+    // copied while the current tile finishes its transposed sweeps, u and the
+    // mass (read by the last pass) right after
+    auto issue_g = [&](int t) {
+        const MultiTile tl = tiles[t];
+        const MultiSeg& sg = prm.seg[tl.seg];
+        const int q3 = sg.q * sg.q * sg.q;
+        uint32_t tx = 0;
+        if (tid == 0) fence_proxy_async();
+        gs = stage_issue<S>(gstage, G + sg.goff + tl.e_first * 6 * q3, tl.ne * 6 * q3, bar, tx, tid, nt);
+        if (tid == 0) mbar_expect_tx(bar, tx);
+    };
+    auto issue_um = [&](int t) {
+        const MultiTile tl = tiles[t];
+        const MultiSeg& sg = prm.seg[tl.seg];
+        const int q3 = sg.q * sg.q * sg.q;
+        uint32_t tx = 0;
+        if (tid == 0) fence_proxy_async();
+        us = stage_issue<S>(ustage, u + sg.uoff + tl.e_first * q3, tl.ne * q3, bar, tx, tid, nt);
+        ms = (mass != nullptr)
+                 ? stage_issue<S>(mstage, mass + sg.uoff + tl.e_first * q3, tl.ne * q3, bar, tx, tid, nt)
+                 : nullptr;
+        if (tid == 0) mbar_arrive_expect_tx(bar, tx);
+    };
+    if (blockIdx.x < ntiles) {
+        issue_g(blockIdx.x);
+        issue_um(blockIdx.x);
+    }
+    uint32_t phase = 0;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, phase ^= 1u) {
+        if (batch_wait_failed(bar, phase, ctx, tid)) return;
         const MultiTile tl = tiles[t];
         const MultiSeg& sg = prm.seg[tl.seg];
         const int q = sg.q;
         const int q3 = q * q * q;
-        uint32_t tx = 0;
-        if (tid == 0) fence_proxy_async();
-        const S* us = stage_issue<S>(ustage, u + sg.uoff + tl.e_first * q3, tl.ne * q3, bar, tx, tid, nt);
-        const S* gs = stage_issue<S>(gstage, G + sg.goff + tl.e_first * 6 * q3, tl.ne * 6 * q3, bar, tx, tid, nt);
-        // the mass term's diagonal, staged too: read in the last pass, where
-        // a global load per point would stall every warp on its latency
-        const S* mb = (mass != nullptr)
-                          ? stage_issue<S>(mstage, mass + sg.uoff + tl.e_first * q3, tl.ne * q3, bar, tx, tid, nt)
-                          : nullptr;
-        if (tid == 0) mbar_arrive_expect_tx(bar, tx);
-        if (batch_wait_failed(bar, phase, ctx, tid)) return;
+        const int tn = t + gridDim.x;
         S* vb = v + sg.uoff + tl.e_first * q3;
+        const S* ub = us;
+        const S* gb = gs;
+        const S* mb = ms;
+        auto early = [&]() {
+            if (tn < ntiles) issue_g(tn);
+        };
         switch (q) {
 #define BK_MULTI_EO_CASE(QQ)                                                                                    \
     case QQ:                                                                                                    \
         bk5_sweep_batch<Eng, QQ, 6, 2, true>(nullptr, prm.eo.template at<QQ>().eo, prm.eo.template at<QQ>().eot, \
-                                             us, gs, W0, W1, W2, nullptr, tl.ne, tid, nt, vb, mb, lambda, dp);  \
+                                             ub, gb, W0, W1, W2, nullptr, tl.ne, tid, nt, vb, mb, lambda, dp,   \
+                                             early);                                                           \
         break;
             BK_MULTI_EO_CASE(3)
             BK_MULTI_EO_CASE(4)
@@ -318,6 +349,7 @@ __global__ void __launch_bounds__(NT, MINB)
             default:
                 break;
         }
+        if (tn < ntiles) issue_um(tn);
     }
     if (dot_part != nullptr) {
         // block sum of the threads' partial dot products, one value per block

@@ -125,23 +125,53 @@ __global__ void __launch_bounds__(BK3AdjCfg<Eng, Q, EB, DPAR>::NT)
         fence_mbar_init();
     }
     __syncthreads();
-    uint32_t phase = 0;
     const long long nbatch = (E + EB - 1) / EB;
-    for (long long bt = blockIdx.x; bt < nbatch; bt += gridDim.x, phase ^= 1u) {
+    // The next batch's u and res are copied as soon as both gradients are
+    // formed (thread 0 adds their bytes to the phase without arriving), its
+    // G and k once the products have read the current ones (thread 0
+    // arrives): the copies overlap the products and the gradients.
+    const S* us = nullptr;
+    const S* rs = nullptr;
+    const S* gs = nullptr;
+    const S* ks = nullptr;
+    auto issue_ur = [&](long long bt, bool arrive) {
         const long long e0 = bt * EB;
         const int ne = int((E - e0) < EB ? (E - e0) : EB);
         uint32_t tx = 0;
         if (tid == 0) fence_proxy_async();
-        const S* us = stage_issue<S>(ustage, u + e0 * P3, ne * P3, bar, tx, tid, nt);
-        const S* rs = stage_issue<S>(rstage, res + e0 * P3, ne * P3, bar, tx, tid, nt);
-        const S* gs = stage_issue<S>(gstage, G + e0 * 6 * Q3, ne * 6 * Q3, bar, tx, tid, nt);
-        const S* ks = stage_issue<S>(kstage, kq + e0 * Q3, ne * Q3, bar, tx, tid, nt);
+        us = stage_issue<S>(ustage, u + e0 * P3, ne * P3, bar, tx, tid, nt);
+        rs = stage_issue<S>(rstage, res + e0 * P3, ne * P3, bar, tx, tid, nt);
+        if (tid == 0) {
+            if (arrive)
+                mbar_arrive_expect_tx(bar, tx);
+            else
+                mbar_expect_tx(bar, tx);
+        }
+    };
+    auto issue_gk = [&](long long bt) {
+        const long long e0 = bt * EB;
+        const int ne = int((E - e0) < EB ? (E - e0) : EB);
+        uint32_t tx = 0;
+        if (tid == 0) fence_proxy_async();
+        gs = stage_issue<S>(gstage, G + e0 * 6 * Q3, ne * 6 * Q3, bar, tx, tid, nt);
+        ks = stage_issue<S>(kstage, kq + e0 * Q3, ne * Q3, bar, tx, tid, nt);
         if (tid == 0) mbar_arrive_expect_tx(bar, tx);
+    };
+    if (blockIdx.x < nbatch) {
+        issue_ur(blockIdx.x, false);
+        issue_gk(blockIdx.x);
+    }
+    uint32_t phase = 0;
+    for (long long bt = blockIdx.x; bt < nbatch; bt += gridDim.x, phase ^= 1u) {
+        const long long e0 = bt * EB;
+        const int ne = int((E - e0) < EB ? (E - e0) : EB);
+        const long long next = bt + gridDim.x;
         if (batch_wait_failed(bar, phase, ctx, tid)) return;
         // g_u -> (W1, W2, W3) with W0 as scratch; g_res -> (W4, W5, W6), W6 = W0
         // (its last use) unless DPAR
         grad_at_points<Eng, WB, Q, EO, DPAR>(us, W0, W1, W2, W3, ne, prm, tid, nt, Cfg::LINES);
         grad_at_points<Eng, WB, Q, EO, DPAR>(rs, W0, W4, W5, W6, ne, prm, tid, nt, Cfg::LINES);
+        if (next < nbatch) issue_ur(next, false);   // u and res stages are free
         for (int w = tid; w < ne * Q3; w += nt) {
             const int e = w / Q3;
             const int x = w - e * Q3;
@@ -182,6 +212,7 @@ __global__ void __launch_bounds__(BK3AdjCfg<Eng, Q, EB, DPAR>::NT)
             go[5 * Q3] = Eng::store(prod(kt, ut));
         }
         __syncthreads();
+        if (next < nbatch) issue_gk(next);
     }
 }
 

@@ -495,12 +495,10 @@ __device__ __forceinline__ int g_index(int i, int j, int f, int k)
 
 // GD: G read from global memory in the pointwise stage (coalesced in every
 // layout: points are walked in G's own order) instead of staged by TMA, which
-// leaves the block's shared memory to u and the work boxes.  NBUF: stage
-// buffers (2: the block's next batch is copied while it computes the
-// current one).
+// leaves the block's shared memory to u and the work boxes.
 // DPAR != 0: three thread groups, one direction each (bk5_sweep_batch), and
 // a fourth work box.
-template <class Eng, int Q, int EB, int F, int LAYOUT, bool GD = false, int NBUF = 1, int DPAR = 0>
+template <class Eng, int Q, int EB, int F, int LAYOUT, bool GD = false, int DPAR = 0>
 struct BK5Cfg {
     using S = typename Eng::S;
     using V = typename Eng::V;
@@ -513,7 +511,7 @@ struct BK5Cfg {
     static constexpr int G_BYTES = GD ? 0 : stage_bytes<S>(EB * F * Q3);
     static constexpr int STAGE_BYTES = U_BYTES + G_BYTES;
     static constexpr int W_BYTES = NBOX * EB * WB::size * int(sizeof(V));
-    static constexpr int SMEM = NBUF * STAGE_BYTES + W_BYTES + 16 * NBUF;
+    static constexpr int SMEM = STAGE_BYTES + W_BYTES + 16;
 };
 
 // One batch of ne elements of order Q whose u (us, dense; shared or global
@@ -522,8 +520,10 @@ struct BK5Cfg {
 // when EO).  W0..W3: padded work boxes of at least ne elements (W3 only
 // when DPAR).  v is written at vb (global), the mass term read at mb (global
 // or shared, may be NULL) with u at us.  dot (optional): the thread's
-// running sum of u . v over its points (FP64).  Ends with a block barrier
-// (after which the stages may be reused).
+// running sum of u . v over its points (FP64).  after_pw: called by every
+// thread after the pointwise stage, when the G stage is no longer read (nor
+// u, unless the mass term or dot reads it at the end).  Ends with a block
+// barrier (after which the stages may be reused).
 //
 // DPAR (even-odd only): the three sweeps of a stage run at the same time on
 // three thread groups of nt/3 threads, one direction per group (warp-uniform
@@ -533,7 +533,11 @@ struct BK5Cfg {
 // one code body per direction (strides known at compile time); DPAR = 2: one
 // body for all three, the direction's strides in registers (a third of the
 // instruction footprint of the stage).
-template <class Eng, int Q, int F, int LAYOUT, bool EO, int DPAR = 0>
+struct NoOp {
+    __device__ __forceinline__ void operator()() const {}
+};
+
+template <class Eng, int Q, int F, int LAYOUT, bool EO, int DPAR = 0, class AfterPw = NoOp>
 __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restrict__ Dp,
                                                 const EOMat<typename Eng::C, Q>& eo,
                                                 const EOMat<typename Eng::C, Q>& eot, const typename Eng::S* us,
@@ -541,7 +545,7 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
                                                 typename Eng::V* W2, typename Eng::V* W3, int ne, int tid, int nt,
                                                 typename Eng::S* __restrict__ vb,
                                                 const typename Eng::S* __restrict__ mb, double lambda,
-                                                double* dot = nullptr)
+                                                double* dot = nullptr, AfterPw after_pw = AfterPw())
 {
     static_assert(!DPAR || EO, "direction-parallel sweeps need the even-odd form");
     using S = typename Eng::S;
@@ -614,6 +618,7 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
         QT[wi] = Eng::result(r2);
     }
     __syncthreads();
+    after_pw();   // the G stage (and u, without a mass term) is free from here
     // 5. transposed derivatives, in place: along i on W0, along j on W1 and
     //    (even-odd) along k on QT
     if constexpr (DPAR == 2) {
@@ -699,82 +704,68 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
     __syncthreads();
 }
 
-template <class Eng, int Q, int EB, int F, int LAYOUT, bool EO = false, bool GD = false, int NBUF = 1,
-          int DPAR = 0>
-__global__ void __launch_bounds__(BK5Cfg<Eng, Q, EB, F, LAYOUT, GD, NBUF, DPAR>::NT)
+// The block walks batches bt = blockIdx.x, + gridDim.x, ...  One stage buffer:
+// the next batch's u and G are copied into it as soon as the current batch
+// stops reading them (after the pointwise stage; after the last pass when a
+// mass term reads u there), so the copies overlap the transposed sweeps and
+// the last pass instead of stalling the block at the start of each batch.
+template <class Eng, int Q, int EB, int F, int LAYOUT, bool EO = false, bool GD = false, int DPAR = 0>
+__global__ void __launch_bounds__(BK5Cfg<Eng, Q, EB, F, LAYOUT, GD, DPAR>::NT)
     bk5_kernel(const __grid_constant__ P5<typename Eng::C, Q> prm, const long long E,
                const typename Eng::S* __restrict__ u, const typename Eng::S* __restrict__ G,
                const typename Eng::S* __restrict__ mass, const double lambda, typename Eng::S* __restrict__ v,
                const DevCtx ctx)
 {
-    static_assert(NBUF == 1 || NBUF == 2, "one or two stage buffers");
-    using Cfg = BK5Cfg<Eng, Q, EB, F, LAYOUT, GD, NBUF, DPAR>;
+    using Cfg = BK5Cfg<Eng, Q, EB, F, LAYOUT, GD, DPAR>;
     using S = typename Eng::S;
     using V = typename Eng::V;
     using WB = typename Cfg::WB;
     constexpr int Q3 = Cfg::Q3;
     extern __shared__ __align__(16) unsigned char smem[];
-    V* W0 = reinterpret_cast<V*>(smem + NBUF * Cfg::STAGE_BYTES);
+    V* W0 = reinterpret_cast<V*>(smem + Cfg::STAGE_BYTES);
     V* W1 = W0 + EB * WB::size;
     V* W2 = W1 + EB * WB::size;
     V* W3 = DPAR ? W2 + EB * WB::size : nullptr;
-    uint64_t* bars = reinterpret_cast<uint64_t*>(reinterpret_cast<unsigned char*>(W0 + Cfg::NBOX * EB * WB::size));
+    uint64_t* bar = reinterpret_cast<uint64_t*>(reinterpret_cast<unsigned char*>(W0 + Cfg::NBOX * EB * WB::size));
     const int tid = threadIdx.x;
     const int nt = Cfg::NT;
 
     if (tid == 0) {
-        for (int b = 0; b < NBUF; ++b) mbar_init(&bars[b], 1);
+        mbar_init(bar, 1);
         fence_mbar_init();
     }
     __syncthreads();
     const long long nbatch = (E + EB - 1) / EB;
-    // where the batch of each stage buffer landed
-    const S* us0 = nullptr;
-    const S* gs0 = nullptr;
-    const S* us1 = nullptr;
-    const S* gs1 = nullptr;
-    // 1. stage u and G of batch bt into buffer b
-    auto issue = [&](long long bt, int b) {
+    // where the staged batch's u and G landed
+    const S* us = nullptr;
+    const S* gs = nullptr;
+    // 1. stage u and G of batch bt (every thread; thread 0 issues the TMA
+    //    part and arrives)
+    auto issue = [&](long long bt) {
         const long long e0 = bt * EB;
         const int ne = int((E - e0) < EB ? (E - e0) : EB);
-        unsigned char* st = smem + b * Cfg::STAGE_BYTES;
         uint32_t tx = 0;
         if (tid == 0) fence_proxy_async();
-        const S* us = stage_issue<S>(st, u + e0 * Q3, ne * Q3, &bars[b], tx, tid, nt);
-        const S* gs = GD ? G + e0 * F * Q3
-                         : stage_issue<S>(st + Cfg::U_BYTES, G + e0 * F * Q3, ne * F * Q3, &bars[b], tx, tid, nt);
-        if (tid == 0) mbar_arrive_expect_tx(&bars[b], tx);
-        if (b == 0) {
-            us0 = us;
-            gs0 = gs;
-        } else {
-            us1 = us;
-            gs1 = gs;
-        }
+        us = stage_issue<S>(smem, u + e0 * Q3, ne * Q3, bar, tx, tid, nt);
+        gs = GD ? G + e0 * F * Q3 : stage_issue<S>(smem + Cfg::U_BYTES, G + e0 * F * Q3, ne * F * Q3, bar, tx, tid, nt);
+        if (tid == 0) mbar_arrive_expect_tx(bar, tx);
     };
-    if (NBUF == 2 && blockIdx.x < nbatch) issue(blockIdx.x, 0);
-    unsigned it = 0;
-    for (long long bt = blockIdx.x; bt < nbatch; bt += gridDim.x, ++it) {
-        const int b = (NBUF == 2) ? int(it & 1u) : 0;
-        const uint32_t parity = (NBUF == 2) ? ((it >> 1) & 1u) : (it & 1u);
-        bool next = false;
-        if (NBUF == 1) {
-            issue(bt, 0);
-        } else if (bt + gridDim.x < nbatch) {
-            // the other buffer was released by the previous batch's final barrier
-            issue(bt + gridDim.x, b ^ 1);
-            next = true;
-        }
-        if (batch_wait_failed(&bars[b], parity, ctx, tid)) {
-            // a copy into the other buffer may still be in flight: let it land
-            if (next) mbar_wait_bounded(&bars[b ^ 1], ((it + 1) >> 1) & 1u, ctx.wait_limit);
-            return;
-        }
+    if (blockIdx.x < nbatch) issue(blockIdx.x);
+    uint32_t phase = 0;
+    for (long long bt = blockIdx.x; bt < nbatch; bt += gridDim.x, phase ^= 1u) {
+        if (batch_wait_failed(bar, phase, ctx, tid)) return;
         const long long e0 = bt * EB;
         const int ne = int((E - e0) < EB ? (E - e0) : EB);
-        bk5_sweep_batch<Eng, Q, F, LAYOUT, EO, DPAR>(prm.D, prm.eo, prm.eot, b == 0 ? us0 : us1, b == 0 ? gs0 : gs1,
-                                                     W0, W1, W2, W3, ne, tid, nt, v + e0 * Q3,
-                                                     (mass != nullptr) ? mass + e0 * Q3 : nullptr, lambda);
+        const long long next = bt + gridDim.x;
+        const S* mb = (mass != nullptr) ? mass + e0 * Q3 : nullptr;
+        const S* ub = us;
+        const S* gb = gs;
+        auto early = [&]() {
+            if (mass == nullptr && next < nbatch) issue(next);
+        };
+        bk5_sweep_batch<Eng, Q, F, LAYOUT, EO, DPAR>(prm.D, prm.eo, prm.eot, ub, gb, W0, W1, W2, W3, ne, tid, nt,
+                                                     v + e0 * Q3, mb, lambda, nullptr, early);
+        if (mass != nullptr && next < nbatch) issue(next);
     }
 }
 
@@ -824,16 +815,25 @@ __global__ void __launch_bounds__(BK1Cfg<Eng, Q, EB>::NT)
         fence_mbar_init();
     }
     __syncthreads();
-    uint32_t phase = 0;
     const long long nbatch = (E + EB - 1) / EB;
-    for (long long bt = blockIdx.x; bt < nbatch; bt += gridDim.x, phase ^= 1u) {
+    // u and qdata of batch bt into the stage; the next batch is issued as
+    // soon as the pointwise stage has read it (copies overlap the sweeps back)
+    const S* us = nullptr;
+    const S* js = nullptr;
+    auto issue = [&](long long bt) {
         const long long e0 = bt * EB;
         const int ne = int((E - e0) < EB ? (E - e0) : EB);
         uint32_t tx = 0;
         if (tid == 0) fence_proxy_async();
-        const S* us = stage_issue<S>(ustage, u + e0 * P3, ne * P3, bar, tx, tid, nt);
-        const S* js = stage_issue<S>(jstage, jxw + e0 * Q3, ne * Q3, bar, tx, tid, nt);
+        us = stage_issue<S>(ustage, u + e0 * P3, ne * P3, bar, tx, tid, nt);
+        js = stage_issue<S>(jstage, jxw + e0 * Q3, ne * Q3, bar, tx, tid, nt);
         if (tid == 0) mbar_arrive_expect_tx(bar, tx);
+    };
+    if (blockIdx.x < nbatch) issue(blockIdx.x);
+    uint32_t phase = 0;
+    for (long long bt = blockIdx.x; bt < nbatch; bt += gridDim.x, phase ^= 1u) {
+        const long long e0 = bt * EB;
+        const int ne = int((E - e0) < EB ? (E - e0) : EB);
         if (batch_wait_failed(bar, phase, ctx, tid)) return;
         load_box<Eng, WB, P, P, P>(us, P3, W0, ne, tid, nt);
         __syncthreads();
@@ -859,6 +859,7 @@ __global__ void __launch_bounds__(BK1Cfg<Eng, Q, EB>::NT)
             W1[wi] = Eng::mul(W1[wi], Eng::load(js[e * Q3 + x]));
         }
         __syncthreads();
+        if (bt + gridDim.x < nbatch) issue(bt + gridDim.x);   // the stage is free
         if constexpr (EO) {
             sweep_eor<Eng, WB, 2, Q, Q, Q, P, +1>(W1, W0, ne, prm.bb, tid, nt);   // (Q,Q,P)
             __syncthreads();
@@ -935,17 +936,29 @@ __global__ void __launch_bounds__(BK3Cfg<Eng, Q, EB, DPAR>::NT)
         fence_mbar_init();
     }
     __syncthreads();
-    uint32_t phase = 0;
     const long long nbatch = (E + EB - 1) / EB;
-    for (long long bt = blockIdx.x; bt < nbatch; bt += gridDim.x, phase ^= 1u) {
+    // u, G and k of batch bt into the stage (every thread; thread 0 issues
+    // the TMA part and arrives).  The next batch is issued as soon as the
+    // pointwise stage has read the stage, so its copies overlap the
+    // transposed sweeps.
+    const S* us = nullptr;
+    const S* gs = nullptr;
+    const S* ks = nullptr;
+    auto issue = [&](long long bt) {
         const long long e0 = bt * EB;
         const int ne = int((E - e0) < EB ? (E - e0) : EB);
         uint32_t tx = 0;
         if (tid == 0) fence_proxy_async();
-        const S* us = stage_issue<S>(ustage, u + e0 * P3, ne * P3, bar, tx, tid, nt);
-        const S* gs = stage_issue<S>(gstage, G + e0 * 6 * Q3, ne * 6 * Q3, bar, tx, tid, nt);
-        const S* ks = (kq != nullptr) ? stage_issue<S>(kstage, kq + e0 * Q3, ne * Q3, bar, tx, tid, nt) : nullptr;
+        us = stage_issue<S>(ustage, u + e0 * P3, ne * P3, bar, tx, tid, nt);
+        gs = stage_issue<S>(gstage, G + e0 * 6 * Q3, ne * 6 * Q3, bar, tx, tid, nt);
+        ks = (kq != nullptr) ? stage_issue<S>(kstage, kq + e0 * Q3, ne * Q3, bar, tx, tid, nt) : nullptr;
         if (tid == 0) mbar_arrive_expect_tx(bar, tx);
+    };
+    if (blockIdx.x < nbatch) issue(blockIdx.x);
+    uint32_t phase = 0;
+    for (long long bt = blockIdx.x; bt < nbatch; bt += gridDim.x, phase ^= 1u) {
+        const long long e0 = bt * EB;
+        const int ne = int((E - e0) < EB ? (E - e0) : EB);
         if (batch_wait_failed(bar, phase, ctx, tid)) return;
         load_box<Eng, WB, P, P, P>(us, P3, W0, ne, tid, nt);
         __syncthreads();
@@ -1002,6 +1015,7 @@ __global__ void __launch_bounds__(BK3Cfg<Eng, Q, EB, DPAR>::NT)
             W3[wi] = Eng::result(r2);
         }
         __syncthreads();
+        if (bt + gridDim.x < nbatch) issue(bt + gridDim.x);   // the stage is free
         if constexpr (DPAR) {
             const int grp = tid / Cfg::LINES;
             if (grp < 3) {

@@ -107,17 +107,15 @@ int grid_for(long long nbatch, int occ)
 }
 
 #if BK_OP_TU == 5
-// One launch of bk5_kernel with the given shape.  One stage buffer: double
-// buffering (NBUF = 2) measured no faster than the overlap of the blocks
-// resident on an SM, which one buffer keeps more of.
+// One launch of bk5_kernel with the given shape.
 template <int Q, int EB, int F, int LAYOUT, bool EO, int DPAR>
 int bk5_launch(const P5<typename Eng::C, Q>& prm, long long E, const void* u, const void* G, const void* mass,
                double lambda, void* v, cudaStream_t s)
 {
-    using Cfg = BK5Cfg<Eng, Q, EB, F, LAYOUT, false, 1, DPAR>;
+    using Cfg = BK5Cfg<Eng, Q, EB, F, LAYOUT, false, DPAR>;
     using S = typename Eng::S;
     static_assert(Cfg::SMEM <= 232448, "BK5 block exceeds the shared memory of an SM");
-    auto kern = bk5_kernel<Eng, Q, EB, F, LAYOUT, EO, false, 1, DPAR>;
+    auto kern = bk5_kernel<Eng, Q, EB, F, LAYOUT, EO, false, DPAR>;
     const int occ = prepare<EoTag<Cfg, EO>>(kern, Cfg::SMEM, Cfg::NT);
     if (occ <= 0) return BK_ERR_CUDA;
     const int grid = grid_for((E + EB - 1) / EB, occ);
@@ -130,7 +128,7 @@ int bk5_launch(const P5<typename Eng::C, Q>& prm, long long E, const void* u, co
 template <int Q, int F, int EB0, int DPAR = 0>
 constexpr int fit_eb5()
 {
-    if constexpr (EB0 > 1 && BK5Cfg<Eng, Q, EB0, F, BK_LAYOUT_TU, false, 1, DPAR>::SMEM > 232448)
+    if constexpr (EB0 > 1 && BK5Cfg<Eng, Q, EB0, F, BK_LAYOUT_TU, false, DPAR>::SMEM > 232448)
         return fit_eb5<Q, F, EB0 - 1, DPAR>();
     else
         return EB0;
