@@ -256,7 +256,9 @@ inline void multi_eo_smem(const MultiSeg* seg, int nseg, int& u_bytes, int& g_by
     total = 2 * u_bytes + g_bytes + 3 * w_bytes + 16;
 }
 
-template <class Eng, int NT, int MINB>
+// DOT: also sum u . v over the launch, one partial per block in dot_part
+// (the CG's p . A p), from compensated per-thread sums.
+template <class Eng, int NT, int MINB, bool DOT = false>
 __global__ void __launch_bounds__(NT, MINB)
     bk5_multi_eo_kernel(const __grid_constant__ PMultiEO<typename Eng::C> prm, const MultiTile* __restrict__ tiles,
                         const int ntiles, const typename Eng::S* __restrict__ u, const typename Eng::S* __restrict__ G,
@@ -281,8 +283,7 @@ __global__ void __launch_bounds__(NT, MINB)
         fence_mbar_init();
     }
     __syncthreads();
-    double dacc = 0.0;   // u . A u over the block's points (dot_part only)
-    double* dp = dot_part != nullptr ? &dacc : nullptr;
+    ffacc dacc = acc_zero();   // u . A u over the thread's points (DOT)
     // where the staged tile's u, G and mass landed
     const S* us = nullptr;
     const S* gs = nullptr;
@@ -334,9 +335,9 @@ __global__ void __launch_bounds__(NT, MINB)
         switch (q) {
 #define BK_MULTI_EO_CASE(QQ)                                                                                    \
     case QQ:                                                                                                    \
-        bk5_sweep_batch<Eng, QQ, 6, 2, true>(nullptr, prm.eo.template at<QQ>().eo, prm.eo.template at<QQ>().eot, \
-                                             ub, gb, W0, W1, W2, nullptr, tl.ne, tid, nt, vb, mb, lambda, dp,   \
-                                             early);                                                           \
+        bk5_sweep_batch<Eng, QQ, 6, 2, true, 0, decltype(early), DOT>(                                         \
+            nullptr, prm.eo.template at<QQ>().eo, prm.eo.template at<QQ>().eot, ub, gb, W0, W1, W2, nullptr,    \
+            tl.ne, tid, nt, vb, mb, lambda, &dacc, early);                                                      \
         break;
             BK_MULTI_EO_CASE(3)
             BK_MULTI_EO_CASE(4)
@@ -351,12 +352,12 @@ __global__ void __launch_bounds__(NT, MINB)
         }
         if (tn < ntiles) issue_um(tn);
     }
-    if (dot_part != nullptr) {
+    if constexpr (DOT) {
         // block sum of the threads' partial dot products, one value per block
         // (the work boxes are free after the last tile; no static shared
         // memory, which would shrink the dynamic limit)
         double* wsum = reinterpret_cast<double*>(W0);
-        double s = dacc;
+        double s = double(dacc.s) + double(dacc.c);
         for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
         if ((tid & 31) == 0) wsum[tid >> 5] = s;
         __syncthreads();

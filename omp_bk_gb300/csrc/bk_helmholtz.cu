@@ -100,7 +100,7 @@ struct MultiLaunch {
 // The even-odd sweep launch: blockDim = the largest tile's lines (eb q^2),
 // rounded up to whole warps; MAXT threads at most, MINB blocks per SM asked
 // of the register allocator.
-template <class Eng, int MAXT, int MINB>
+template <class Eng, int MAXT, int MINB, bool DOT = false>
 struct MultiEOLaunch {
     static int threads(const MultiSeg* seg, int nseg)
     {
@@ -119,7 +119,7 @@ struct MultiEOLaunch {
     }
     static int prepare(int total, int nt)
     {
-        auto kern = bk5_multi_eo_kernel<Eng, MAXT, MINB>;
+        auto kern = bk5_multi_eo_kernel<Eng, MAXT, MINB, DOT>;
         static int set[kMaxDevices] = {0};
         static int occ_of[kMaxDevices][3] = {{0, 0, 0}};
         const int dev = current_device();
@@ -161,7 +161,8 @@ struct MultiEOLaunch {
         const int total = smem(prm, ub, gb, wb);
         const int nt = threads(prm.seg, prm.nseg);
         if (total > 232448 || nt > MAXT) return BK_ERR_ARG;
-        auto kern = bk5_multi_eo_kernel<Eng, MAXT, MINB>;
+        if (DOT != (dot_part != nullptr)) return BK_ERR_ARG;
+        auto kern = bk5_multi_eo_kernel<Eng, MAXT, MINB, DOT>;
         const int occ = prepare(total, nt);
         if (occ < 1) return BK_ERR_CUDA;
         int grid = occ * sm_count();
@@ -484,9 +485,9 @@ int apply_plan(bk_hplan* h, int eng, const void* G, const void* mass, double lam
         switch (eng) {
             case 0: return MultiEOLaunch<EngDfma, 256, 2>::run(h->e_dfma, h->tiles, h->ntiles, u, G, mass, lambda, v, s);
             case 1: return MultiEOLaunch<EngFF, 256, 2>::run(h->e_ff, h->tiles, h->ntiles, u, G, mass, lambda, v, s);
-            case 2: return MultiEOLaunch<EngF32, 256, 2>::run(h->e_f32, h->tiles, h->ntiles, u, G, mass, lambda, v, s);
+            case 2: return MultiEOLaunch<EngF32, 256, 4>::run(h->e_f32, h->tiles, h->ntiles, u, G, mass, lambda, v, s);
             default:
-                return MultiEOLaunch<EngMixed, 256, 2>::run(h->e_f32, h->tiles, h->ntiles, u, G, mass, lambda, v, s);
+                return MultiEOLaunch<EngMixed, 256, 4>::run(h->e_f32, h->tiles, h->ntiles, u, G, mass, lambda, v, s);
         }
     }
     switch (eng) {
@@ -516,7 +517,7 @@ int build_inner_graph(bk_hplan* h, const void* G32, const void* mass32, double l
         // kernel attributes and occupancy outside the capture
         int st = 0, cb = 0;
         if (h->kernel == BK_KERNEL_SWEEP) {
-            if (MultiEOLaunch<EngMixed, 256, 2>::prepare(h->e_f32) < 1) return BK_ERR_CUDA;
+            if (MultiEOLaunch<EngMixed, 256, 4, true>::prepare(h->e_f32) < 1) return BK_ERR_CUDA;
         } else if (MultiLaunch<EngMixed, 2>::prepare(MultiLaunch<EngMixed, 2>::smem(h->p_f32, st, cb)) < 1) {
             return BK_ERR_CUDA;
         }
@@ -588,7 +589,7 @@ int build_inner_graph(bk_hplan* h, const void* G32, const void* mass32, double l
                 if (h->kernel == BK_KERNEL_SWEEP) {
                     // p . Ap summed by the apply itself (one partial per block)
                     int nparts = 0;
-                    arc = MultiEOLaunch<EngMixed, 256, 2>::run(h->e_f32, h->tiles, h->ntiles, h->p32, G32, mass32,
+                    arc = MultiEOLaunch<EngMixed, 256, 4, true>::run(h->e_f32, h->tiles, h->ntiles, h->p32, G32, mass32,
                                                                 lambda, h->Ap32, s, h->part, &nparts);
                     cg_pap_kernel<<<1, kRedThreads, 0, s>>>(h->part, nparts, h->sc);
                 } else {

@@ -519,8 +519,9 @@ struct BK5Cfg {
 // D(i, n) in parameter space; eo, eot: the even-odd forms of D and D^T (used
 // when EO).  W0..W3: padded work boxes of at least ne elements (W3 only
 // when DPAR).  v is written at vb (global), the mass term read at mb (global
-// or shared, may be NULL) with u at us.  dot (optional): the thread's
-// running sum of u . v over its points (FP64).  after_pw: called by every
+// or shared, may be NULL) with u at us.  DOT (FP32 storage): the thread's
+// running sum of u . v over its points in *dot, each product exact (FMA) and
+// the sum compensated (float-float: about 44 bits).  after_pw: called by every
 // thread after the pointwise stage, when the G stage is no longer read (nor
 // u, unless the mass term or dot reads it at the end).  Ends with a block
 // barrier (after which the stages may be reused).
@@ -537,7 +538,7 @@ struct NoOp {
     __device__ __forceinline__ void operator()() const {}
 };
 
-template <class Eng, int Q, int F, int LAYOUT, bool EO, int DPAR = 0, class AfterPw = NoOp>
+template <class Eng, int Q, int F, int LAYOUT, bool EO, int DPAR = 0, class AfterPw = NoOp, bool DOT = false>
 __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restrict__ Dp,
                                                 const EOMat<typename Eng::C, Q>& eo,
                                                 const EOMat<typename Eng::C, Q>& eot, const typename Eng::S* us,
@@ -545,8 +546,9 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
                                                 typename Eng::V* W2, typename Eng::V* W3, int ne, int tid, int nt,
                                                 typename Eng::S* __restrict__ vb,
                                                 const typename Eng::S* __restrict__ mb, double lambda,
-                                                double* dot = nullptr, AfterPw after_pw = AfterPw())
+                                                ffacc* dot = nullptr, AfterPw after_pw = AfterPw())
 {
+    static_assert(!DOT || sizeof(typename Eng::S) == 4, "the fused dot product is for FP32 storage");
     static_assert(!DPAR || EO, "direction-parallel sweeps need the even-odd form");
     using S = typename Eng::S;
     using V = typename Eng::V;
@@ -699,7 +701,7 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
         S out = Eng::store(res);
         if (mb != nullptr) out += lam * mb[w] * us[w];
         vb[w] = out;
-        if (dot != nullptr) *dot = fma(double(us[w]), double(out), *dot);   // u . A u, for CG
+        if constexpr (DOT) acc_madd_f(*dot, us[w], out);   // u . A u for CG, compensated
     }
     __syncthreads();
 }
