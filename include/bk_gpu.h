@@ -95,7 +95,10 @@ typedef struct bk_options {
     int layout;    /* BK5: bk_layout; BK3 reads G factor-major (bk3_sumfact.h:53) */
     int nfactors;  /* BK5: 6 (symmetric rr rs rt ss st tt) or 9 (full 3x3,
                       row-major; bk5_offload.cpp "F") */
-    int elems_per_block; /* elements per thread block; 0: the tuned default */
+    int elems_per_block; /* BK5 column kernel: elements per thread block, 0
+                            or its default (other values BK_ERR_ARG); the
+                            sweep kernels use per-order tables measured on
+                            GB300 and ignore it */
     int kernel;    /* bk_kernel_shape (BK5); BK1/BK3 have the sweep kernel only */
 } bk_options;
 

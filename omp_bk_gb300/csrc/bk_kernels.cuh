@@ -26,6 +26,7 @@
 #pragma once
 
 #include <cstdint>
+#include <type_traits>
 
 #include "bk_device.cuh"
 #include "bk_engine.cuh"
@@ -493,12 +494,9 @@ __device__ __forceinline__ int g_index(int i, int j, int f, int k)
     return ((f * Q + k) * Q + i) * Q + j;
 }
 
-// GD: G read from global memory in the pointwise stage (coalesced in every
-// layout: points are walked in G's own order) instead of staged by TMA, which
-// leaves the block's shared memory to u and the work boxes.
 // DPAR != 0: three thread groups, one direction each (bk5_sweep_batch), and
 // a fourth work box.
-template <class Eng, int Q, int EB, int F, int LAYOUT, bool GD = false, int DPAR = 0>
+template <class Eng, int Q, int EB, int F, int LAYOUT, int DPAR = 0>
 struct BK5Cfg {
     using S = typename Eng::S;
     using V = typename Eng::V;
@@ -508,7 +506,7 @@ struct BK5Cfg {
     static constexpr int NT = DPAR ? 3 * LINES : (LINES < 64 ? 64 : LINES);
     static constexpr int NBOX = DPAR ? 4 : 3;
     static constexpr int U_BYTES = stage_bytes<S>(EB * Q3);
-    static constexpr int G_BYTES = GD ? 0 : stage_bytes<S>(EB * F * Q3);
+    static constexpr int G_BYTES = stage_bytes<S>(EB * F * Q3);
     static constexpr int STAGE_BYTES = U_BYTES + G_BYTES;
     static constexpr int W_BYTES = NBOX * EB * WB::size * int(sizeof(V));
     static constexpr int SMEM = STAGE_BYTES + W_BYTES + 16;
@@ -676,33 +674,41 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
     // 7. -> v in global memory (consecutive threads, consecutive values):
     //    the sum of the three terms (even-odd: here; otherwise already in W2)
     //    and the Helmholtz mass term lambda * mass * u in the storage type's
-    //    arithmetic (double for the FP64 engines)
-    for (int w = tid; w < ne * Q3; w += nt) {
-        const int e = w / Q3;
-        const int x = w - e * Q3;
-        const int i = x / (Q * Q);
-        const int j = (x / Q) % Q;
-        const int k = x % Q;
-        const int wi = e * WB::size + WB::at(i, j, k);
-        V res;
-        if constexpr (EO) {
-            if constexpr (HasSum3<Eng>::value) {
-                res = Eng::sum3(QT[wi], W0[wi], W1[wi]);
+    //    arithmetic (double for the FP64 engines).  The loop is written twice
+    //    (with and without the mass term) so that no point carries the
+    //    predicated-off mass arithmetic.
+    auto last_pass = [&](auto with_mass) {
+        for (int w = tid; w < ne * Q3; w += nt) {
+            const int e = w / Q3;
+            const int x = w - e * Q3;
+            const int i = x / (Q * Q);
+            const int j = (x / Q) % Q;
+            const int k = x % Q;
+            const int wi = e * WB::size + WB::at(i, j, k);
+            V res;
+            if constexpr (EO) {
+                if constexpr (HasSum3<Eng>::value) {
+                    res = Eng::sum3(QT[wi], W0[wi], W1[wi]);
+                } else {
+                    A acc = Eng::zero();
+                    Eng::add(acc, QT[wi]);
+                    Eng::add(acc, W0[wi]);
+                    Eng::add(acc, W1[wi]);
+                    res = Eng::result(acc);
+                }
             } else {
-                A acc = Eng::zero();
-                Eng::add(acc, QT[wi]);
-                Eng::add(acc, W0[wi]);
-                Eng::add(acc, W1[wi]);
-                res = Eng::result(acc);
+                res = W2[wi];
             }
-        } else {
-            res = W2[wi];
+            S out = Eng::store(res);
+            if constexpr (decltype(with_mass)::value) out += lam * mb[w] * us[w];
+            vb[w] = out;
+            if constexpr (DOT) acc_madd_f(*dot, us[w], out);   // u . A u for CG, compensated
         }
-        S out = Eng::store(res);
-        if (mb != nullptr) out += lam * mb[w] * us[w];
-        vb[w] = out;
-        if constexpr (DOT) acc_madd_f(*dot, us[w], out);   // u . A u for CG, compensated
-    }
+    };
+    if (mb != nullptr)
+        last_pass(std::true_type{});
+    else
+        last_pass(std::false_type{});
     __syncthreads();
 }
 
@@ -711,14 +717,14 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
 // stops reading them (after the pointwise stage; after the last pass when a
 // mass term reads u there), so the copies overlap the transposed sweeps and
 // the last pass instead of stalling the block at the start of each batch.
-template <class Eng, int Q, int EB, int F, int LAYOUT, bool EO = false, bool GD = false, int DPAR = 0>
-__global__ void __launch_bounds__(BK5Cfg<Eng, Q, EB, F, LAYOUT, GD, DPAR>::NT)
+template <class Eng, int Q, int EB, int F, int LAYOUT, bool EO = false, int DPAR = 0>
+__global__ void __launch_bounds__(BK5Cfg<Eng, Q, EB, F, LAYOUT, DPAR>::NT)
     bk5_kernel(const __grid_constant__ P5<typename Eng::C, Q> prm, const long long E,
                const typename Eng::S* __restrict__ u, const typename Eng::S* __restrict__ G,
                const typename Eng::S* __restrict__ mass, const double lambda, typename Eng::S* __restrict__ v,
                const DevCtx ctx)
 {
-    using Cfg = BK5Cfg<Eng, Q, EB, F, LAYOUT, GD, DPAR>;
+    using Cfg = BK5Cfg<Eng, Q, EB, F, LAYOUT, DPAR>;
     using S = typename Eng::S;
     using V = typename Eng::V;
     using WB = typename Cfg::WB;
@@ -749,7 +755,7 @@ __global__ void __launch_bounds__(BK5Cfg<Eng, Q, EB, F, LAYOUT, GD, DPAR>::NT)
         uint32_t tx = 0;
         if (tid == 0) fence_proxy_async();
         us = stage_issue<S>(smem, u + e0 * Q3, ne * Q3, bar, tx, tid, nt);
-        gs = GD ? G + e0 * F * Q3 : stage_issue<S>(smem + Cfg::U_BYTES, G + e0 * F * Q3, ne * F * Q3, bar, tx, tid, nt);
+        gs = stage_issue<S>(smem + Cfg::U_BYTES, G + e0 * F * Q3, ne * F * Q3, bar, tx, tid, nt);
         if (tid == 0) mbar_arrive_expect_tx(bar, tx);
     };
     if (blockIdx.x < nbatch) issue(blockIdx.x);
@@ -993,29 +999,37 @@ __global__ void __launch_bounds__(BK3Cfg<Eng, Q, EB, DPAR>::NT)
             sweep<Eng, WB, 2, Q, Q, Q, Q>(W2, W3, ne, Dg, tid, nt);   // qt
         }
         __syncthreads();
-        for (int w = tid; w < ne * Q3; w += nt) {
-            const int e = w / Q3;
-            const int x = w - e * Q3;
-            const int i = x / (Q * Q), j = (x / Q) % Q, k = x % Q;
-            const int wi = e * WB::size + WB::at(i, j, k);
-            V qr = W0[wi], qs = W1[wi], qt = W3[wi];
-            if (ks != nullptr) {
-                const V kk = Eng::load(ks[e * Q3 + x]);
-                qr = Eng::mul(kk, qr);
-                qs = Eng::mul(kk, qs);
-                qt = Eng::mul(kk, qt);
+        // fluxes (k G grad u with the coefficient); written twice, with and
+        // without k, so that no point carries predicated-off products
+        auto fluxes = [&](auto with_k) {
+            for (int w = tid; w < ne * Q3; w += nt) {
+                const int e = w / Q3;
+                const int x = w - e * Q3;
+                const int i = x / (Q * Q), j = (x / Q) % Q, k = x % Q;
+                const int wi = e * WB::size + WB::at(i, j, k);
+                V qr = W0[wi], qs = W1[wi], qt = W3[wi];
+                if constexpr (decltype(with_k)::value) {
+                    const V kk = Eng::load(ks[e * Q3 + x]);
+                    qr = Eng::mul(kk, qr);
+                    qs = Eng::mul(kk, qs);
+                    qt = Eng::mul(kk, qt);
+                }
+                const S* ge = gs + e * 6 * Q3 + x;   // factor-major
+                const V g0 = Eng::load(ge[0]), g1 = Eng::load(ge[Q3]), g2 = Eng::load(ge[2 * Q3]);
+                const V g3 = Eng::load(ge[3 * Q3]), g4 = Eng::load(ge[4 * Q3]), g5 = Eng::load(ge[5 * Q3]);
+                A r0 = Eng::zero(), r1 = Eng::zero(), r2 = Eng::zero();
+                Eng::vmadd(r0, g0, qr); Eng::vmadd(r0, g1, qs); Eng::vmadd(r0, g2, qt);
+                Eng::vmadd(r1, g1, qr); Eng::vmadd(r1, g3, qs); Eng::vmadd(r1, g4, qt);
+                Eng::vmadd(r2, g2, qr); Eng::vmadd(r2, g4, qs); Eng::vmadd(r2, g5, qt);
+                W0[wi] = Eng::result(r0);
+                W1[wi] = Eng::result(r1);
+                W3[wi] = Eng::result(r2);
             }
-            const S* ge = gs + e * 6 * Q3 + x;   // factor-major
-            const V g0 = Eng::load(ge[0]), g1 = Eng::load(ge[Q3]), g2 = Eng::load(ge[2 * Q3]);
-            const V g3 = Eng::load(ge[3 * Q3]), g4 = Eng::load(ge[4 * Q3]), g5 = Eng::load(ge[5 * Q3]);
-            A r0 = Eng::zero(), r1 = Eng::zero(), r2 = Eng::zero();
-            Eng::vmadd(r0, g0, qr); Eng::vmadd(r0, g1, qs); Eng::vmadd(r0, g2, qt);
-            Eng::vmadd(r1, g1, qr); Eng::vmadd(r1, g3, qs); Eng::vmadd(r1, g4, qt);
-            Eng::vmadd(r2, g2, qr); Eng::vmadd(r2, g4, qs); Eng::vmadd(r2, g5, qt);
-            W0[wi] = Eng::result(r0);
-            W1[wi] = Eng::result(r1);
-            W3[wi] = Eng::result(r2);
-        }
+        };
+        if (ks != nullptr)
+            fluxes(std::true_type{});
+        else
+            fluxes(std::false_type{});
         __syncthreads();
         if (bt + gridDim.x < nbatch) issue(bt + gridDim.x);   // the stage is free
         if constexpr (DPAR) {

@@ -112,10 +112,10 @@ template <int Q, int EB, int F, int LAYOUT, bool EO, int DPAR>
 int bk5_launch(const P5<typename Eng::C, Q>& prm, long long E, const void* u, const void* G, const void* mass,
                double lambda, void* v, cudaStream_t s)
 {
-    using Cfg = BK5Cfg<Eng, Q, EB, F, LAYOUT, false, DPAR>;
+    using Cfg = BK5Cfg<Eng, Q, EB, F, LAYOUT, DPAR>;
     using S = typename Eng::S;
     static_assert(Cfg::SMEM <= 232448, "BK5 block exceeds the shared memory of an SM");
-    auto kern = bk5_kernel<Eng, Q, EB, F, LAYOUT, EO, false, DPAR>;
+    auto kern = bk5_kernel<Eng, Q, EB, F, LAYOUT, EO, DPAR>;
     const int occ = prepare<EoTag<Cfg, EO>>(kern, Cfg::SMEM, Cfg::NT);
     if (occ <= 0) return BK_ERR_CUDA;
     const int grid = grid_for((E + EB - 1) / EB, occ);
@@ -128,7 +128,7 @@ int bk5_launch(const P5<typename Eng::C, Q>& prm, long long E, const void* u, co
 template <int Q, int F, int EB0, int DPAR = 0>
 constexpr int fit_eb5()
 {
-    if constexpr (EB0 > 1 && BK5Cfg<Eng, Q, EB0, F, BK_LAYOUT_TU, false, DPAR>::SMEM > 232448)
+    if constexpr (EB0 > 1 && BK5Cfg<Eng, Q, EB0, F, BK_LAYOUT_TU, DPAR>::SMEM > 232448)
         return fit_eb5<Q, F, EB0 - 1, DPAR>();
     else
         return EB0;
@@ -142,11 +142,10 @@ constexpr bool sweep_dpar5(int q) { return eng_is_ff() && q >= 6 && q <= 9; }
 constexpr int sweep_eb5_dpar(int q) { return q == 6 ? 4 : q == 7 ? 2 : 1; }
 
 template <int Q>
-int bk5_sweep_q(int F, int gd, const double* D, long long E, const void* u, const void* G, const void* mass,
+int bk5_sweep_q(int F, const double* D, long long E, const void* u, const void* G, const void* mass,
                 double lambda, void* v, cudaStream_t s)
 {
     constexpr int L = BK_LAYOUT_TU;
-    (void)gd;
     P5<typename Eng::C, Q> prm;
     for (int i = 0; i < Q * Q; ++i) prm.D[i] = Eng::coef(D[i]);
     // the even-odd contractions when D is centro-antisymmetric (GLL points);
@@ -313,19 +312,19 @@ using namespace BK_TU_NS;
 #if BK_OP_TU == 5
 #define BK_CATS_(a, b, c) a##_##b##_L##c
 #define BK_CATS(a, b, c) BK_CATS_(a, b, c)
-int BK_CATS(bk5_sweep, BK_SFX, BK_LAYOUT_TU)(int p, int F, int gd, const double* D, long long E, const void* u,
+int BK_CATS(bk5_sweep, BK_SFX, BK_LAYOUT_TU)(int p, int F, const double* D, long long E, const void* u,
                                               const void* G, const void* mass, double lambda, void* v,
                                               cudaStream_t s)
 {
     switch (p + 1) {
-        case 2: return bk5_sweep_q<2>(F, gd, D, E, u, G, mass, lambda, v, s);
-        case 3: return bk5_sweep_q<3>(F, gd, D, E, u, G, mass, lambda, v, s);
-        case 4: return bk5_sweep_q<4>(F, gd, D, E, u, G, mass, lambda, v, s);
-        case 5: return bk5_sweep_q<5>(F, gd, D, E, u, G, mass, lambda, v, s);
-        case 6: return bk5_sweep_q<6>(F, gd, D, E, u, G, mass, lambda, v, s);
-        case 7: return bk5_sweep_q<7>(F, gd, D, E, u, G, mass, lambda, v, s);
-        case 8: return bk5_sweep_q<8>(F, gd, D, E, u, G, mass, lambda, v, s);
-        case 9: return bk5_sweep_q<9>(F, gd, D, E, u, G, mass, lambda, v, s);
+        case 2: return bk5_sweep_q<2>(F, D, E, u, G, mass, lambda, v, s);
+        case 3: return bk5_sweep_q<3>(F, D, E, u, G, mass, lambda, v, s);
+        case 4: return bk5_sweep_q<4>(F, D, E, u, G, mass, lambda, v, s);
+        case 5: return bk5_sweep_q<5>(F, D, E, u, G, mass, lambda, v, s);
+        case 6: return bk5_sweep_q<6>(F, D, E, u, G, mass, lambda, v, s);
+        case 7: return bk5_sweep_q<7>(F, D, E, u, G, mass, lambda, v, s);
+        case 8: return bk5_sweep_q<8>(F, D, E, u, G, mass, lambda, v, s);
+        case 9: return bk5_sweep_q<9>(F, D, E, u, G, mass, lambda, v, s);
         default: return BK_ERR_ORDER;
     }
 }
@@ -402,11 +401,10 @@ int BK_CAT(launch_bk5, BK_SFX)(int p, long long E, const double* D, const void* 
     // AUTO: the sweep kernel, measured equal or faster than the column kernel
     // for every form at p = 7 (GB300)
     if (kernel == BK_KERNEL_SWEEP || kernel == BK_KERNEL_AUTO) {
-        const int gd = 0;
         switch (layout) {
-            case 0: return BK_CATL(bk5_sweep, BK_SFX, 0)(p, F, gd, D, E, u, G, mass, lambda, v, s);
-            case 1: return BK_CATL(bk5_sweep, BK_SFX, 1)(p, F, gd, D, E, u, G, mass, lambda, v, s);
-            case 2: return BK_CATL(bk5_sweep, BK_SFX, 2)(p, F, gd, D, E, u, G, mass, lambda, v, s);
+            case 0: return BK_CATL(bk5_sweep, BK_SFX, 0)(p, F, D, E, u, G, mass, lambda, v, s);
+            case 1: return BK_CATL(bk5_sweep, BK_SFX, 1)(p, F, D, E, u, G, mass, lambda, v, s);
+            case 2: return BK_CATL(bk5_sweep, BK_SFX, 2)(p, F, D, E, u, G, mass, lambda, v, s);
             default: return BK_ERR_PREC;
         }
     }
