@@ -184,12 +184,11 @@ __global__ void __launch_bounds__(BK3AdjCfg<Eng, Q, EB, DPAR>::NT)
             const V g3 = Eng::load(ge[3 * Q3]), g4 = Eng::load(ge[4 * Q3]), g5 = Eng::load(ge[5 * Q3]);
             const V kk = Eng::load(ks[e * Q3 + x]);
             // dL/dk = sum_ab res_a G_ab u_b
-            A f0 = Eng::zero(), f1 = Eng::zero(), f2 = Eng::zero();
-            Eng::vmadd(f0, g0, ur); Eng::vmadd(f0, g1, us_); Eng::vmadd(f0, g2, ut);
-            Eng::vmadd(f1, g1, ur); Eng::vmadd(f1, g3, us_); Eng::vmadd(f1, g4, ut);
-            Eng::vmadd(f2, g2, ur); Eng::vmadd(f2, g4, us_); Eng::vmadd(f2, g5, ut);
-            A d = Eng::zero();
-            Eng::vmadd(d, rr, Eng::result(f0));
+            A f0 = Eng::vfirst(g0, ur), f1 = Eng::vfirst(g1, ur), f2 = Eng::vfirst(g2, ur);
+            Eng::vmadd(f0, g1, us_); Eng::vmadd(f0, g2, ut);
+            Eng::vmadd(f1, g3, us_); Eng::vmadd(f1, g4, ut);
+            Eng::vmadd(f2, g4, us_); Eng::vmadd(f2, g5, ut);
+            A d = Eng::vfirst(rr, Eng::result(f0));
             Eng::vmadd(d, rs_, Eng::result(f1));
             Eng::vmadd(d, rt, Eng::result(f2));
             const long long o = (e0 + e) * Q3 + x;
@@ -197,10 +196,9 @@ __global__ void __launch_bounds__(BK3AdjCfg<Eng, Q, EB, DPAR>::NT)
             // dL/dG
             S* go = dG + (e0 + e) * 6 * Q3 + x;
             const V kr = Eng::mul(kk, rr), ks_ = Eng::mul(kk, rs_), kt = Eng::mul(kk, rt);
-            auto prod = [&](V a, V b) { A t = Eng::zero(); Eng::vmadd(t, a, b); return Eng::result(t); };
+            auto prod = [&](V a, V b) { return Eng::result(Eng::vfirst(a, b)); };
             auto prod2 = [&](V a, V b, V c, V dd) {
-                A t = Eng::zero();
-                Eng::vmadd(t, a, b);
+                A t = Eng::vfirst(a, b);
                 Eng::vmadd(t, c, dd);
                 return Eng::result(t);
             };

@@ -26,6 +26,10 @@ struct EngDfma {
     __device__ static __forceinline__ V load(S x) { return x; }
     __device__ static __forceinline__ S store(V x) { return x; }
     __device__ static __forceinline__ A zero() { return 0.0; }
+    // an accumulator started with a first product / value (no add to zero)
+    __device__ static __forceinline__ A first(C c, V x) { return c * x; }
+    __device__ static __forceinline__ A vfirst(V a, V x) { return a * x; }
+    __device__ static __forceinline__ A from(V x) { return x; }
     __device__ static __forceinline__ void madd(A& acc, C c, V x) { acc = fma(c, x, acc); }
     __device__ static __forceinline__ void vmadd(A& acc, V a, V x) { acc = fma(a, x, acc); }
     __device__ static __forceinline__ void add(A& acc, V x) { acc += x; }
@@ -52,6 +56,10 @@ struct EngFF {
     __device__ static __forceinline__ V load(S x) { return split(x); }
     __device__ static __forceinline__ S store(V x) { return join(x); }
     __device__ static __forceinline__ A zero() { return acc_zero(); }
+    // the first product needs no TwoSum into an empty accumulator
+    __device__ static __forceinline__ A first(C c, V x) { return acc_first(c, x); }
+    __device__ static __forceinline__ A vfirst(V a, V x) { return acc_first(a, x); }
+    __device__ static __forceinline__ A from(V x) { return ffacc{x.hi, x.lo}; }
     __device__ static __forceinline__ void madd(A& acc, C c, V x) { acc_madd(acc, c, x); }
     __device__ static __forceinline__ void vmadd(A& acc, V a, V x) { acc_madd(acc, a, x); }
     __device__ static __forceinline__ void add(A& acc, V x) { acc_add(acc, x); }
@@ -82,6 +90,9 @@ struct EngF32 {
     __device__ static __forceinline__ V load(S x) { return x; }
     __device__ static __forceinline__ S store(V x) { return x; }
     __device__ static __forceinline__ A zero() { return 0.0f; }
+    __device__ static __forceinline__ A first(C c, V x) { return c * x; }
+    __device__ static __forceinline__ A vfirst(V a, V x) { return a * x; }
+    __device__ static __forceinline__ A from(V x) { return x; }
     __device__ static __forceinline__ void madd(A& acc, C c, V x) { acc = fmaf(c, x, acc); }
     __device__ static __forceinline__ void vmadd(A& acc, V a, V x) { acc = fmaf(a, x, acc); }
     __device__ static __forceinline__ void add(A& acc, V x) { acc += x; }

@@ -75,6 +75,17 @@ __device__ __forceinline__ void acc_madd(ffacc& acc, const ff a, const ff x)
     acc.c = __fadd_rn(acc.c, __fadd_rn(e, pe));
 }
 
+// The accumulator holding a * x alone: the product as p + pe (no TwoSum
+// into zero).
+__device__ __forceinline__ ffacc acc_first(const ff a, const ff x)
+{
+    const float p = __fmul_rn(a.hi, x.hi);
+    float pe = __fmaf_rn(a.hi, x.hi, -p);
+    pe = __fmaf_rn(a.hi, x.lo, pe);
+    pe = __fmaf_rn(a.lo, x.hi, pe);
+    return ffacc{p, pe};
+}
+
 // acc += x (float-float).
 __device__ __forceinline__ void acc_add(ffacc& acc, const ff x)
 {

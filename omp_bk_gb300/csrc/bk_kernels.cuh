@@ -136,9 +136,9 @@ __device__ __forceinline__ void sweep(const typename Eng::V* in, typename Eng::V
         for (int n = 0; n < NI; ++n) x[n] = in[base + n * SD];
 #pragma unroll
         for (int o = 0; o < NO; ++o) {
-            A acc = Eng::zero();
+            A acc = Eng::first(mat(o, 0), x[0]);
 #pragma unroll
-            for (int n = 0; n < NI; ++n) Eng::madd(acc, mat(o, n), x[n]);
+            for (int n = 1; n < NI; ++n) Eng::madd(acc, mat(o, n), x[n]);
             out[base + o * SD] = Eng::result(acc);
         }
     }
@@ -218,9 +218,9 @@ __device__ __forceinline__ void sweep_eo(const typename Eng::V* in, typename Eng
         }
 #pragma unroll
         for (int o = 0; o < H; ++o) {
-            A aa = Eng::zero(), bb = Eng::zero();
+            A aa = Eng::first(m.A[o * H], ev[0]), bb = Eng::first(m.B[o * H], dv[0]);
 #pragma unroll
-            for (int n = 0; n < H; ++n) {
+            for (int n = 1; n < H; ++n) {
                 Eng::madd(aa, m.A[o * H + n], ev[n]);
                 Eng::madd(bb, m.B[o * H + n], dv[n]);
             }
@@ -231,9 +231,9 @@ __device__ __forceinline__ void sweep_eo(const typename Eng::V* in, typename Eng
             out[base + (Q - 1 - o) * SD] = d;
         }
         if (Q & 1) {
-            A t = Eng::zero();
+            A t = Eng::first(m.r[0], dv[0]);
 #pragma unroll
-            for (int n = 0; n < H; ++n) Eng::madd(t, m.r[n], dv[n]);
+            for (int n = 1; n < H; ++n) Eng::madd(t, m.r[n], dv[n]);
             out[base + H * SD] = Eng::result(t);
         }
     }
@@ -271,9 +271,9 @@ __device__ __forceinline__ void sweep_eo_dyn(const typename Eng::V* in, typename
         }
 #pragma unroll
         for (int o = 0; o < H; ++o) {
-            A aa = Eng::zero(), bb = Eng::zero();
+            A aa = Eng::first(m.A[o * H], ev[0]), bb = Eng::first(m.B[o * H], dv[0]);
 #pragma unroll
-            for (int n = 0; n < H; ++n) {
+            for (int n = 1; n < H; ++n) {
                 Eng::madd(aa, m.A[o * H + n], ev[n]);
                 Eng::madd(bb, m.B[o * H + n], dv[n]);
             }
@@ -284,9 +284,9 @@ __device__ __forceinline__ void sweep_eo_dyn(const typename Eng::V* in, typename
             po[(Q - 1 - o) * SD] = d;
         }
         if (Q & 1) {
-            A t = Eng::zero();
+            A t = Eng::first(m.r[0], dv[0]);
 #pragma unroll
-            for (int n = 0; n < H; ++n) Eng::madd(t, m.r[n], dv[n]);
+            for (int n = 1; n < H; ++n) Eng::madd(t, m.r[n], dv[n]);
             po[H * SD] = Eng::result(t);
         }
     }
@@ -370,17 +370,17 @@ __device__ __forceinline__ void sweep_eor(const typename Eng::V* in, typename En
         }
         V mid_out;
         if constexpr ((NO & 1) != 0) {
-            A t = Eng::zero();
+            A t = Eng::first(m.r[0], SIGN > 0 ? ev[0] : dv[0]);
 #pragma unroll
-            for (int n = 0; n < HI; ++n) Eng::madd(t, m.r[n], SIGN > 0 ? ev[n] : dv[n]);
+            for (int n = 1; n < HI; ++n) Eng::madd(t, m.r[n], SIGN > 0 ? ev[n] : dv[n]);
             if constexpr (SIGN > 0 && (NI & 1) != 0) Eng::madd(t, m.rm, x[HI]);
             mid_out = Eng::result(t);
         }
 #pragma unroll
         for (int o = 0; o < HO; ++o) {
-            A aa = Eng::zero(), bb = Eng::zero();
+            A aa = Eng::first(m.A[o * HI], ev[0]), bb = Eng::first(m.B[o * HI], dv[0]);
 #pragma unroll
-            for (int n = 0; n < HI; ++n) {
+            for (int n = 1; n < HI; ++n) {
                 Eng::madd(aa, m.A[o * HI + n], ev[n]);
                 Eng::madd(bb, m.B[o * HI + n], dv[n]);
             }
@@ -602,16 +602,16 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
         const V qr = W0[wi], qs = W1[wi], qt = QT[wi];
         const S* ge = gs + e * F * Q3;
         auto g = [&](int f) { return Eng::load(ge[g_index<Eng, Q, F, LAYOUT>(i, j, f, k)]); };
-        A r0 = Eng::zero(), r1 = Eng::zero(), r2 = Eng::zero();
+        A r0, r1, r2;
         if (F == 6) {
             const V g0 = g(0), g1 = g(1), g2 = g(2), g3 = g(3), g4 = g(4), g5 = g(5);
-            Eng::vmadd(r0, g0, qr); Eng::vmadd(r0, g1, qs); Eng::vmadd(r0, g2, qt);
-            Eng::vmadd(r1, g1, qr); Eng::vmadd(r1, g3, qs); Eng::vmadd(r1, g4, qt);
-            Eng::vmadd(r2, g2, qr); Eng::vmadd(r2, g4, qs); Eng::vmadd(r2, g5, qt);
+            r0 = Eng::vfirst(g0, qr); Eng::vmadd(r0, g1, qs); Eng::vmadd(r0, g2, qt);
+            r1 = Eng::vfirst(g1, qr); Eng::vmadd(r1, g3, qs); Eng::vmadd(r1, g4, qt);
+            r2 = Eng::vfirst(g2, qr); Eng::vmadd(r2, g4, qs); Eng::vmadd(r2, g5, qt);
         } else {
-            Eng::vmadd(r0, g(0), qr); Eng::vmadd(r0, g(1), qs); Eng::vmadd(r0, g(2), qt);
-            Eng::vmadd(r1, g(3), qr); Eng::vmadd(r1, g(4), qs); Eng::vmadd(r1, g(5), qt);
-            Eng::vmadd(r2, g(6), qr); Eng::vmadd(r2, g(7), qs); Eng::vmadd(r2, g(8), qt);
+            r0 = Eng::vfirst(g(0), qr); Eng::vmadd(r0, g(1), qs); Eng::vmadd(r0, g(2), qt);
+            r1 = Eng::vfirst(g(3), qr); Eng::vmadd(r1, g(4), qs); Eng::vmadd(r1, g(5), qt);
+            r2 = Eng::vfirst(g(6), qr); Eng::vmadd(r2, g(7), qs); Eng::vmadd(r2, g(8), qt);
         }
         W0[wi] = Eng::result(r0);
         W1[wi] = Eng::result(r1);
@@ -655,9 +655,9 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
             for (int n = 0; n < Q; ++n) x[n] = W2[base + n];
 #pragma unroll
             for (int o = 0; o < Q; ++o) {
-                A acc = Eng::zero();
+                A acc = Eng::first(Dt(o, 0), x[0]);
 #pragma unroll
-                for (int n = 0; n < Q; ++n) Eng::madd(acc, Dt(o, n), x[n]);
+                for (int n = 1; n < Q; ++n) Eng::madd(acc, Dt(o, n), x[n]);
                 V res;
                 if constexpr (HasSum3<Eng>::value) {
                     res = Eng::sum3(Eng::result(acc), W0[base + o], W1[base + o]);
@@ -690,8 +690,7 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
                 if constexpr (HasSum3<Eng>::value) {
                     res = Eng::sum3(QT[wi], W0[wi], W1[wi]);
                 } else {
-                    A acc = Eng::zero();
-                    Eng::add(acc, QT[wi]);
+                    A acc = Eng::from(QT[wi]);
                     Eng::add(acc, W0[wi]);
                     Eng::add(acc, W1[wi]);
                     res = Eng::result(acc);
@@ -1017,10 +1016,10 @@ __global__ void __launch_bounds__(BK3Cfg<Eng, Q, EB, DPAR>::NT)
                 const S* ge = gs + e * 6 * Q3 + x;   // factor-major
                 const V g0 = Eng::load(ge[0]), g1 = Eng::load(ge[Q3]), g2 = Eng::load(ge[2 * Q3]);
                 const V g3 = Eng::load(ge[3 * Q3]), g4 = Eng::load(ge[4 * Q3]), g5 = Eng::load(ge[5 * Q3]);
-                A r0 = Eng::zero(), r1 = Eng::zero(), r2 = Eng::zero();
-                Eng::vmadd(r0, g0, qr); Eng::vmadd(r0, g1, qs); Eng::vmadd(r0, g2, qt);
-                Eng::vmadd(r1, g1, qr); Eng::vmadd(r1, g3, qs); Eng::vmadd(r1, g4, qt);
-                Eng::vmadd(r2, g2, qr); Eng::vmadd(r2, g4, qs); Eng::vmadd(r2, g5, qt);
+                A r0 = Eng::vfirst(g0, qr), r1 = Eng::vfirst(g1, qr), r2 = Eng::vfirst(g2, qr);
+                Eng::vmadd(r0, g1, qs); Eng::vmadd(r0, g2, qt);
+                Eng::vmadd(r1, g3, qs); Eng::vmadd(r1, g4, qt);
+                Eng::vmadd(r2, g4, qs); Eng::vmadd(r2, g5, qt);
                 W0[wi] = Eng::result(r0);
                 W1[wi] = Eng::result(r1);
                 W3[wi] = Eng::result(r2);
@@ -1062,12 +1061,13 @@ __global__ void __launch_bounds__(BK3Cfg<Eng, Q, EB, DPAR>::NT)
                 for (int n = 0; n < Q; ++n) x[n] = W3[base + n];
 #pragma unroll
                 for (int o = 0; o < Q; ++o) {
-                    A acc = Eng::zero();
+                    A acc;
                     if constexpr (EO) {
-                        Eng::add(acc, x[o]);
+                        acc = Eng::from(x[o]);
                     } else {
+                        acc = Eng::first(Dtr(o, 0), x[0]);
 #pragma unroll
-                        for (int n = 0; n < Q; ++n) Eng::madd(acc, Dtr(o, n), x[n]);
+                        for (int n = 1; n < Q; ++n) Eng::madd(acc, Dtr(o, n), x[n]);
                     }
                     if constexpr (HasSum3<Eng>::value) {
                         W2[base + o] = Eng::sum3(Eng::result(acc), W0[base + o], W1[base + o]);

@@ -139,3 +139,23 @@ def test_tuner(bklib):
     best = tune.tune([(2, 512), (5, 256), (8, 64)], max_elements=512, reps=2, use_cache=False)
     for p in (2, 5, 8):
         assert best[p] in tune.candidates(p)
+
+
+def test_operator_spd(bklib, small_plan):
+    """K + lambda M is symmetric positive definite: u.Au >= lambda u.Mu > 0
+    (K positive semi-definite, the GLL mass positive) and u.Aw = w.Au."""
+    bk = bklib
+    plan, G, M, _ = small_plan
+    lam = 1.0
+    for seed in (21, 22, 23):
+        u = bk.fill_uniform(torch.empty(plan.n, dtype=torch.float64, device="cuda"), seed)
+        w = bk.fill_uniform(torch.empty_like(u), seed + 100)
+        Au, Aw = torch.empty_like(u), torch.empty_like(u)
+        plan.apply(G, M, lam, u, Au, prec=bk.PREC_FP64)
+        plan.apply(G, M, lam, w, Aw, prec=bk.PREC_FP64)
+        torch.cuda.synchronize()
+        uAu = float(torch.dot(u, Au))
+        uMu = float(torch.dot(u, M * u))
+        assert uMu > 0 and uAu >= lam * uMu * (1 - 1e-12)
+        scale = float(torch.linalg.norm(u) * torch.linalg.norm(Aw))
+        assert abs(float(torch.dot(u, Aw)) - float(torch.dot(w, Au))) <= 1e-12 * scale
