@@ -136,10 +136,10 @@ constexpr int fit_eb5()
 
 // The direction-parallel even-odd shape (three thread groups, one direction
 // each, one shared code body: DPAR = 2) for the float-float engine where it
-// measured faster on GB300: q = 6 (EB 4), 7 (EB 2), 8 and 9 (EB 1), 2-26 %
-// over one thread per line (q = 8: 31.5 against 24.9 GDoF/s).
+// measured faster on GB300: q = 6 (EB 4), 7 (EB 2), 8 (EB 1) and 9 (EB 3),
+// 2-33 % over one thread per line (q = 8: 36.9 against 30.2 GDoF/s).
 constexpr bool sweep_dpar5(int q) { return eng_is_ff() && q >= 6 && q <= 9; }
-constexpr int sweep_eb5_dpar(int q) { return q == 6 ? 4 : q == 7 ? 2 : 1; }
+constexpr int sweep_eb5_dpar(int q) { return q == 6 ? 4 : q == 7 ? 2 : q == 9 ? 3 : 1; }
 
 template <int Q>
 int bk5_sweep_q(int F, const double* D, long long E, const void* u, const void* G, const void* mass,
