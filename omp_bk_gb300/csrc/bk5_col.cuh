@@ -310,10 +310,10 @@ __global__ void __launch_bounds__(BK5ColCfg<Eng, Q, EB, F, NBUF, LAYOUT>::NT)
         unsigned char* st = stage0 + sb * Cfg::STAGE;
         uint32_t tx = 0;
         if (tid == 0) fence_proxy_async();
-        const S* us_ = stage_issue<S>(st, u + e0 * Q3, ne * Q3, &bars[sb], tx, tid, nt);
+        const S* us_ = stage_issue<S>(st, u + e0 * Q3, ne * Q3, u + E * Q3, &bars[sb], tx, tid, nt);
         const S* gs_ = Cfg::GDIR ? nullptr
-                                 : stage_issue<S>(st + Cfg::U_BYTES, G + e0 * F * Q3, ne * F * Q3, &bars[sb], tx,
-                                                  tid, nt);
+                                 : stage_issue<S>(st + Cfg::U_BYTES, G + e0 * F * Q3, ne * F * Q3, G + E * F * Q3,
+                                                  &bars[sb], tx, tid, nt);
         if (sb == 0) {
             us_slot0 = us_;
             gs_slot0 = gs_;

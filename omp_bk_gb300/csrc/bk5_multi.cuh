@@ -55,6 +55,8 @@ struct PMulti {
     C D[kMultiDTotal];          // D_q(i, n) at multi_doff(q) + i*q + n
     MultiSeg seg[kMultiNQ];
     int nseg;
+    long long n;    // values of u, v and mass over all segments
+    long long ng;   // values of G over all segments
 };
 
 // G is staged by TMA here (not held in registers): the kernel carries the
@@ -99,12 +101,13 @@ __global__ void __launch_bounds__(NT, 2)
         unsigned char* st = stage0 + sb * stage_bytes_;
         uint32_t tx = 0;
         if (tid == 0) fence_proxy_async();
-        const S* us_ = stage_issue<S>(st, u + sg.uoff + tl.e_first * q3, tl.ne * q3, &bars[sb], tx, tid, NT);
+        const S* us_ = stage_issue<S>(st, u + sg.uoff + tl.e_first * q3, tl.ne * q3, u + prm.n, &bars[sb], tx, tid, NT);
         const S* gs_ = nullptr;
         if constexpr (!GDIR) {
             // the G stage follows the u stage of the largest tile
             const int ub = ((tl.ne * q3 * int(sizeof(S)) + 15) / 16) * 16 + 16;
-            gs_ = stage_issue<S>(st + ub, G + sg.goff + tl.e_first * 6 * q3, tl.ne * 6 * q3, &bars[sb], tx, tid, NT);
+            gs_ = stage_issue<S>(st + ub, G + sg.goff + tl.e_first * 6 * q3, tl.ne * 6 * q3, G + prm.ng, &bars[sb], tx,
+                                tid, NT);
         }
         if (sb == 0) {
             us_slot0 = us_;
@@ -206,6 +209,8 @@ struct PMultiEO {
     EOSet<C> eo;
     MultiSeg seg[kMultiNQ];
     int nseg;
+    long long n;    // values of u, v and mass over all segments
+    long long ng;   // values of G over all segments
 };
 
 // Host: the even-odd forms of D_q (D(i, n) = d[i*q + n]) into P; false if D_q
@@ -298,7 +303,7 @@ __global__ void __launch_bounds__(NT, MINB)
         const int q3 = sg.q * sg.q * sg.q;
         uint32_t tx = 0;
         if (tid == 0) fence_proxy_async();
-        gs = stage_issue<S>(gstage, G + sg.goff + tl.e_first * 6 * q3, tl.ne * 6 * q3, bar, tx, tid, nt);
+        gs = stage_issue<S>(gstage, G + sg.goff + tl.e_first * 6 * q3, tl.ne * 6 * q3, G + prm.ng, bar, tx, tid, nt);
         if (tid == 0) mbar_expect_tx(bar, tx);
     };
     auto issue_um = [&](int t) {
@@ -307,9 +312,9 @@ __global__ void __launch_bounds__(NT, MINB)
         const int q3 = sg.q * sg.q * sg.q;
         uint32_t tx = 0;
         if (tid == 0) fence_proxy_async();
-        us = stage_issue<S>(ustage, u + sg.uoff + tl.e_first * q3, tl.ne * q3, bar, tx, tid, nt);
+        us = stage_issue<S>(ustage, u + sg.uoff + tl.e_first * q3, tl.ne * q3, u + prm.n, bar, tx, tid, nt);
         ms = (mass != nullptr)
-                 ? stage_issue<S>(mstage, mass + sg.uoff + tl.e_first * q3, tl.ne * q3, bar, tx, tid, nt)
+                 ? stage_issue<S>(mstage, mass + sg.uoff + tl.e_first * q3, tl.ne * q3, mass + prm.n, bar, tx, tid, nt)
                  : nullptr;
         if (tid == 0) mbar_arrive_expect_tx(bar, tx);
     };

@@ -139,8 +139,8 @@ __global__ void __launch_bounds__(BK3AdjCfg<Eng, Q, EB, DPAR>::NT)
         const int ne = int((E - e0) < EB ? (E - e0) : EB);
         uint32_t tx = 0;
         if (tid == 0) fence_proxy_async();
-        us = stage_issue<S>(ustage, u + e0 * P3, ne * P3, bar, tx, tid, nt);
-        rs = stage_issue<S>(rstage, res + e0 * P3, ne * P3, bar, tx, tid, nt);
+        us = stage_issue<S>(ustage, u + e0 * P3, ne * P3, u + E * P3, bar, tx, tid, nt);
+        rs = stage_issue<S>(rstage, res + e0 * P3, ne * P3, res + E * P3, bar, tx, tid, nt);
         if (tid == 0) {
             if (arrive)
                 mbar_arrive_expect_tx(bar, tx);
@@ -153,8 +153,8 @@ __global__ void __launch_bounds__(BK3AdjCfg<Eng, Q, EB, DPAR>::NT)
         const int ne = int((E - e0) < EB ? (E - e0) : EB);
         uint32_t tx = 0;
         if (tid == 0) fence_proxy_async();
-        gs = stage_issue<S>(gstage, G + e0 * 6 * Q3, ne * 6 * Q3, bar, tx, tid, nt);
-        ks = stage_issue<S>(kstage, kq + e0 * Q3, ne * Q3, bar, tx, tid, nt);
+        gs = stage_issue<S>(gstage, G + e0 * 6 * Q3, ne * 6 * Q3, G + E * 6 * Q3, bar, tx, tid, nt);
+        ks = stage_issue<S>(kstage, kq + e0 * Q3, ne * Q3, kq + E * Q3, bar, tx, tid, nt);
         if (tid == 0) mbar_arrive_expect_tx(bar, tx);
     };
     if (blockIdx.x < nbatch) {

@@ -459,6 +459,8 @@ void fill_params(PMulti<C>& P, const bk_hplan& h, const double* const* Dq, C (*c
         P.seg[s] = h.seg[s];
     }
     P.nseg = h.nseg;
+    P.n = h.n;
+    P.ng = h.ng;
 }
 
 template <class C, class Conv>
@@ -471,6 +473,8 @@ bool fill_eo_params(PMultiEO<C>& P, const bk_hplan& h, const double* const* Dq, 
         P.seg[s] = h.seg[s];
     }
     P.nseg = h.nseg;
+    P.n = h.n;
+    P.ng = h.ng;
     return ok;
 }
 

@@ -71,31 +71,31 @@ constexpr int stage_bytes(int n)
 
 // Issues the copy of src[0, n) (global) into the shared buffer `buf`
 // (16-byte aligned, stage_bytes(n) long).  Returns where src[0] lands.
-// Thread 0 issues the TMA part and adds its bytes to *tx; the head and the
-// tail (fewer than 16 bytes each) are loaded by the threads of the block.
+// `lim` is the end of the source array, whose start is 16-byte aligned: the
+// TMA copy runs from src rounded down to 16 bytes (still inside the array)
+// to the end rounded up to 16 bytes when that stays inside the array, so a
+// slice that does not start or end on a 16-byte boundary still needs no
+// synchronous loads; only a slice ending on the array's own unaligned end
+// loads its last few values with plain loads.  Thread 0 issues the TMA
+// part; every thread adds its bytes to *tx.
 template <class S>
-__device__ __forceinline__ S* stage_issue(void* buf, const S* src, int n, uint64_t* bar, uint32_t& tx,
+__device__ __forceinline__ S* stage_issue(void* buf, const S* src, int n, const S* lim, uint64_t* bar, uint32_t& tx,
                                           int tid, int nt)
 {
     const uintptr_t a = reinterpret_cast<uintptr_t>(src);
     const uintptr_t b = a + uintptr_t(n) * sizeof(S);
-    const uintptr_t a_up = (a + 15) & ~uintptr_t(15);
-    const uintptr_t b_dn = b & ~uintptr_t(15);
-    // place src[0] at offset (a mod 16) so that a_up lands on a 16-byte boundary
-    char* dst0 = static_cast<char*>(buf) + (a & 15);
-    S* dst = reinterpret_cast<S*>(dst0);
-    if (a_up < b_dn) {
-        if (tid == 0) {
-            tma_load_1d(dst0 + (a_up - a), reinterpret_cast<const void*>(a_up), uint32_t(b_dn - a_up), bar);
-        }
-        tx += uint32_t(b_dn - a_up);
-        const int head = int((a_up - a) / sizeof(S));
-        const int tail0 = int((b_dn - a) / sizeof(S));
-        for (int i = tid; i < head; i += nt) dst[i] = src[i];
-        for (int i = tail0 + tid; i < n; i += nt) dst[i] = src[i];
-    } else {
-        for (int i = tid; i < n; i += nt) dst[i] = src[i];
+    const uintptr_t a_dn = a & ~uintptr_t(15);
+    const uintptr_t b_up = (b + 15) & ~uintptr_t(15);
+    const uintptr_t b_cut = (b_up <= reinterpret_cast<uintptr_t>(lim)) ? b_up : (b & ~uintptr_t(15));
+    // src[0] at offset (a mod 16), so that a_dn lands on buf itself
+    S* dst = reinterpret_cast<S*>(static_cast<char*>(buf) + (a & 15));
+    int plain0 = 0;   // first value loaded with plain loads
+    if (b_cut > a_dn) {
+        if (tid == 0) tma_load_1d(buf, reinterpret_cast<const void*>(a_dn), uint32_t(b_cut - a_dn), bar);
+        tx += uint32_t(b_cut - a_dn);
+        plain0 = b_cut >= b ? n : int((b_cut - a) / sizeof(S));
     }
+    for (int i = plain0 + tid; i < n; i += nt) dst[i] = src[i];
     return dst;
 }
 
@@ -753,8 +753,8 @@ __global__ void __launch_bounds__(BK5Cfg<Eng, Q, EB, F, LAYOUT, DPAR>::NT)
         const int ne = int((E - e0) < EB ? (E - e0) : EB);
         uint32_t tx = 0;
         if (tid == 0) fence_proxy_async();
-        us = stage_issue<S>(smem, u + e0 * Q3, ne * Q3, bar, tx, tid, nt);
-        gs = stage_issue<S>(smem + Cfg::U_BYTES, G + e0 * F * Q3, ne * F * Q3, bar, tx, tid, nt);
+        us = stage_issue<S>(smem, u + e0 * Q3, ne * Q3, u + E * Q3, bar, tx, tid, nt);
+        gs = stage_issue<S>(smem + Cfg::U_BYTES, G + e0 * F * Q3, ne * F * Q3, G + E * F * Q3, bar, tx, tid, nt);
         if (tid == 0) mbar_arrive_expect_tx(bar, tx);
     };
     if (blockIdx.x < nbatch) issue(blockIdx.x);
@@ -832,8 +832,8 @@ __global__ void __launch_bounds__(BK1Cfg<Eng, Q, EB>::NT)
         const int ne = int((E - e0) < EB ? (E - e0) : EB);
         uint32_t tx = 0;
         if (tid == 0) fence_proxy_async();
-        us = stage_issue<S>(ustage, u + e0 * P3, ne * P3, bar, tx, tid, nt);
-        js = stage_issue<S>(jstage, jxw + e0 * Q3, ne * Q3, bar, tx, tid, nt);
+        us = stage_issue<S>(ustage, u + e0 * P3, ne * P3, u + E * P3, bar, tx, tid, nt);
+        js = stage_issue<S>(jstage, jxw + e0 * Q3, ne * Q3, jxw + E * Q3, bar, tx, tid, nt);
         if (tid == 0) mbar_arrive_expect_tx(bar, tx);
     };
     if (blockIdx.x < nbatch) issue(blockIdx.x);
@@ -956,9 +956,9 @@ __global__ void __launch_bounds__(BK3Cfg<Eng, Q, EB, DPAR>::NT)
         const int ne = int((E - e0) < EB ? (E - e0) : EB);
         uint32_t tx = 0;
         if (tid == 0) fence_proxy_async();
-        us = stage_issue<S>(ustage, u + e0 * P3, ne * P3, bar, tx, tid, nt);
-        gs = stage_issue<S>(gstage, G + e0 * 6 * Q3, ne * 6 * Q3, bar, tx, tid, nt);
-        ks = (kq != nullptr) ? stage_issue<S>(kstage, kq + e0 * Q3, ne * Q3, bar, tx, tid, nt) : nullptr;
+        us = stage_issue<S>(ustage, u + e0 * P3, ne * P3, u + E * P3, bar, tx, tid, nt);
+        gs = stage_issue<S>(gstage, G + e0 * 6 * Q3, ne * 6 * Q3, G + E * 6 * Q3, bar, tx, tid, nt);
+        ks = (kq != nullptr) ? stage_issue<S>(kstage, kq + e0 * Q3, ne * Q3, kq + E * Q3, bar, tx, tid, nt) : nullptr;
         if (tid == 0) mbar_arrive_expect_tx(bar, tx);
     };
     if (blockIdx.x < nbatch) issue(blockIdx.x);
