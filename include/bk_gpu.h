@@ -100,7 +100,21 @@ typedef struct bk_options {
                             sweep kernels use per-order tables measured on
                             GB300 and ignore it */
     int kernel;    /* bk_kernel_shape (BK5); BK1/BK3 have the sweep kernel only */
+    int gform;     /* bk_gform (BK5): how G is stored */
 } bk_options;
+
+/* BK5 geometric-factor storage forms. */
+enum bk_gform {
+    BK_G_STORAGE = 0, /* the storage type of prec (double for FP64) */
+    BK_G_FF = 1       /* float-float pairs (float hi, float lo; 8 bytes per
+                         value, the same footprint as double) made once by
+                         bk_g_to_ff: the float-float engine then skips the
+                         split of every G value it loads.  The pair is the
+                         split the engine applies to a double, so the apply's
+                         result is bitwise that of the double G.  FP64 with
+                         engine AUTO or FF, 6 factors, a D on points symmetric
+                         about 0 (GLL), sweep kernel; otherwise BK_ERR_PREC */
+};
 
 /* BK5 kernel shapes. */
 enum bk_kernel_shape {
@@ -114,7 +128,8 @@ enum bk_kernel_shape {
 };
 
 /* bk_options with the defaults: prec FP64, engine AUTO, BK5 layout
- * INTERLEAVED with 6 factors, elems_per_block 0, kernel AUTO. */
+ * INTERLEAVED with 6 factors, elems_per_block 0, kernel AUTO, gform
+ * STORAGE. */
 bk_options bk_default_options(void);
 
 /* ---- operator apply ------------------------------------------------------- */
@@ -177,6 +192,15 @@ int bk3_apply_k(int p, int64_t E, const double* B, const double* D, const void* 
 int bk3_adjoint(int p, int64_t E, const double* B, const double* D, const void* G, const void* k,
                 const void* u, const void* res, void* dk, void* dG, const bk_options* opt,
                 bk_stream_t stream);
+
+/* Splits n doubles G (device) into float-float pairs Gff (device, n x 8
+ * bytes; may be G itself: the conversion is in place value by value): hi =
+ * the value truncated to 24 significant bits, lo = the rest rounded to a
+ * float, exactly as the float-float engine splits a double it loads.  For
+ * BK5 applies with gform = BK_G_FF; a one-time preparation of the operator,
+ * like the reference's relayout of G (make_bk5_G, include/bk_harness.h:220).
+ * Asynchronous on stream. */
+int bk_g_to_ff(const void* G, void* Gff, int64_t n, bk_stream_t stream);
 
 /* ---- device status -------------------------------------------------------- */
 

@@ -34,6 +34,7 @@ PREC_FP64, PREC_FP32, PREC_MIXED = 0, 1, 2
 ENGINE_AUTO, ENGINE_DFMA, ENGINE_FF = 0, 1, 2
 LAYOUT_FACTOR, LAYOUT_INTERLEAVED, LAYOUT_COLUMN = 0, 1, 2
 KERNEL_AUTO, KERNEL_SWEEP, KERNEL_COLUMN = 0, 1, 2
+G_STORAGE, G_FF = 0, 1
 
 # every symbol the C headers declare (checked by the CPU tests)
 EXPORTS = [
@@ -46,6 +47,7 @@ EXPORTS = [
     "bk_hplan_create", "bk_hplan_destroy", "bk_hplan_size", "bk_hplan_set_kernel", "bk_hplan_apply", "bk_hplan_cg",
     "bk_dot_noalloc",
     "bk_host_plan_create", "bk_host_plan_destroy", "bk1_apply_host", "bk3_apply_host", "bk5_apply_host",
+    "bk_g_to_ff",
 ]
 
 
@@ -59,7 +61,7 @@ class BKError(RuntimeError):
 
 class Options(C.Structure):
     _fields_ = [("prec", C.c_int), ("engine", C.c_int), ("layout", C.c_int), ("nfactors", C.c_int),
-                ("elems_per_block", C.c_int), ("kernel", C.c_int)]
+                ("elems_per_block", C.c_int), ("kernel", C.c_int), ("gform", C.c_int)]
 
 
 _lib = None
@@ -106,6 +108,7 @@ def lib():
         "bk_stream_kernel": [C.c_int, C.c_longlong, _vp, _vp, _vp, C.c_int, _vp],
         "bk_dot": [C.c_longlong, _vp, _vp, C.c_int, _vp, _vp, C.c_longlong, C.c_int, _vp],
         "bk_axpby": [C.c_longlong, C.c_double, _vp, C.c_double, _vp, C.c_int, _vp],
+        "bk_g_to_ff": [_vp, _vp, _i64, _vp],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -168,9 +171,11 @@ class ApplyOptions:
     nfactors: int = 6
     elems_per_block: int = 0
     kernel: int = KERNEL_AUTO
+    gform: int = G_STORAGE
 
     def c(self) -> Options:
-        return Options(self.prec, self.engine, self.layout, self.nfactors, self.elems_per_block, self.kernel)
+        return Options(self.prec, self.engine, self.layout, self.nfactors, self.elems_per_block, self.kernel,
+                       self.gform)
 
 
 # ---- operator apply (device tensors) -------------------------------------------
@@ -195,14 +200,25 @@ def bk3_apply(p, E, B, D, G, u, v, k=None, prec=PREC_FP64, engine=ENGINE_AUTO, s
 
 
 def bk5_apply(p, E, D, G, u, v, prec=PREC_FP64, engine=ENGINE_AUTO, layout=LAYOUT_INTERLEAVED, nfactors=6,
-              mass=None, lam=0.0, kernel=KERNEL_AUTO, elems_per_block=0, stream=None):
-    """v = D^T G D u (+ lam * mass * u) per element (openmp/BK5.cpp:18-103)."""
+              mass=None, lam=0.0, kernel=KERNEL_AUTO, elems_per_block=0, gform=G_STORAGE, stream=None):
+    """v = D^T G D u (+ lam * mass * u) per element (openmp/BK5.cpp:18-103).
+    gform=G_FF: G holds the float-float pairs made by g_to_ff."""
     _order(p, "bk5_apply")
     Dh, Dp = _host(D)
     o = ApplyOptions(prec=prec, engine=engine, layout=layout, nfactors=nfactors, kernel=kernel,
-                     elems_per_block=elems_per_block).c()
+                     elems_per_block=elems_per_block, gform=gform).c()
     check(lib().bk5_apply_ex(p, E, Dp, _ptr(G), _ptr(u), _ptr(mass), float(lam), _ptr(v), C.byref(o),
                              _stream(stream)), "bk5_apply")
+
+
+def g_to_ff(G, out=None, stream=None):
+    """The float-float pairs of a float64 device tensor G (bk_g_to_ff): a
+    tensor of G's shape and dtype float64 whose 8-byte values hold (float hi,
+    float lo); in place when out is G.  For bk5_apply(..., gform=G_FF)."""
+    if out is None:
+        out = G.new_empty(G.shape)
+    check(lib().bk_g_to_ff(_ptr(G), _ptr(out), G.numel(), _stream(stream)), "bk_g_to_ff")
+    return out
 
 
 def sum_factorization(bk: int, p: int, nelmt: int, *args, prec=PREC_FP64, **kw):

@@ -247,9 +247,9 @@ __device__ __forceinline__ void bk5_col_batch(const typename Eng::C* __restrict_
             if constexpr (HasSum3<Eng>::value) {
                 res = Eng::sum3(Eng::result(az), Eng::result(ax[k]), Eng::result(ay[k]));
             } else {
-                Eng::add(az, Eng::result(ax[k]));
-                Eng::add(az, Eng::result(ay[k]));
-                res = Eng::result(az);
+                Eng::add(az, Eng::loose(ax[k]));
+                Eng::add(az, Eng::loose(ay[k]));
+                res = Eng::loose(az);
             }
             if (mo != nullptr) {
                 // + lambda * mass * u at the point
@@ -258,7 +258,7 @@ __device__ __forceinline__ void bk5_col_batch(const typename Eng::C* __restrict_
                 V m = Eng::load(mo[k]);
                 if (lam_scaled) m = Eng::mul(lam, m);
                 Eng::vmadd(am, m, ucol[k]);
-                res = Eng::result(am);
+                res = Eng::loose(am);
             }
             vo[k] = Eng::store(res);
         }

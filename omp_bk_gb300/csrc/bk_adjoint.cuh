@@ -192,15 +192,15 @@ __global__ void __launch_bounds__(BK3AdjCfg<Eng, Q, EB, DPAR>::NT)
             Eng::vmadd(d, rs_, Eng::result(f1));
             Eng::vmadd(d, rt, Eng::result(f2));
             const long long o = (e0 + e) * Q3 + x;
-            dk[o] = Eng::store(Eng::result(d));
+            dk[o] = Eng::store(Eng::loose(d));
             // dL/dG
             S* go = dG + (e0 + e) * 6 * Q3 + x;
             const V kr = Eng::mul(kk, rr), ks_ = Eng::mul(kk, rs_), kt = Eng::mul(kk, rt);
-            auto prod = [&](V a, V b) { return Eng::result(Eng::vfirst(a, b)); };
+            auto prod = [&](V a, V b) { return Eng::loose(Eng::vfirst(a, b)); };
             auto prod2 = [&](V a, V b, V c, V dd) {
                 A t = Eng::vfirst(a, b);
                 Eng::vmadd(t, c, dd);
-                return Eng::result(t);
+                return Eng::loose(t);
             };
             go[0] = Eng::store(prod(kr, ur));
             go[Q3] = Eng::store(prod2(kr, us_, ks_, ur));

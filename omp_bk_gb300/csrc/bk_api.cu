@@ -132,6 +132,7 @@ bk_options bk_default_options(void)
     o.nfactors = 6;
     o.elems_per_block = 0;
     o.kernel = BK_KERNEL_AUTO;
+    o.gform = BK_G_STORAGE;
     return o;
 }
 
@@ -152,14 +153,23 @@ int bk5_apply_ex(int p, int64_t E, const double* D, const void* G, const void* u
     if (o.elems_per_block < 0 || o.elems_per_block > 64) return BK_ERR_ARG;
     const int eng = engine_of(o);
     if (eng < 0) return BK_ERR_PREC;
+    // G split ahead of time: the float-float engine (FP64, engine AUTO or FF),
+    // 6 factors, sweep kernel
+    if (o.gform != BK_G_STORAGE &&
+        (o.gform != BK_G_FF || eng != 1 || o.nfactors != 6 || o.kernel == BK_KERNEL_COLUMN))
+        return BK_ERR_PREC;
     if (E == 0) return BK_OK;
     if ((rc = status_or_null())) return rc;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     switch (eng) {
-        case 0: return launch_bk5_dfma(p, E, D, G, u, mass, lambda, v, o.nfactors, o.layout, o.elems_per_block, o.kernel, s);
-        case 1: return launch_bk5_ff(p, E, D, G, u, mass, lambda, v, o.nfactors, o.layout, o.elems_per_block, o.kernel, s);
-        case 2: return launch_bk5_f32(p, E, D, G, u, mass, lambda, v, o.nfactors, o.layout, o.elems_per_block, o.kernel, s);
-        default: return launch_bk5_mixed(p, E, D, G, u, mass, lambda, v, o.nfactors, o.layout, o.elems_per_block, o.kernel, s);
+        case 0: return launch_bk5_dfma(p, E, D, G, u, mass, lambda, v, o.nfactors, o.layout, o.elems_per_block, o.kernel,
+                                      o.gform, s);
+        case 1: return launch_bk5_ff(p, E, D, G, u, mass, lambda, v, o.nfactors, o.layout, o.elems_per_block, o.kernel,
+                                      o.gform, s);
+        case 2: return launch_bk5_f32(p, E, D, G, u, mass, lambda, v, o.nfactors, o.layout, o.elems_per_block, o.kernel,
+                                      o.gform, s);
+        default: return launch_bk5_mixed(p, E, D, G, u, mass, lambda, v, o.nfactors, o.layout, o.elems_per_block, o.kernel,
+                                      o.gform, s);
     }
 }
 

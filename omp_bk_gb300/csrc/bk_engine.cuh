@@ -34,6 +34,7 @@ struct EngDfma {
     __device__ static __forceinline__ void vmadd(A& acc, V a, V x) { acc = fma(a, x, acc); }
     __device__ static __forceinline__ void add(A& acc, V x) { acc += x; }
     __device__ static __forceinline__ V result(A acc) { return acc; }
+    __device__ static __forceinline__ V loose(A acc) { return acc; }
     __device__ static __forceinline__ V mul(V a, V b) { return a * b; }
     __device__ static __forceinline__ V vadd(V a, V b) { return a + b; }
     __device__ static __forceinline__ V vsub(V a, V b) { return a - b; }
@@ -54,6 +55,8 @@ struct EngFF {
     using A = ffacc;
     static constexpr int kId = BK_ENGINE_FF;
     __device__ static __forceinline__ V load(S x) { return split(x); }
+    // a value split ahead of time (bk_g_to_ff): no work
+    __device__ static __forceinline__ V load(ff2 x) { return ff{x.hi, x.lo}; }
     __device__ static __forceinline__ S store(V x) { return join(x); }
     __device__ static __forceinline__ A zero() { return acc_zero(); }
     // the first product needs no TwoSum into an empty accumulator
@@ -64,6 +67,8 @@ struct EngFF {
     __device__ static __forceinline__ void vmadd(A& acc, V a, V x) { acc_madd(acc, a, x); }
     __device__ static __forceinline__ void add(A& acc, V x) { acc_add(acc, x); }
     __device__ static __forceinline__ V result(A acc) { return acc_result(acc); }
+    // for values that are only summed or stored next: not renormalised
+    __device__ static __forceinline__ V loose(A acc) { return acc_loose(acc); }
     __device__ static __forceinline__ V mul(V a, V b) { return ff_mul(a, b); }
     __device__ static __forceinline__ V vadd(V a, V b) { return ff_add(a, b); }
     __device__ static __forceinline__ V vsub(V a, V b) { return ff_add(a, ff{-b.hi, -b.lo}); }
@@ -97,6 +102,7 @@ struct EngF32 {
     __device__ static __forceinline__ void vmadd(A& acc, V a, V x) { acc = fmaf(a, x, acc); }
     __device__ static __forceinline__ void add(A& acc, V x) { acc += x; }
     __device__ static __forceinline__ V result(A acc) { return acc; }
+    __device__ static __forceinline__ V loose(A acc) { return acc; }
     __device__ static __forceinline__ V mul(V a, V b) { return a * b; }
     __device__ static __forceinline__ V vadd(V a, V b) { return a + b; }
     __device__ static __forceinline__ V vsub(V a, V b) { return a - b; }

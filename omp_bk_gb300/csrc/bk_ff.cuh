@@ -39,6 +39,15 @@ struct ff {
 
 __device__ __forceinline__ ff ff_make(float hi, float lo) { return ff{hi, lo}; }
 
+// A float-float value stored in memory (8 bytes, 8-byte aligned so that it
+// moves as one 64-bit access): the form of a geometric-factor array that has
+// been split once ahead of the applies (bk_g_to_ff), in place of the split of
+// every binary64 value as it is loaded.
+struct alignas(8) ff2 {
+    float hi;
+    float lo;
+};
+
 // s + e == a + b exactly (Knuth's TwoSum).
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
 {
@@ -115,17 +124,27 @@ __device__ __forceinline__ ff acc_result(const ffacc& acc)
     return r;
 }
 
-// a * b, both float-float (the lo*lo term dropped), normalised.
+// a * b, both float-float (the lo*lo term dropped), as the unevaluated pair
+// p + pe (p the rounded hi product, pe its exact error plus the cross
+// terms), not renormalised: every consumer (multiply-adds, accumulators,
+// join) takes hi and lo separately.
 __device__ __forceinline__ ff ff_mul(const ff a, const ff b)
 {
     const float p = __fmul_rn(a.hi, b.hi);
     float pe = __fmaf_rn(a.hi, b.hi, -p);
     pe = __fmaf_rn(a.hi, b.lo, pe);
     pe = __fmaf_rn(a.lo, b.hi, pe);
-    ff r;
-    fast_two_sum(p, pe, r.hi, r.lo);
-    return r;
+    return ff{p, pe};
 }
+
+// The accumulated value as the unevaluated pair s + c, not renormalised
+// (after cancellation |c| may exceed |s|).  Only for values that are summed
+// or stored next, never multiplied: the FP32 rounding of a product with a
+// loose pair's lo part is an error relative to the magnitudes summed before
+// the cancellation (measured: 5e-12 relative on a strongly cancelling BK1
+// result), where a renormalised pair keeps 2^-48 of the value itself.
+// join() renormalises with TwoSum.
+__device__ __forceinline__ ff acc_loose(const ffacc& acc) { return ff{acc.s, acc.c}; }
 
 // a + b without the final renormalisation: hi = fl(a.hi + b.hi) and lo the
 // exact error of that sum plus the lo parts, so |lo| may reach a few ulp(hi).
@@ -141,7 +160,8 @@ __device__ __forceinline__ ff ff_add_loose(const ff a, const ff b)
 // a + b and b - a from two compensated accumulators, each renormalised once
 // with TwoSum (safe after cancellation, where the compensation may exceed
 // the sum) instead of normalising a and b first and then adding them: 28
-// flops for the pair instead of 34.
+// flops for the pair instead of 34.  The results feed further products, so
+// they are renormalised (see acc_loose).
 __device__ __forceinline__ void acc_sum_diff(const ffacc& a, const ffacc& b, ff& sum, ff& diff)
 {
     float s, e, t, f;
@@ -207,15 +227,16 @@ __device__ __forceinline__ ff split(const double x)
     return r;
 }
 
-// hi + lo rounded to the nearest double.  Fast path: the normalised hi has a
-// biased float exponent 53..254; lo becomes an integer count k of double ulps
-// of hi (|k| <= 2^28) added to hi's binary64 pattern.  When hi is a power of
-// two and lo points below it, the sum lies in the binade below, whose ulp is
-// half as large.
+// hi + lo rounded to the nearest double.  The pair is first renormalised
+// with TwoSum (it may be loose: |lo| > |hi| after cancellation).  Fast path:
+// the normalised hi has a biased float exponent 53..254; lo becomes an
+// integer count k of double ulps of hi (|k| <= 2^28) added to hi's binary64
+// pattern.  When hi is a power of two and lo points below it, the sum lies in
+// the binade below, whose ulp is half as large.
 __device__ __forceinline__ double join(const ff v)
 {
     float s, t;
-    fast_two_sum(v.hi, v.lo, s, t);
+    two_sum(v.hi, v.lo, s, t);
     const uint32_t sb = __float_as_uint(s);
     const uint32_t e8 = (sb >> 23) & 0xffu;
     if (e8 - 53u <= 254u - 53u) {

@@ -536,11 +536,12 @@ struct NoOp {
     __device__ __forceinline__ void operator()() const {}
 };
 
-template <class Eng, int Q, int F, int LAYOUT, bool EO, int DPAR = 0, class AfterPw = NoOp, bool DOT = false>
+template <class Eng, int Q, int F, int LAYOUT, bool EO, int DPAR = 0, class AfterPw = NoOp, bool DOT = false,
+          class GS = typename Eng::S>
 __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restrict__ Dp,
                                                 const EOMat<typename Eng::C, Q>& eo,
                                                 const EOMat<typename Eng::C, Q>& eot, const typename Eng::S* us,
-                                                const typename Eng::S* gs, typename Eng::V* W0, typename Eng::V* W1,
+                                                const GS* gs, typename Eng::V* W0, typename Eng::V* W1,
                                                 typename Eng::V* W2, typename Eng::V* W3, int ne, int tid, int nt,
                                                 typename Eng::S* __restrict__ vb,
                                                 const typename Eng::S* __restrict__ mb, double lambda,
@@ -600,7 +601,7 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
         }
         const int wi = e * WB::size + WB::at(i, j, k);
         const V qr = W0[wi], qs = W1[wi], qt = QT[wi];
-        const S* ge = gs + e * F * Q3;
+        const GS* ge = gs + e * F * Q3;
         auto g = [&](int f) { return Eng::load(ge[g_index<Eng, Q, F, LAYOUT>(i, j, f, k)]); };
         A r0, r1, r2;
         if (F == 6) {
@@ -664,7 +665,7 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
                 } else {
                     Eng::add(acc, W0[base + o]);
                     Eng::add(acc, W1[base + o]);
-                    res = Eng::result(acc);
+                    res = Eng::loose(acc);
                 }
                 W2[base + o] = res;
             }
@@ -693,7 +694,7 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
                     A acc = Eng::from(QT[wi]);
                     Eng::add(acc, W0[wi]);
                     Eng::add(acc, W1[wi]);
-                    res = Eng::result(acc);
+                    res = Eng::loose(acc);   // store() renormalises
                 }
             } else {
                 res = W2[wi];
@@ -716,10 +717,10 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
 // stops reading them (after the pointwise stage; after the last pass when a
 // mass term reads u there), so the copies overlap the transposed sweeps and
 // the last pass instead of stalling the block at the start of each batch.
-template <class Eng, int Q, int EB, int F, int LAYOUT, bool EO = false, int DPAR = 0>
+template <class Eng, int Q, int EB, int F, int LAYOUT, bool EO = false, int DPAR = 0, class GS = typename Eng::S>
 __global__ void __launch_bounds__(BK5Cfg<Eng, Q, EB, F, LAYOUT, DPAR>::NT)
     bk5_kernel(const __grid_constant__ P5<typename Eng::C, Q> prm, const long long E,
-               const typename Eng::S* __restrict__ u, const typename Eng::S* __restrict__ G,
+               const typename Eng::S* __restrict__ u, const GS* __restrict__ G,
                const typename Eng::S* __restrict__ mass, const double lambda, typename Eng::S* __restrict__ v,
                const DevCtx ctx)
 {
@@ -727,6 +728,7 @@ __global__ void __launch_bounds__(BK5Cfg<Eng, Q, EB, F, LAYOUT, DPAR>::NT)
     using S = typename Eng::S;
     using V = typename Eng::V;
     using WB = typename Cfg::WB;
+    static_assert(sizeof(GS) == sizeof(S), "G is staged in the footprint of the storage type");
     constexpr int Q3 = Cfg::Q3;
     extern __shared__ __align__(16) unsigned char smem[];
     V* W0 = reinterpret_cast<V*>(smem + Cfg::STAGE_BYTES);
@@ -745,7 +747,7 @@ __global__ void __launch_bounds__(BK5Cfg<Eng, Q, EB, F, LAYOUT, DPAR>::NT)
     const long long nbatch = (E + EB - 1) / EB;
     // where the staged batch's u and G landed
     const S* us = nullptr;
-    const S* gs = nullptr;
+    const GS* gs = nullptr;
     // 1. stage u and G of batch bt (every thread; thread 0 issues the TMA
     //    part and arrives)
     auto issue = [&](long long bt) {
@@ -754,7 +756,7 @@ __global__ void __launch_bounds__(BK5Cfg<Eng, Q, EB, F, LAYOUT, DPAR>::NT)
         uint32_t tx = 0;
         if (tid == 0) fence_proxy_async();
         us = stage_issue<S>(smem, u + e0 * Q3, ne * Q3, u + E * Q3, bar, tx, tid, nt);
-        gs = stage_issue<S>(smem + Cfg::U_BYTES, G + e0 * F * Q3, ne * F * Q3, G + E * F * Q3, bar, tx, tid, nt);
+        gs = stage_issue<GS>(smem + Cfg::U_BYTES, G + e0 * F * Q3, ne * F * Q3, G + E * F * Q3, bar, tx, tid, nt);
         if (tid == 0) mbar_arrive_expect_tx(bar, tx);
     };
     if (blockIdx.x < nbatch) issue(blockIdx.x);
@@ -766,7 +768,7 @@ __global__ void __launch_bounds__(BK5Cfg<Eng, Q, EB, F, LAYOUT, DPAR>::NT)
         const long long next = bt + gridDim.x;
         const S* mb = (mass != nullptr) ? mass + e0 * Q3 : nullptr;
         const S* ub = us;
-        const S* gb = gs;
+        const GS* gb = gs;
         auto early = [&]() {
             if (mass == nullptr && next < nbatch) issue(next);
         };

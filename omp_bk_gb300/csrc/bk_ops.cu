@@ -108,18 +108,20 @@ int grid_for(long long nbatch, int occ)
 
 #if BK_OP_TU == 5
 // One launch of bk5_kernel with the given shape.
-template <int Q, int EB, int F, int LAYOUT, bool EO, int DPAR>
+// GS: the type G is stored in (the storage type, or ff2 pairs split ahead of
+// time for the float-float engine).
+template <int Q, int EB, int F, int LAYOUT, bool EO, int DPAR, class GS = typename Eng::S>
 int bk5_launch(const P5<typename Eng::C, Q>& prm, long long E, const void* u, const void* G, const void* mass,
                double lambda, void* v, cudaStream_t s)
 {
     using Cfg = BK5Cfg<Eng, Q, EB, F, LAYOUT, DPAR>;
     using S = typename Eng::S;
     static_assert(Cfg::SMEM <= 232448, "BK5 block exceeds the shared memory of an SM");
-    auto kern = bk5_kernel<Eng, Q, EB, F, LAYOUT, EO, DPAR>;
+    auto kern = bk5_kernel<Eng, Q, EB, F, LAYOUT, EO, DPAR, GS>;
     const int occ = prepare<EoTag<Cfg, EO>>(kern, Cfg::SMEM, Cfg::NT);
     if (occ <= 0) return BK_ERR_CUDA;
     const int grid = grid_for((E + EB - 1) / EB, occ);
-    kern<<<grid, Cfg::NT, Cfg::SMEM, s>>>(prm, E, static_cast<const S*>(u), static_cast<const S*>(G),
+    kern<<<grid, Cfg::NT, Cfg::SMEM, s>>>(prm, E, static_cast<const S*>(u), static_cast<const GS*>(G),
                                           static_cast<const S*>(mass), lambda, static_cast<S*>(v), dev_ctx());
     return cudaGetLastError() == cudaSuccess ? BK_OK : BK_ERR_CUDA;
 }
@@ -143,7 +145,7 @@ constexpr int sweep_eb5_dpar(int q) { return q == 6 ? 4 : q == 7 ? 2 : q == 9 ? 
 
 template <int Q>
 int bk5_sweep_q(int F, const double* D, long long E, const void* u, const void* G, const void* mass,
-                double lambda, void* v, cudaStream_t s)
+                double lambda, void* v, int gform, cudaStream_t s)
 {
     constexpr int L = BK_LAYOUT_TU;
     P5<typename Eng::C, Q> prm;
@@ -155,8 +157,14 @@ int bk5_sweep_q(int F, const double* D, long long E, const void* u, const void* 
     if (eo) {
         constexpr int DP = sweep_dpar5(Q) ? 2 : 0;
         constexpr int EB = fit_eb5<Q, 6, DP ? sweep_eb5_dpar(Q) : sweep_eb5(Q), DP>();
+        if (gform == BK_G_FF) {
+            // G split ahead of time: the float-float engine's even-odd path
+            if constexpr (eng_is_ff()) return bk5_launch<Q, EB, 6, L, true, DP, ff2>(prm, E, u, G, mass, lambda, v, s);
+            return BK_ERR_PREC;
+        }
         return bk5_launch<Q, EB, 6, L, true, DP>(prm, E, u, G, mass, lambda, v, s);
     }
+    if (gform != BK_G_STORAGE) return BK_ERR_PREC;   // split G: even-odd D (GLL points), 6 factors
     if (F == 6) return bk5_launch<Q, fit_eb5<Q, 6, sweep_eb5(Q)>(), 6, L, false, 0>(prm, E, u, G, mass, lambda, v, s);
     if (F == 9) return bk5_launch<Q, fit_eb5<Q, 9, sweep_eb5(Q)>(), 9, L, false, 0>(prm, E, u, G, mass, lambda, v, s);
     return BK_ERR_PREC;
@@ -313,18 +321,18 @@ using namespace BK_TU_NS;
 #define BK_CATS_(a, b, c) a##_##b##_L##c
 #define BK_CATS(a, b, c) BK_CATS_(a, b, c)
 int BK_CATS(bk5_sweep, BK_SFX, BK_LAYOUT_TU)(int p, int F, const double* D, long long E, const void* u,
-                                              const void* G, const void* mass, double lambda, void* v,
+                                              const void* G, const void* mass, double lambda, void* v, int gform,
                                               cudaStream_t s)
 {
     switch (p + 1) {
-        case 2: return bk5_sweep_q<2>(F, D, E, u, G, mass, lambda, v, s);
-        case 3: return bk5_sweep_q<3>(F, D, E, u, G, mass, lambda, v, s);
-        case 4: return bk5_sweep_q<4>(F, D, E, u, G, mass, lambda, v, s);
-        case 5: return bk5_sweep_q<5>(F, D, E, u, G, mass, lambda, v, s);
-        case 6: return bk5_sweep_q<6>(F, D, E, u, G, mass, lambda, v, s);
-        case 7: return bk5_sweep_q<7>(F, D, E, u, G, mass, lambda, v, s);
-        case 8: return bk5_sweep_q<8>(F, D, E, u, G, mass, lambda, v, s);
-        case 9: return bk5_sweep_q<9>(F, D, E, u, G, mass, lambda, v, s);
+        case 2: return bk5_sweep_q<2>(F, D, E, u, G, mass, lambda, v, gform, s);
+        case 3: return bk5_sweep_q<3>(F, D, E, u, G, mass, lambda, v, gform, s);
+        case 4: return bk5_sweep_q<4>(F, D, E, u, G, mass, lambda, v, gform, s);
+        case 5: return bk5_sweep_q<5>(F, D, E, u, G, mass, lambda, v, gform, s);
+        case 6: return bk5_sweep_q<6>(F, D, E, u, G, mass, lambda, v, gform, s);
+        case 7: return bk5_sweep_q<7>(F, D, E, u, G, mass, lambda, v, gform, s);
+        case 8: return bk5_sweep_q<8>(F, D, E, u, G, mass, lambda, v, gform, s);
+        case 9: return bk5_sweep_q<9>(F, D, E, u, G, mass, lambda, v, gform, s);
         default: return BK_ERR_ORDER;
     }
 }
@@ -395,16 +403,18 @@ int BK_CAT(launch_bk3, BK_SFX)(int p, long long E, const double* B, const double
 #define BK_CATL(a, b, c) BK_CATL_(a, b, c)
 // BK5 dispatch: kernel shape and G layout
 int BK_CAT(launch_bk5, BK_SFX)(int p, long long E, const double* D, const void* G, const void* u, const void* mass,
-                                double lambda, void* v, int F, int layout, int eb, int kernel, cudaStream_t s)
+                                double lambda, void* v, int F, int layout, int eb, int kernel, int gform,
+                                cudaStream_t s)
 {
     if (p < 1 || p > 8) return BK_ERR_ORDER;
+    if (gform != BK_G_STORAGE && kernel == BK_KERNEL_COLUMN) return BK_ERR_PREC;   // sweep kernel only
     // AUTO: the sweep kernel, measured equal or faster than the column kernel
     // for every form at p = 7 (GB300)
     if (kernel == BK_KERNEL_SWEEP || kernel == BK_KERNEL_AUTO) {
         switch (layout) {
-            case 0: return BK_CATL(bk5_sweep, BK_SFX, 0)(p, F, D, E, u, G, mass, lambda, v, s);
-            case 1: return BK_CATL(bk5_sweep, BK_SFX, 1)(p, F, D, E, u, G, mass, lambda, v, s);
-            case 2: return BK_CATL(bk5_sweep, BK_SFX, 2)(p, F, D, E, u, G, mass, lambda, v, s);
+            case 0: return BK_CATL(bk5_sweep, BK_SFX, 0)(p, F, D, E, u, G, mass, lambda, v, gform, s);
+            case 1: return BK_CATL(bk5_sweep, BK_SFX, 1)(p, F, D, E, u, G, mass, lambda, v, gform, s);
+            case 2: return BK_CATL(bk5_sweep, BK_SFX, 2)(p, F, D, E, u, G, mass, lambda, v, gform, s);
             default: return BK_ERR_PREC;
         }
     }

@@ -16,6 +16,8 @@
 
 #include <cuda_runtime.h>
 
+#include "bk_ff.cuh"
+#include "bk_gpu.h"
 #include "bk_vec.h"
 
 namespace {
@@ -108,6 +110,17 @@ __global__ void axpby_kernel(long long n, double a, const T* __restrict__ x, dou
         y[i] = T(a * double(x[i]) + b * double(y[i]));
 }
 
+// G (binary64) -> float-float pairs, value by value (in place allowed): the
+// float-float engine's own split, so that an apply on the pairs is bitwise
+// the apply on the doubles.
+__global__ void g_to_ff_kernel(const double* G, bkg::ff2* out, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const bkg::ff v = bkg::split(G[i]);
+        out[i] = bkg::ff2{v.hi, v.lo};
+    }
+}
+
 int ok() { return cudaGetLastError() == cudaSuccess ? BK_OK : BK_ERR_CUDA; }
 
 int dot_blocks(long long n)
@@ -181,6 +194,17 @@ int bk_axpby(long long n, double a, const void* x, double b, void* y, int f64, b
         axpby_kernel<double><<<g, 256, 0, s>>>(n, a, static_cast<const double*>(x), b, static_cast<double*>(y));
     else
         axpby_kernel<float><<<g, 256, 0, s>>>(n, a, static_cast<const float*>(x), b, static_cast<float*>(y));
+    return ok();
+}
+
+int bk_g_to_ff(const void* G, void* Gff, int64_t n, bk_stream_t stream)
+{
+    if (n < 0) return BK_ERR_SIZE;
+    if (n == 0) return BK_OK;
+    if (!G || !Gff) return BK_ERR_NULL;
+    if ((reinterpret_cast<uintptr_t>(G) | reinterpret_cast<uintptr_t>(Gff)) & 15) return BK_ERR_ALIGN;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    g_to_ff_kernel<<<waves(n / 2 + 1), 256, 0, s>>>(static_cast<const double*>(G), static_cast<bkg::ff2*>(Gff), n);
     return ok();
 }
 

@@ -63,6 +63,16 @@ def test_host_argument_errors(bklib):
     assert L.bk5_apply_opt(3, 4, dp, a16, a16, a16, C.byref(o), None) == bklib.BK_ERR_PREC
     o = bklib.ApplyOptions(engine=9).c()
     assert L.bk5_apply_opt(3, 4, dp, a16, a16, a16, C.byref(o), None) == bklib.BK_ERR_PREC
+    # G split into float-float pairs: the float-float engine, 6 factors, sweep kernel
+    for kw in (dict(gform=2), dict(gform=bklib.G_FF, prec=bklib.PREC_MIXED),
+               dict(gform=bklib.G_FF, engine=bklib.ENGINE_DFMA), dict(gform=bklib.G_FF, nfactors=9),
+               dict(gform=bklib.G_FF, kernel=bklib.KERNEL_COLUMN)):
+        o = bklib.ApplyOptions(**kw).c()
+        assert L.bk5_apply_opt(3, 4, dp, a16, a16, a16, C.byref(o), None) == bklib.BK_ERR_PREC
+    assert L.bk_g_to_ff(a16, a16, -1, None) == bklib.BK_ERR_SIZE
+    assert L.bk_g_to_ff(None, a16, 4, None) == bklib.BK_ERR_NULL
+    assert L.bk_g_to_ff(a16, a8, 4, None) == bklib.BK_ERR_ALIGN
+    assert L.bk_g_to_ff(None, None, 0, None) == bklib.BK_OK
     # E = 0 is a no-op, even with null device pointers
     assert L.bk5_apply(3, 0, dp, None, None, None, 0, None) == bklib.BK_OK
     assert L.bk1_apply(8, 0, dp, None, None, None, 0, None) == bklib.BK_OK

@@ -294,3 +294,52 @@ def test_bk1_gll_gauss_even_odd(bklib, p, engine):
         tol = TOL32
     assert np.all(np.isfinite(out))
     assert oracle.rel_maxdiff(out, ref) < tol
+
+
+@pytest.mark.parametrize("p", P_ALL)
+@pytest.mark.parametrize("layout", [0, 1, 2])
+@pytest.mark.parametrize("with_mass", [False, True])
+def test_bk5_split_g_is_bitwise(bklib, p, layout, with_mass):
+    """G split once into float-float pairs (bk_g_to_ff) gives bitwise the
+    apply on the doubles: the pairs are the engine's own split of each value.
+    The conversion also runs in place."""
+    E = 13
+    nq = p + 1
+    D, _, _ = bklib.bk5_matrices(p)
+    rng = np.random.default_rng(300 + p)
+    u = dev(rng.uniform(-1, 1, E * nq ** 3), "f64")
+    g = dev(rng.uniform(0.5, 1.5, E * 6 * nq ** 3) * (1 + 1e-9 * rng.standard_normal(E * 6 * nq ** 3)), "f64")
+    mass = dev(rng.uniform(0.5, 1.5, E * nq ** 3), "f64") if with_mass else None
+    v0 = torch.empty_like(u)
+    v1 = torch.full_like(u, float("nan"))
+    bklib.bk5_apply(p, E, D, g, u, v0, layout=layout, mass=mass, lam=0.7 if with_mass else 0.0)
+    gff = bklib.g_to_ff(g)
+    bklib.bk5_apply(p, E, D, gff, u, v1, layout=layout, mass=mass, lam=0.7 if with_mass else 0.0,
+                    gform=bklib.G_FF)
+    g_in_place = g.clone()
+    bklib.g_to_ff(g_in_place, out=g_in_place)
+    torch.cuda.synchronize()
+    assert torch.equal(v0, v1)
+    assert torch.equal(g_in_place, gff)
+    # hi + lo is the double to 2^-48
+    pairs = gff.view(torch.float32).view(-1, 2).double()
+    assert torch.max(torch.abs(pairs[:, 0] + pairs[:, 1] - g) / torch.abs(g)).item() < 2.0 ** -47
+
+
+def test_bk5_split_g_unsupported(bklib):
+    """The split G form is for the float-float engine's even-odd sweep kernel
+    only: every other combination is rejected, none computes."""
+    p, E = 4, 3
+    nq = p + 1
+    D, _, _ = bklib.bk5_matrices(p)
+    g = torch.ones(E * 6 * nq ** 3, dtype=torch.float64, device="cuda")
+    u = torch.ones(E * nq ** 3, dtype=torch.float64, device="cuda")
+    v = torch.empty_like(u)
+    for kw in (dict(engine=bklib.ENGINE_DFMA), dict(prec=bklib.PREC_MIXED), dict(nfactors=9),
+               dict(kernel=bklib.KERNEL_COLUMN)):
+        with pytest.raises(bklib.BKError, match="precision"):
+            bklib.bk5_apply(p, E, D, g, u, v, gform=bklib.G_FF, **kw)
+    # a D that is not centro-antisymmetric has no even-odd form
+    Dn = np.random.default_rng(1).uniform(-1, 1, (nq, nq))
+    with pytest.raises(bklib.BKError, match="precision"):
+        bklib.bk5_apply(p, E, Dn, g, u, v, gform=bklib.G_FF)
