@@ -236,7 +236,7 @@ inline bool multi_eo_fill(EOSet<C>& P, int q, const double* d, Conv conv)
 // Bytes of one padded work box of eb elements of order q for values of vbytes.
 inline int multi_wbox_bytes(int q, int eb, int vbytes)
 {
-    return eb * q * box_ps(q, vbytes) * vbytes;
+    return eb * bk5_box(q, vbytes, 2) * vbytes;   // the element stride of WBox5
 }
 
 // Shared memory of the even-odd launch: u stage (followed by the mass stage,

@@ -59,6 +59,39 @@ struct WBox {
     __device__ static __forceinline__ int at(int i, int j, int k) { return i * PS + j * ZP + k; }
 };
 
+// The BK5 work box (the sweep kernel and the mixed-order Helmholtz kernel):
+// row stride, plane stride and element stride (values) per Q and value size,
+// each the minimum of a model of the warps' shared-memory wavefronts over
+// the box's access patterns (the dense walk of the load and last passes, the
+// pointwise walk in G's (k, i, j) order, and the thread-per-line sweeps of
+// the three directions, reads and writes), averaged over the elements per
+// block that occur.  For small Q a warp spans several elements, so the
+// element stride matters as much as the row and plane strides.  Model
+// wavefronts per access against the strides of WBox (1 = conflict-free):
+//   4-byte values, Q = 2..9: 1.20 1.56 1.46 1.57 1.56 1.39 1.39 1.21
+//                  (WBox:    2.48 2.19 2.00 1.95 2.03 1.77 1.39 1.84)
+//   8-byte values, Q = 2..9: 1.25 1.60 1.08 1.37 1.54 1.25 1.39 1.13
+//                  (WBox:    2.75 2.48 2.00 1.82 1.98 1.68 1.39 1.64)
+constexpr int bk5_box(int q, int vbytes, int what)   // what: 0 ZP, 1 PS, 2 element stride
+{
+    // {ZP, PS, element stride} for q = 2..9
+    constexpr int t4[8][3] = {{2, 16, 36}, {3, 9, 27}, {6, 24, 97}, {5, 25, 125},
+                              {6, 36, 216}, {7, 49, 349}, {9, 72, 576}, {9, 81, 729}};
+    constexpr int t8[8][3] = {{4, 8, 18}, {3, 9, 27}, {4, 19, 76}, {5, 25, 125},
+                              {9, 54, 324}, {7, 49, 343}, {9, 72, 576}, {9, 81, 737}};
+    return (q < 2 || q > 9) ? (what == 0 ? box_zp(q) : (what == 1 ? box_ps(q, vbytes) : q * box_ps(q, vbytes)))
+                            : (vbytes == 8 ? t8[q - 2][what] : t4[q - 2][what]);
+}
+
+template <int Q, class V>
+struct WBox5 {
+    static constexpr int ZP = bk5_box(Q, int(sizeof(V)), 0);
+    static constexpr int PS = bk5_box(Q, int(sizeof(V)), 1);
+    static constexpr int size = bk5_box(Q, int(sizeof(V)), 2);
+    static_assert((Q - 1) * ZP + Q <= PS && (Q - 1) * PS + PS <= size, "box strides overlap");
+    __device__ static __forceinline__ int at(int i, int j, int k) { return i * PS + j * ZP + k; }
+};
+
 // ---- staging -------------------------------------------------------------------
 
 // Shared-memory footprint (bytes) of a staged slice of n values of type S:
@@ -500,7 +533,7 @@ template <class Eng, int Q, int EB, int F, int LAYOUT, int DPAR = 0>
 struct BK5Cfg {
     using S = typename Eng::S;
     using V = typename Eng::V;
-    using WB = WBox<Q, V>;
+    using WB = WBox5<Q, V>;
     static constexpr int Q3 = Q * Q * Q;
     static constexpr int LINES = ((EB * Q * Q + 31) / 32) * 32;   // one direction, whole warps
     static constexpr int NT = DPAR ? 3 * LINES : (LINES < 64 ? 64 : LINES);
@@ -508,7 +541,7 @@ struct BK5Cfg {
     static constexpr int U_BYTES = stage_bytes<S>(EB * Q3);
     static constexpr int G_BYTES = stage_bytes<S>(EB * F * Q3);
     static constexpr int STAGE_BYTES = U_BYTES + G_BYTES;
-    static constexpr int W_BYTES = NBOX * EB * WB::size * int(sizeof(V));
+    static constexpr int W_BYTES = ((NBOX * EB * WB::size * int(sizeof(V)) + 15) / 16) * 16;
     static constexpr int SMEM = STAGE_BYTES + W_BYTES + 16;
 };
 
@@ -552,7 +585,7 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
     using S = typename Eng::S;
     using V = typename Eng::V;
     using A = typename Eng::A;
-    using WB = WBox<Q, V>;
+    using WB = WBox5<Q, V>;
     constexpr int Q3 = Q * Q * Q;
     const Mat<typename Eng::C, Q, false> Dm{Dp};   // D(i, n)
     const Mat<typename Eng::C, Q, true> Dt{Dp};    // D(n, i)
@@ -714,8 +747,8 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
 
 // The block walks batches bt = blockIdx.x, + gridDim.x, ...  One stage buffer:
 // the next batch's u and G are copied into it as soon as the current batch
-// stops reading them (after the pointwise stage; after the last pass when a
-// mass term reads u there), so the copies overlap the transposed sweeps and
+// stops reading them (after the pointwise stage; u after the last pass when a
+// mass term reads it there), so the copies overlap the transposed sweeps and
 // the last pass instead of stalling the block at the start of each batch.
 template <class Eng, int Q, int EB, int F, int LAYOUT, bool EO = false, int DPAR = 0, class GS = typename Eng::S>
 __global__ void __launch_bounds__(BK5Cfg<Eng, Q, EB, F, LAYOUT, DPAR>::NT)
@@ -735,7 +768,7 @@ __global__ void __launch_bounds__(BK5Cfg<Eng, Q, EB, F, LAYOUT, DPAR>::NT)
     V* W1 = W0 + EB * WB::size;
     V* W2 = W1 + EB * WB::size;
     V* W3 = DPAR ? W2 + EB * WB::size : nullptr;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(reinterpret_cast<unsigned char*>(W0 + Cfg::NBOX * EB * WB::size));
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + Cfg::STAGE_BYTES + Cfg::W_BYTES);
     const int tid = threadIdx.x;
     const int nt = Cfg::NT;
 
@@ -748,18 +781,29 @@ __global__ void __launch_bounds__(BK5Cfg<Eng, Q, EB, F, LAYOUT, DPAR>::NT)
     // where the staged batch's u and G landed
     const S* us = nullptr;
     const GS* gs = nullptr;
-    // 1. stage u and G of batch bt (every thread; thread 0 issues the TMA
-    //    part and arrives)
-    auto issue = [&](long long bt) {
+    // 1. stage G (every thread; thread 0 issues the TMA part and adds its
+    //    bytes to the phase without arriving), then u (thread 0 arrives):
+    //    batch bt's phase completes when both have landed
+    auto issue_g = [&](long long bt) {
+        const long long e0 = bt * EB;
+        const int ne = int((E - e0) < EB ? (E - e0) : EB);
+        uint32_t tx = 0;
+        if (tid == 0) fence_proxy_async();
+        gs = stage_issue<GS>(smem + Cfg::U_BYTES, G + e0 * F * Q3, ne * F * Q3, G + E * F * Q3, bar, tx, tid, nt);
+        if (tid == 0) mbar_expect_tx(bar, tx);
+    };
+    auto issue_u = [&](long long bt) {
         const long long e0 = bt * EB;
         const int ne = int((E - e0) < EB ? (E - e0) : EB);
         uint32_t tx = 0;
         if (tid == 0) fence_proxy_async();
         us = stage_issue<S>(smem, u + e0 * Q3, ne * Q3, u + E * Q3, bar, tx, tid, nt);
-        gs = stage_issue<GS>(smem + Cfg::U_BYTES, G + e0 * F * Q3, ne * F * Q3, G + E * F * Q3, bar, tx, tid, nt);
         if (tid == 0) mbar_arrive_expect_tx(bar, tx);
     };
-    if (blockIdx.x < nbatch) issue(blockIdx.x);
+    if (blockIdx.x < nbatch) {
+        issue_g(blockIdx.x);
+        issue_u(blockIdx.x);
+    }
     uint32_t phase = 0;
     for (long long bt = blockIdx.x; bt < nbatch; bt += gridDim.x, phase ^= 1u) {
         if (batch_wait_failed(bar, phase, ctx, tid)) return;
@@ -769,12 +813,18 @@ __global__ void __launch_bounds__(BK5Cfg<Eng, Q, EB, F, LAYOUT, DPAR>::NT)
         const S* mb = (mass != nullptr) ? mass + e0 * Q3 : nullptr;
         const S* ub = us;
         const GS* gb = gs;
+        // after the pointwise stage the G stage is free, and the u stage too
+        // unless the mass term reads u in the last pass (then u follows the
+        // batch)
         auto early = [&]() {
-            if (mass == nullptr && next < nbatch) issue(next);
+            if (next < nbatch) {
+                issue_g(next);
+                if (mass == nullptr) issue_u(next);
+            }
         };
         bk5_sweep_batch<Eng, Q, F, LAYOUT, EO, DPAR>(prm.D, prm.eo, prm.eot, ub, gb, W0, W1, W2, W3, ne, tid, nt,
                                                      v + e0 * Q3, mb, lambda, nullptr, early);
-        if (mass != nullptr && next < nbatch) issue(next);
+        if (mass != nullptr && next < nbatch) issue_u(next);
     }
 }
 
