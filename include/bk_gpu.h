@@ -100,10 +100,10 @@ typedef struct bk_options {
                             sweep kernels use per-order tables measured on
                             GB300 and ignore it */
     int kernel;    /* bk_kernel_shape (BK5); BK1/BK3 have the sweep kernel only */
-    int gform;     /* bk_gform (BK5): how G is stored */
+    int gform;     /* bk_gform (BK5, BK3): how G is stored */
 } bk_options;
 
-/* BK5 geometric-factor storage forms. */
+/* Geometric-factor storage forms (BK5, BK3). */
 enum bk_gform {
     BK_G_STORAGE = 0, /* the storage type of prec (double for FP64) */
     BK_G_FF = 1       /* float-float pairs (float hi, float lo; 8 bytes per
@@ -112,14 +112,18 @@ enum bk_gform {
                          split of every G value it loads.  The pair is the
                          split the engine applies to a double, so the apply's
                          result is bitwise that of the double G.  FP64 with
-                         engine AUTO or FF, 6 factors, a D on points symmetric
-                         about 0 (GLL), sweep kernel; otherwise BK_ERR_PREC */
+                         engine AUTO or FF and the even-odd path: BK5 with 6
+                         factors, D on points symmetric about 0 (GLL), sweep
+                         kernel; BK3 with B and D of GLL nodes and Gauss
+                         points.  Otherwise (and for BK1 and the adjoint,
+                         which take no split G) BK_ERR_PREC */
 };
 
 /* BK5 kernel shapes. */
 enum bk_kernel_shape {
-    BK_KERNEL_AUTO = 0,   /* the faster of the two as measured on GB300 (the
-                             sweep kernel at p = 7 for every form) */
+    BK_KERNEL_AUTO = 0,   /* the faster of the two as measured on GB300: the
+                             column kernel for the FP32-storage forms at
+                             p <= 6, the sweep kernel otherwise */
     BK_KERNEL_SWEEP = 1,  /* one thread per line of the box per 1-D contraction,
                              all intermediates in shared memory */
     BK_KERNEL_COLUMN = 2  /* one thread per k-column of an element, the

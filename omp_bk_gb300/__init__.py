@@ -188,13 +188,14 @@ def bk1_apply(p, E, B, qdata, u, v, prec=PREC_FP64, engine=ENGINE_AUTO, stream=N
     check(lib().bk1_apply_opt(p, E, Bp, _ptr(qdata), _ptr(u), _ptr(v), C.byref(o), _stream(stream)), "bk1_apply")
 
 
-def bk3_apply(p, E, B, D, G, u, v, k=None, prec=PREC_FP64, engine=ENGINE_AUTO, stream=None):
+def bk3_apply(p, E, B, D, G, u, v, k=None, prec=PREC_FP64, engine=ENGINE_AUTO, gform=G_STORAGE, stream=None):
     """v = B^T D^T (k) G D B u per element (openmp/bk3_sumfact.h:17-187); G
-    factor-major, k an optional coefficient at the quadrature points."""
+    factor-major, k an optional coefficient at the quadrature points.
+    gform=G_FF: G holds the float-float pairs made by g_to_ff."""
     _order(p, "bk3_apply")
     Bh, Bp = _host(B)
     Dh, Dp = _host(D)
-    o = ApplyOptions(prec=prec, engine=engine).c()
+    o = ApplyOptions(prec=prec, engine=engine, gform=gform).c()
     check(lib().bk3_apply_k(p, E, Bp, Dp, _ptr(G), _ptr(k), _ptr(u), _ptr(v), C.byref(o), _stream(stream)),
           "bk3_apply")
 

@@ -1,0 +1,175 @@
+"""Shared-memory wavefront model of the sweep kernels' work boxes, and the
+search that chose their strides (the tables bk5_box and bk3_box in
+csrc/bk_kernels.cuh).
+
+A work box holds one element's values at i * PS + j * ZP + k (row stride ZP,
+plane stride PS) and consecutive elements ES values apart.  The kernels walk
+the box in a few fixed ways, 32 consecutive work items per warp:
+
+  dense      (i, j, k), k fastest: the load of u, the last pass, the store;
+  pointwise  G's (k, i, j) order (BK5 layout 2) or the dense order (BK3);
+  sweeps     one thread per line of a direction, all lines of the block's
+             elements in turn; each reads its NI inputs and writes its NO
+             outputs at base + n * stride.
+
+A warp instruction on 4-byte values costs the largest number of distinct
+words any of the 32 banks is asked for; on 8-byte values each half warp is
+one pass over 16 bank pairs.  The score of a box is the weighted mean of
+wavefronts per access over the walks of one batch, divided by the
+conflict-free count (1 for 4-byte values, 2 for full 8-byte warps): 1.0 is
+conflict-free.  For small Q a warp spans several elements, so the element
+stride ES matters as much as ZP and PS.
+
+    python -m omp_bk_gb300.box_model --op 5 --vbytes 4        # search, prints the table rows
+"""
+from __future__ import annotations
+
+import argparse
+
+
+def wavefronts(addrs, vbytes: int) -> int:
+    """Wavefronts of one warp access to the value indices `addrs` (None =
+    inactive lane)."""
+    if vbytes == 4:
+        banks: dict = {}
+        for a in addrs:
+            if a is not None:
+                banks.setdefault(a % 32, set()).add(a)
+        return max((len(s) for s in banks.values()), default=0)
+    total = 0
+    for half in (addrs[:16], addrs[16:]):
+        banks = {}
+        for a in half:
+            if a is not None:
+                banks.setdefault(a % 16, set()).add(a)
+        total += max((len(s) for s in banks.values()), default=0)
+    return total
+
+
+def _warps(n: int, f):
+    return [[f(w) if w < n else None for w in range(w0, w0 + 32)] for w0 in range(0, n, 32)]
+
+
+def _dense(X, Y, Z, eb, zp, ps, es):
+    n = X * Y * Z
+
+    def f(w):
+        e, x = divmod(w, n)
+        i, r = divmod(x, Y * Z)
+        j, k = divmod(r, Z)
+        return e * es + i * ps + j * zp + k
+    return _warps(eb * n, f)
+
+
+def _kij(Q, eb, zp, ps, es):
+    def f(w):
+        e, x = divmod(w, Q ** 3)
+        k, r = divmod(x, Q * Q)
+        i, j = divmod(r, Q)
+        return e * es + i * ps + j * zp + k
+    return _warps(eb * Q ** 3, f)
+
+
+def _sweep(X, Y, Z, d, NO, eb, zp, ps, es):
+    """Accesses of a sweep along direction d of an (X, Y, Z) box into extent
+    NO (the line enumeration of sweep / sweep_eo / sweep_eor)."""
+    NI = (X, Y, Z)[d]
+    LB = Y if d == 2 else Z
+    L = X * Y * Z // NI
+    sd = ps if d == 0 else (zp if d == 1 else 1)
+    out = []
+    for n in list(range(NI)) + list(range(NO)):
+        def f(w, n=n):
+            e, l = divmod(w, L)
+            a, b = divmod(l, LB)
+            base = (a * zp + b) if d == 0 else ((a * ps + b) if d == 1 else (a * ps + b * zp))
+            return e * es + base + n * sd
+        out += _warps(eb * L, f)
+    return out
+
+
+def walks(op: int, Q: int, eb: int, zp: int, ps: int, es: int):
+    """(weight, warps) of one batch of eb elements.  op 5: BK5 (Q points);
+    op 3: BK3 (P = Q - 1 nodes, Q points)."""
+    if op == 5:
+        yield 4, _dense(Q, Q, Q, eb, zp, ps, es)         # load u, last pass (3 reads)
+        yield 6, _kij(Q, eb, zp, ps, es)                 # pointwise: 3 reads, 3 writes
+        for d in range(3):                               # gradient and transposed
+            yield 1, _sweep(Q, Q, Q, d, Q, eb, zp, ps, es)
+            yield 1, _sweep(Q, Q, Q, d, Q, eb, zp, ps, es)
+        return
+    P = Q - 1
+    yield 2, _dense(P, P, P, eb, zp, ps, es)             # load u, store v
+    for _ in range(2):                                   # interpolation and its transpose
+        yield 1, _sweep(P, P, P, 0, Q, eb, zp, ps, es)
+        yield 1, _sweep(Q, P, P, 1, Q, eb, zp, ps, es)
+        yield 1, _sweep(Q, Q, P, 2, Q, eb, zp, ps, es)
+    for d in range(3):
+        yield 2, _sweep(Q, Q, Q, d, Q, eb, zp, ps, es)
+    yield 6, _dense(Q, Q, Q, eb, zp, ps, es)             # pointwise
+
+
+def score(op: int, Q: int, eb: int, vbytes: int, zp: int, ps: int, es: int) -> float:
+    ideal = 1 if vbytes == 4 else 2
+    tot = norm = 0.0
+    for wgt, ws in walks(op, Q, eb, zp, ps, es):
+        for a in ws:
+            act = sum(x is not None for x in a)
+            if act == 0:
+                continue
+            tot += wgt * wavefronts(a, vbytes)
+            norm += wgt * (ideal if (vbytes == 4 or act > 16) else 1)
+    return tot / norm
+
+
+def legacy(Q: int, vbytes: int):
+    """The first strides (ZP, PS, ES): odd rows, plane stride 8 mod 16 / 32."""
+    zp = Q + 1 if Q % 2 == 0 else Q
+    if vbytes == 8:
+        ps = Q * zp if (Q * zp) % 16 == 8 else Q * zp + ((24 - (Q * zp) % 16) % 16)
+    else:
+        ps = Q * zp if (Q * zp) % 32 == 8 else Q * zp + ((40 - (Q * zp) % 32) % 32)
+    return zp, ps, Q * ps
+
+
+# elements per block that occur (sweep kernel tables and the Helmholtz tiles)
+EBS = {
+    (5, 4): {2: [12], 3: [12, 17], 4: [8, 10], 5: [4, 6], 6: [3, 4], 7: [2, 3], 8: [1, 2], 9: [1]},
+    (5, 8): {2: [16], 3: [16, 14], 4: [8], 5: [4, 5], 6: [4, 3], 7: [2], 8: [2, 1], 9: [3, 1]},
+    (3, 4): {3: [16], 4: [8], 5: [6], 6: [4], 7: [3], 8: [1], 9: [1], 10: [1]},
+    (3, 8): {3: [12], 4: [8], 5: [8], 6: [3], 7: [3], 8: [1], 9: [3], 10: [1]},
+}
+
+
+def mean_score(op, Q, vbytes, zp, ps, es):
+    ebs = EBS[(op, vbytes)][Q]
+    return sum(score(op, Q, eb, vbytes, zp, ps, es) for eb in ebs) / len(ebs)
+
+
+def search(op: int, Q: int, vbytes: int):
+    """The strides with the lowest mean score (ties: the smaller box)."""
+    best = None
+    for zp in range(Q, Q + 4):
+        for ps in range(Q * zp, Q * zp + 33):
+            for pad in range(0, 33):
+                s = round(mean_score(op, Q, vbytes, zp, ps, Q * ps + pad), 3)
+                key = (s, Q * ps + pad)
+                if best is None or key < best[0]:
+                    best = (key, zp, ps, Q * ps + pad)
+    return best[1], best[2], best[3], best[0][0]
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("--op", type=int, choices=(3, 5), default=5)
+    ap.add_argument("--vbytes", type=int, choices=(4, 8), default=4)
+    args = ap.parse_args(argv)
+    for Q in sorted(EBS[(args.op, args.vbytes)]):
+        zp, ps, es, s = search(args.op, Q, args.vbytes)
+        lz, lp, le = legacy(Q, args.vbytes)
+        print(f"Q={Q}: {{{zp}, {ps}, {es}}}  score {s:.2f}  (first strides {lz},{lp},{le}: "
+              f"{mean_score(args.op, Q, args.vbytes, lz, lp, le):.2f})", flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -22,7 +22,7 @@ template <class Eng, int Q, int EB, int DPAR = 0>
 struct BK3AdjCfg {
     using S = typename Eng::S;
     using V = typename Eng::V;
-    using WB = WBox<Q, V>;
+    using WB = WBox3<Q, V>;
     static constexpr int P = Q - 1;
     static constexpr int Q3 = Q * Q * Q;
     static constexpr int P3 = P * P * P;
@@ -32,7 +32,7 @@ struct BK3AdjCfg {
     static constexpr int U_BYTES = stage_bytes<S>(EB * P3);
     static constexpr int G_BYTES = stage_bytes<S>(EB * 6 * Q3);
     static constexpr int K_BYTES = stage_bytes<S>(EB * Q3);
-    static constexpr int W_BYTES = NBOX * EB * WB::size * int(sizeof(V));
+    static constexpr int W_BYTES = ((NBOX * EB * WB::size * int(sizeof(V)) + 15) / 16) * 16;
     static constexpr int SMEM = 2 * U_BYTES + G_BYTES + K_BYTES + W_BYTES + 16;
 };
 
@@ -116,7 +116,7 @@ __global__ void __launch_bounds__(BK3AdjCfg<Eng, Q, EB, DPAR>::NT)
     V* W4 = W3 + EB * WB::size;
     V* W5 = W4 + EB * WB::size;
     V* W6 = DPAR ? W5 + EB * WB::size : W0;   // the third component of g_res
-    uint64_t* bar = reinterpret_cast<uint64_t*>(reinterpret_cast<unsigned char*>(W0 + Cfg::NBOX * EB * WB::size));
+    uint64_t* bar = reinterpret_cast<uint64_t*>(kstage + Cfg::K_BYTES + Cfg::W_BYTES);
     const int tid = threadIdx.x;
     const int nt = Cfg::NT;
 

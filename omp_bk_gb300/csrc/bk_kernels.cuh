@@ -37,11 +37,12 @@ constexpr int kMaxQ = 10;
 
 // ---- padded work boxes ---------------------------------------------------------
 
-// Row and plane strides of a Q x Q x Q work box of `vbytes`-byte values.
-// Rows of odd length in 8-byte words (or in 4-byte words) keep the
-// contiguous lines of direction 2 on distinct banks; the plane stride is
-// chosen so that the lines of direction 1 (which differ in the plane index)
-// split evenly across the banks.
+// The first strides of a Q x Q x Q work box of `vbytes`-byte values (now
+// the fallback outside the tables below and the baseline the tables are
+// scored against): rows of odd length keep the contiguous lines of
+// direction 2 on distinct banks; the plane stride is chosen so that the
+// lines of direction 1 split evenly across the banks; elements Q planes
+// apart.
 constexpr int box_zp(int q) { return (q % 2 == 0) ? q + 1 : q; }
 constexpr int box_ps(int q, int vbytes)
 {
@@ -51,37 +52,62 @@ constexpr int box_ps(int q, int vbytes)
                          : ((q * box_zp(q)) % 32 == 8 ? q * box_zp(q) : q * box_zp(q) + ((40 - (q * box_zp(q)) % 32) % 32));
 }
 
-template <int Q, class V>
-struct WBox {
-    static constexpr int ZP = box_zp(Q);
-    static constexpr int PS = box_ps(Q, int(sizeof(V)));
-    static constexpr int size = Q * PS;   // values per element (padded)
-    __device__ static __forceinline__ int at(int i, int j, int k) { return i * PS + j * ZP + k; }
-};
-
 // The BK5 work box (the sweep kernel and the mixed-order Helmholtz kernel):
 // row stride, plane stride and element stride (values) per Q and value size,
 // each the minimum of a model of the warps' shared-memory wavefronts over
 // the box's access patterns (the dense walk of the load and last passes, the
 // pointwise walk in G's (k, i, j) order, and the thread-per-line sweeps of
 // the three directions, reads and writes), averaged over the elements per
-// block that occur.  For small Q a warp spans several elements, so the
-// element stride matters as much as the row and plane strides.  Model
-// wavefronts per access against the strides of WBox (1 = conflict-free):
-//   4-byte values, Q = 2..9: 1.20 1.56 1.46 1.57 1.56 1.39 1.39 1.21
-//                  (WBox:    2.48 2.19 2.00 1.95 2.03 1.77 1.39 1.84)
-//   8-byte values, Q = 2..9: 1.25 1.60 1.08 1.37 1.54 1.25 1.39 1.13
-//                  (WBox:    2.75 2.48 2.00 1.82 1.98 1.68 1.39 1.64)
+// block that occur (omp_bk_gb300/box_model.py, --op 5).  For small Q a warp
+// spans several elements, so the element stride matters as much as the row
+// and plane strides.  Model wavefronts per access (1 = conflict-free)
+// against the first strides (box_zp, box_ps):
+//   4-byte values, Q = 2..9: 1.21 1.57 1.54 1.56 1.65 1.53 1.36 1.22
+//                   (first:  2.62 2.27 2.00 1.90 1.92 1.70 1.36 1.75)
+//   8-byte values, Q = 2..9: 1.36 1.62 1.18 1.41 1.44 1.43 1.36 1.23
+//                   (first:  3.09 2.55 2.00 1.80 1.96 1.65 1.36 1.62)
 constexpr int bk5_box(int q, int vbytes, int what)   // what: 0 ZP, 1 PS, 2 element stride
 {
     // {ZP, PS, element stride} for q = 2..9
     constexpr int t4[8][3] = {{2, 16, 36}, {3, 9, 27}, {6, 24, 97}, {5, 25, 125},
-                              {6, 36, 216}, {7, 49, 349}, {9, 72, 576}, {9, 81, 729}};
+                              {7, 42, 252}, {7, 49, 343}, {9, 72, 576}, {9, 81, 729}};
     constexpr int t8[8][3] = {{4, 8, 18}, {3, 9, 27}, {4, 19, 76}, {5, 25, 125},
                               {9, 54, 324}, {7, 49, 343}, {9, 72, 576}, {9, 81, 737}};
     return (q < 2 || q > 9) ? (what == 0 ? box_zp(q) : (what == 1 ? box_ps(q, vbytes) : q * box_ps(q, vbytes)))
                             : (vbytes == 8 ? t8[q - 2][what] : t4[q - 2][what]);
 }
+
+// The work box of BK1, BK3 and the BK3 adjoint (P = Q - 1 nodes, Q points):
+// the same model over their walks (the dense P^3 load and store, the
+// interpolation sweeps through the (Q,P,P) and (Q,Q,P) boxes and back, the
+// gradient sweeps and the dense pointwise walk; box_model.py --op 3).  At
+// 4-byte Q = 8 the model ties the first strides with {8, 71, 568}; the
+// first strides measured faster (BK3 p=6 mixed 87.6 against 83.0 GDoF/s)
+// and are kept.  Model wavefronts per access, Q = 3..10, against the first
+// strides:
+//   4-byte values: 1.45 1.55 1.48 1.67 1.64 1.49 1.31 1.48
+//                 (2.49 2.21 1.96 1.86 1.73 1.49 1.61 1.81)
+//   8-byte values: 1.44 1.25 1.43 1.58 1.58 1.55 1.40 1.47
+//                 (2.51 2.08 1.81 1.90 1.69 1.55 1.58 1.90)
+constexpr int bk3_box(int q, int vbytes, int what)   // what: 0 ZP, 1 PS, 2 element stride
+{
+    // {ZP, PS, element stride} for q = 3..10
+    constexpr int b4[8][3] = {{3, 9, 27}, {4, 19, 80}, {5, 25, 125}, {6, 36, 216},
+                              {7, 49, 343}, {9, 72, 576}, {9, 81, 729}, {10, 105, 1050}};
+    constexpr int b8[8][3] = {{3, 9, 27}, {4, 19, 76}, {5, 25, 125}, {9, 54, 324},
+                              {7, 54, 385}, {9, 72, 576}, {9, 81, 729}, {10, 105, 1050}};
+    return (q < 3 || q > 10) ? (what == 0 ? box_zp(q) : (what == 1 ? box_ps(q, vbytes) : q * box_ps(q, vbytes)))
+                             : (vbytes == 8 ? b8[q - 3][what] : b4[q - 3][what]);
+}
+
+template <int Q, class V>
+struct WBox3 {
+    static constexpr int ZP = bk3_box(Q, int(sizeof(V)), 0);
+    static constexpr int PS = bk3_box(Q, int(sizeof(V)), 1);
+    static constexpr int size = bk3_box(Q, int(sizeof(V)), 2);
+    static_assert((Q - 1) * ZP + Q <= PS && (Q - 1) * PS + PS <= size, "box strides overlap");
+    __device__ static __forceinline__ int at(int i, int j, int k) { return i * PS + j * ZP + k; }
+};
 
 template <int Q, class V>
 struct WBox5 {
@@ -834,14 +860,14 @@ template <class Eng, int Q, int EB>
 struct BK1Cfg {
     using S = typename Eng::S;
     using V = typename Eng::V;
-    using WB = WBox<Q, V>;
+    using WB = WBox3<Q, V>;
     static constexpr int P = Q - 1;
     static constexpr int Q3 = Q * Q * Q;
     static constexpr int P3 = P * P * P;
     static constexpr int NT = ((EB * Q * Q + 31) / 32) * 32 < 64 ? 64 : ((EB * Q * Q + 31) / 32) * 32;
     static constexpr int U_BYTES = stage_bytes<S>(EB * Q3);   // also holds the P^3 output
     static constexpr int J_BYTES = stage_bytes<S>(EB * Q3);
-    static constexpr int W_BYTES = 2 * EB * WB::size * int(sizeof(V));
+    static constexpr int W_BYTES = ((2 * EB * WB::size * int(sizeof(V)) + 15) / 16) * 16;
     static constexpr int SMEM = U_BYTES + J_BYTES + W_BYTES + 16;
 };
 
@@ -861,7 +887,7 @@ __global__ void __launch_bounds__(BK1Cfg<Eng, Q, EB>::NT)
     unsigned char* jstage = ustage + Cfg::U_BYTES;
     V* W0 = reinterpret_cast<V*>(jstage + Cfg::J_BYTES);
     V* W1 = W0 + EB * WB::size;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(reinterpret_cast<unsigned char*>(W1 + EB * WB::size));
+    uint64_t* bar = reinterpret_cast<uint64_t*>(jstage + Cfg::J_BYTES + Cfg::W_BYTES);
     const int tid = threadIdx.x;
     const int nt = Cfg::NT;
     // interpolation out(p) = sum_i in(i) B(i, p): M(o=p, n=i) = B[i*Q + p]
@@ -948,7 +974,7 @@ template <class Eng, int Q, int EB, int DPAR = 0>
 struct BK3Cfg {
     using S = typename Eng::S;
     using V = typename Eng::V;
-    using WB = WBox<Q, V>;
+    using WB = WBox3<Q, V>;
     static constexpr int P = Q - 1;
     static constexpr int Q3 = Q * Q * Q;
     static constexpr int P3 = P * P * P;
@@ -957,19 +983,20 @@ struct BK3Cfg {
     static constexpr int U_BYTES = stage_bytes<S>(EB * P3);
     static constexpr int G_BYTES = stage_bytes<S>(EB * 6 * Q3);
     static constexpr int K_BYTES = stage_bytes<S>(EB * Q3);
-    static constexpr int W_BYTES = 4 * EB * WB::size * int(sizeof(V));
+    static constexpr int W_BYTES = ((4 * EB * WB::size * int(sizeof(V)) + 15) / 16) * 16;
     static constexpr int SMEM = U_BYTES + G_BYTES + K_BYTES + W_BYTES + 16;
 };
 
-template <class Eng, int Q, int EB, bool EO = false, int DPAR = 0>
+template <class Eng, int Q, int EB, bool EO = false, int DPAR = 0, class GS = typename Eng::S>
 __global__ void __launch_bounds__(BK3Cfg<Eng, Q, EB, DPAR>::NT)
     bk3_kernel(const __grid_constant__ P13<typename Eng::C, Q> prm, const long long E,
-               const typename Eng::S* __restrict__ u, const typename Eng::S* __restrict__ G,
+               const typename Eng::S* __restrict__ u, const GS* __restrict__ G,
                const typename Eng::S* __restrict__ kq, typename Eng::S* __restrict__ v, const DevCtx ctx)
 {
     static_assert(!DPAR || EO, "direction-parallel sweeps need the even-odd form");
     using Cfg = BK3Cfg<Eng, Q, EB, DPAR>;
     using S = typename Eng::S;
+    static_assert(sizeof(GS) == sizeof(S), "G is staged in the footprint of the storage type");
     using V = typename Eng::V;
     using A = typename Eng::A;
     using WB = typename Cfg::WB;
@@ -982,7 +1009,7 @@ __global__ void __launch_bounds__(BK3Cfg<Eng, Q, EB, DPAR>::NT)
     V* W1 = W0 + EB * WB::size;
     V* W2 = W1 + EB * WB::size;
     V* W3 = W2 + EB * WB::size;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(reinterpret_cast<unsigned char*>(W3 + EB * WB::size));
+    uint64_t* bar = reinterpret_cast<uint64_t*>(kstage + Cfg::K_BYTES + Cfg::W_BYTES);
     const int tid = threadIdx.x;
     const int nt = Cfg::NT;
     const Mat<typename Eng::C, Q, true> Bi{prm.B};    // M(p, i) = B[i*Q + p]
@@ -1001,7 +1028,7 @@ __global__ void __launch_bounds__(BK3Cfg<Eng, Q, EB, DPAR>::NT)
     // pointwise stage has read the stage, so its copies overlap the
     // transposed sweeps.
     const S* us = nullptr;
-    const S* gs = nullptr;
+    const GS* gs = nullptr;
     const S* ks = nullptr;
     auto issue = [&](long long bt) {
         const long long e0 = bt * EB;
@@ -1009,7 +1036,7 @@ __global__ void __launch_bounds__(BK3Cfg<Eng, Q, EB, DPAR>::NT)
         uint32_t tx = 0;
         if (tid == 0) fence_proxy_async();
         us = stage_issue<S>(ustage, u + e0 * P3, ne * P3, u + E * P3, bar, tx, tid, nt);
-        gs = stage_issue<S>(gstage, G + e0 * 6 * Q3, ne * 6 * Q3, G + E * 6 * Q3, bar, tx, tid, nt);
+        gs = stage_issue<GS>(gstage, G + e0 * 6 * Q3, ne * 6 * Q3, G + E * 6 * Q3, bar, tx, tid, nt);
         ks = (kq != nullptr) ? stage_issue<S>(kstage, kq + e0 * Q3, ne * Q3, kq + E * Q3, bar, tx, tid, nt) : nullptr;
         if (tid == 0) mbar_arrive_expect_tx(bar, tx);
     };
@@ -1065,7 +1092,7 @@ __global__ void __launch_bounds__(BK3Cfg<Eng, Q, EB, DPAR>::NT)
                     qs = Eng::mul(kk, qs);
                     qt = Eng::mul(kk, qt);
                 }
-                const S* ge = gs + e * 6 * Q3 + x;   // factor-major
+                const GS* ge = gs + e * 6 * Q3 + x;   // factor-major
                 const V g0 = Eng::load(ge[0]), g1 = Eng::load(ge[Q3]), g2 = Eng::load(ge[2 * Q3]);
                 const V g3 = Eng::load(ge[3 * Q3]), g4 = Eng::load(ge[4 * Q3]), g5 = Eng::load(ge[5 * Q3]);
                 A r0 = Eng::vfirst(g0, qr), r1 = Eng::vfirst(g1, qr), r2 = Eng::vfirst(g2, qr);

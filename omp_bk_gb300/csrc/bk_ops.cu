@@ -235,18 +235,18 @@ int bk1_q(const double* B, long long E, const void* jxw, const void* u, void* v,
 #endif  // BK_OP_TU == 1
 
 #if BK_OP_TU == 3
-template <int Q, int EB, bool EO, int DPAR>
+template <int Q, int EB, bool EO, int DPAR, class GS = typename Eng::S>
 int bk3_launch(const P13<typename Eng::C, Q>& prm, long long E, const void* G, const void* k, const void* u, void* v,
                cudaStream_t s)
 {
     using Cfg = BK3Cfg<Eng, Q, EB, DPAR>;
     using S = typename Eng::S;
     static_assert(Cfg::SMEM <= 232448, "BK3 block exceeds the shared memory of an SM");
-    auto kern = bk3_kernel<Eng, Q, EB, EO, DPAR>;
+    auto kern = bk3_kernel<Eng, Q, EB, EO, DPAR, GS>;
     const int occ = prepare<EoTag<Cfg, EO>>(kern, Cfg::SMEM, Cfg::NT);
     if (occ <= 0) return BK_ERR_CUDA;
     const int grid = grid_for((E + EB - 1) / EB, occ);
-    kern<<<grid, Cfg::NT, Cfg::SMEM, s>>>(prm, E, static_cast<const S*>(u), static_cast<const S*>(G),
+    kern<<<grid, Cfg::NT, Cfg::SMEM, s>>>(prm, E, static_cast<const S*>(u), static_cast<const GS*>(G),
                                           static_cast<const S*>(k), static_cast<S*>(v), dev_ctx());
     return cudaGetLastError() == cudaSuccess ? BK_OK : BK_ERR_CUDA;
 }
@@ -259,7 +259,7 @@ constexpr int sweep_eb3_dpar(int q) { return q == 8 ? 2 : 3; }
 
 template <int Q, int EB>
 int bk3_q(const double* B, const double* D, long long E, const void* G, const void* k, const void* u, void* v,
-          cudaStream_t s)
+          int gform, cudaStream_t s)
 {
     P13<typename Eng::C, Q> prm;
     for (int i = 0; i < (Q - 1) * Q; ++i) prm.B[i] = Eng::coef(B[i]);
@@ -269,8 +269,15 @@ int bk3_q(const double* B, const double* D, long long E, const void* G, const vo
     const bool eo = make_p13_eo<typename Eng::C, Q>(prm, B, D, &Eng::coef);
     if (eo) {
         constexpr int DP = sweep_dpar3(Q) ? 2 : 0;
+        if (gform == BK_G_FF) {
+            // G split ahead of time: the float-float engine's even-odd path
+            if constexpr (eng_is_ff())
+                return bk3_launch<Q, DP ? sweep_eb3_dpar(Q) : EB, true, DP, ff2>(prm, E, G, k, u, v, s);
+            return BK_ERR_PREC;
+        }
         return bk3_launch<Q, DP ? sweep_eb3_dpar(Q) : EB, true, DP>(prm, E, G, k, u, v, s);
     }
+    if (gform != BK_G_STORAGE) return BK_ERR_PREC;   // split G: even-odd B and D (GLL nodes, Gauss points)
     return bk3_launch<Q, EB, false, 0>(prm, E, G, k, u, v, s);
 }
 
@@ -380,18 +387,18 @@ int BK_CAT(launch_bk1, BK_SFX)(int p, long long E, const double* B, const void* 
 
 #if BK_OP_TU == 3
 int BK_CAT(launch_bk3, BK_SFX)(int p, long long E, const double* B, const double* D, const void* G, const void* k,
-                                const void* u, void* v, int eb, cudaStream_t s)
+                                const void* u, void* v, int eb, int gform, cudaStream_t s)
 {
     (void)eb;
     switch (p + 2) {
-        case 3: return bk3_q<3, sweep_eb3(3)>(B, D, E, G, k, u, v, s);
-        case 4: return bk3_q<4, sweep_eb3(4)>(B, D, E, G, k, u, v, s);
-        case 5: return bk3_q<5, sweep_eb3(5)>(B, D, E, G, k, u, v, s);
-        case 6: return bk3_q<6, sweep_eb3(6)>(B, D, E, G, k, u, v, s);
-        case 7: return bk3_q<7, sweep_eb3(7)>(B, D, E, G, k, u, v, s);
-        case 8: return bk3_q<8, sweep_eb3(8)>(B, D, E, G, k, u, v, s);
-        case 9: return bk3_q<9, sweep_eb3(9)>(B, D, E, G, k, u, v, s);
-        case 10: return bk3_q<10, sweep_eb3(10)>(B, D, E, G, k, u, v, s);
+        case 3: return bk3_q<3, sweep_eb3(3)>(B, D, E, G, k, u, v, gform, s);
+        case 4: return bk3_q<4, sweep_eb3(4)>(B, D, E, G, k, u, v, gform, s);
+        case 5: return bk3_q<5, sweep_eb3(5)>(B, D, E, G, k, u, v, gform, s);
+        case 6: return bk3_q<6, sweep_eb3(6)>(B, D, E, G, k, u, v, gform, s);
+        case 7: return bk3_q<7, sweep_eb3(7)>(B, D, E, G, k, u, v, gform, s);
+        case 8: return bk3_q<8, sweep_eb3(8)>(B, D, E, G, k, u, v, gform, s);
+        case 9: return bk3_q<9, sweep_eb3(9)>(B, D, E, G, k, u, v, gform, s);
+        case 10: return bk3_q<10, sweep_eb3(10)>(B, D, E, G, k, u, v, gform, s);
         default: return BK_ERR_ORDER;
     }
 }
@@ -408,9 +415,14 @@ int BK_CAT(launch_bk5, BK_SFX)(int p, long long E, const double* D, const void* 
 {
     if (p < 1 || p > 8) return BK_ERR_ORDER;
     if (gform != BK_G_STORAGE && kernel == BK_KERNEL_COLUMN) return BK_ERR_PREC;   // sweep kernel only
-    // AUTO: the sweep kernel, measured equal or faster than the column kernel
-    // for every form at p = 7 (GB300)
-    if (kernel == BK_KERNEL_SWEEP || kernel == BK_KERNEL_AUTO) {
+    // AUTO, as measured on GB300 (E_p = 2^(8-p) * 4096, with and without the
+    // mass term): the column kernel for the FP32-storage forms at p <= 6,
+    // whose sweeps are bound by shared-memory traffic the column kernel keeps
+    // in registers (mixed p = 5: 136 against 110 GDoF/s), and the sweep
+    // kernel otherwise (p = 7 mixed: 141 against 117; float-float at every
+    // p: 34 against 25 at p = 5)
+    const bool auto_col = (kernel == BK_KERNEL_AUTO) && !eng_is_ff() && !eng_is_dfma() && p <= 6;
+    if (kernel == BK_KERNEL_SWEEP || (kernel == BK_KERNEL_AUTO && !auto_col)) {
         switch (layout) {
             case 0: return BK_CATL(bk5_sweep, BK_SFX, 0)(p, F, D, E, u, G, mass, lambda, v, gform, s);
             case 1: return BK_CATL(bk5_sweep, BK_SFX, 1)(p, F, D, E, u, G, mass, lambda, v, gform, s);

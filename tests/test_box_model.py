@@ -1,0 +1,42 @@
+"""The work-box stride tables of the sweep kernels (csrc/bk_kernels.cuh)
+against the shared-memory wavefront model that chose them
+(omp_bk_gb300/box_model.py): every entry is a valid box (rows, planes and
+elements do not overlap) and scores no worse than the first, odd-row
+strides.  No GPU."""
+import os
+import re
+
+import pytest
+
+from omp_bk_gb300 import box_model
+
+SRC = os.path.join(os.path.dirname(__file__), "..", "omp_bk_gb300", "csrc", "bk_kernels.cuh")
+
+
+def _table(name):
+    text = open(SRC).read()
+    m = re.search(r"constexpr int " + name + r"\[\d+\]\[3\] = \{(.*?)\};", text, re.S)
+    assert m, name
+    return [tuple(int(x) for x in t) for t in re.findall(r"\{\s*(\d+),\s*(\d+),\s*(\d+)\s*\}", m.group(1))]
+
+
+@pytest.mark.parametrize("op,name,vb,q0", [(5, "t4", 4, 2), (5, "t8", 8, 2), (3, "b4", 4, 3), (3, "b8", 8, 3)])
+def test_tables_valid_and_no_worse(op, name, vb, q0):
+    rows = _table(name)
+    qs = sorted(box_model.EBS[(op, vb)])
+    assert len(rows) == len(qs) and qs[0] == q0
+    for Q, (zp, ps, es) in zip(qs, rows):
+        assert zp >= Q and (Q - 1) * zp + Q <= ps and Q * ps <= es, (Q, zp, ps, es)
+        new = box_model.mean_score(op, Q, vb, zp, ps, es)
+        old = box_model.mean_score(op, Q, vb, *box_model.legacy(Q, vb))
+        assert new <= old + 1e-9, (Q, new, old)
+
+
+def test_wavefront_counts():
+    # 32 consecutive 4-byte words: one wavefront; all lanes on one bank: 32
+    assert box_model.wavefronts(list(range(32)), 4) == 1
+    assert box_model.wavefronts([32 * i for i in range(32)], 4) == 32
+    # a broadcast is one wavefront
+    assert box_model.wavefronts([5] * 32, 4) == 1
+    # 8-byte values: two half-warp passes when conflict-free
+    assert box_model.wavefronts(list(range(32)), 8) == 2

@@ -343,3 +343,25 @@ def test_bk5_split_g_unsupported(bklib):
     Dn = np.random.default_rng(1).uniform(-1, 1, (nq, nq))
     with pytest.raises(bklib.BKError, match="precision"):
         bklib.bk5_apply(p, E, Dn, g, u, v, gform=bklib.G_FF)
+
+
+@pytest.mark.parametrize("p", P_ALL)
+@pytest.mark.parametrize("coef", [False, True])
+def test_bk3_split_g_is_bitwise(bklib, p, coef):
+    """BK3 on G split once into float-float pairs gives bitwise the apply on
+    the doubles (GLL nodes, Gauss points: the even-odd path)."""
+    E = 7
+    B, D, _, _, _ = bklib.bk1_bk3_matrices(p)
+    nq = p + 2
+    rng = np.random.default_rng(400 + p)
+    u = dev(rng.uniform(-1, 1, E * (nq - 1) ** 3), "f64")
+    g = dev(rng.uniform(0.5, 1.5, E * 6 * nq ** 3) * (1 + 1e-9 * rng.standard_normal(E * 6 * nq ** 3)), "f64")
+    k = dev(np.exp(rng.normal(0, 0.5, E * nq ** 3)), "f64") if coef else None
+    v0 = torch.empty_like(u)
+    v1 = torch.full_like(u, float("nan"))
+    bklib.bk3_apply(p, E, B, D, g, u, v0, k=k)
+    bklib.bk3_apply(p, E, B, D, bklib.g_to_ff(g), u, v1, k=k, gform=bklib.G_FF)
+    torch.cuda.synchronize()
+    assert torch.equal(v0, v1)
+    with pytest.raises(bklib.BKError, match="precision"):
+        bklib.bk3_apply(p, E, B, D, g, u, v1, prec=bklib.PREC_MIXED, gform=bklib.G_FF)
