@@ -64,7 +64,7 @@ def values_per_element(bk: int, p: int):
     return P ** 3, 6 * Q ** 3
 
 
-def _sweep_point(bk_mod, torch, bk, p, form, E, ntests, stream):
+def _sweep_point(bk_mod, torch, bk, p, form, E, ntests, stream, kernel="auto", layout=1):
     prec_name, eng_name, vb = FORMS[form]
     prec, engine = getattr(bk_mod, prec_name), getattr(bk_mod, eng_name)
     dt = torch.float64 if vb == 8 else torch.float32
@@ -80,7 +80,9 @@ def _sweep_point(bk_mod, torch, bk, p, form, E, ntests, stream):
         call = lambda: bk_mod.bk3_apply(p, E, B, D, g, u, v, prec=prec, engine=engine, stream=stream)
     else:
         D = bk_mod.bk5_matrices(p)[0]
-        call = lambda: bk_mod.bk5_apply(p, E, D, g, u, v, prec=prec, engine=engine, stream=stream)
+        kern = {"auto": bk_mod.KERNEL_AUTO, "sweep": bk_mod.KERNEL_SWEEP, "column": bk_mod.KERNEL_COLUMN}[kernel]
+        call = lambda: bk_mod.bk5_apply(p, E, D, g, u, v, prec=prec, engine=engine, kernel=kern, layout=layout,
+                                        stream=stream)
     call()
     torch.cuda.synchronize()
     best_host = best_dev = float("inf")
@@ -123,6 +125,10 @@ def parse(argv=None):
     ap.add_argument("--bk", default="5", help="operators, comma separated (1, 3, 5)")
     ap.add_argument("--p", default="2,4,6", help="orders, comma separated")
     ap.add_argument("--kernels", default="ff,mixed", help="forms: ff, dfma, mixed, fp32")
+    ap.add_argument("--kernel", default="auto", choices=("auto", "sweep", "column"),
+                    help="BK5 kernel shape (bk_kernel_shape)")
+    ap.add_argument("--layout", type=int, default=1, choices=(0, 1, 2),
+                    help="BK5 G layout (bk_layout; 1 = BK5.cpp's interleaved layout)")
     ap.add_argument("--dof-min", type=float, default=1e3)
     ap.add_argument("--dof-max", type=float, default=1e8)
     ap.add_argument("--ppd", type=int, default=4, help="points per decade")
@@ -148,7 +154,8 @@ def main(argv=None):
                 if form not in FORMS:
                     raise SystemExit(f"unknown form {form!r}")
                 for E in element_counts(nodes_per_dim(bk, p), args.dof_min, args.dof_max, args.ppd):
-                    dofs, g, gb, gd, gbd = _sweep_point(bk_mod, torch, bk, p, form, E, args.ntests, stream)
+                    dofs, g, gb, gd, gbd = _sweep_point(bk_mod, torch, bk, p, form, E, args.ntests, stream,
+                                                        args.kernel, args.layout)
                     row = f"cuda,{nq},bk{bk}_{form},{E},{dofs},{g:.4f},{gb:.2f},{gd:.4f},{gbd:.2f}"
                     rows.append(row)
                     print(row, flush=True)
