@@ -398,6 +398,44 @@ inline bool make_eor(const double* m, int ld, bool trans, int sign, EORMat<C, NO
     return dev <= 1e-13 * big;
 }
 
+// The NO outputs y of one line of NI inputs x through the even-odd form m
+// (see EORMat); x and y are register arrays of the caller.
+template <class Eng, int NI, int NO, int SIGN, class EM>
+__device__ __forceinline__ void eor_line(const typename Eng::V (&x)[NI], typename Eng::V (&y)[NO], const EM& m)
+{
+    using V = typename Eng::V;
+    using A = typename Eng::A;
+    constexpr int HI = NI / 2, HO = NO / 2;
+    V ev[HI > 0 ? HI : 1], dv[HI > 0 ? HI : 1];
+#pragma unroll
+    for (int n = 0; n < HI; ++n) {
+        ev[n] = Eng::vadd_in(x[n], x[NI - 1 - n]);
+        dv[n] = Eng::vsub_in(x[n], x[NI - 1 - n]);
+    }
+    if constexpr ((NO & 1) != 0) {
+        A t = Eng::first(m.r[0], SIGN > 0 ? ev[0] : dv[0]);
+#pragma unroll
+        for (int n = 1; n < HI; ++n) Eng::madd(t, m.r[n], SIGN > 0 ? ev[n] : dv[n]);
+        if constexpr (SIGN > 0 && (NI & 1) != 0) Eng::madd(t, m.rm, x[HI]);
+        y[HO] = Eng::result(t);
+    }
+#pragma unroll
+    for (int o = 0; o < HO; ++o) {
+        A aa = Eng::first(m.A[o * HI], ev[0]), bb = Eng::first(m.B[o * HI], dv[0]);
+#pragma unroll
+        for (int n = 1; n < HI; ++n) {
+            Eng::madd(aa, m.A[o * HI + n], ev[n]);
+            Eng::madd(bb, m.B[o * HI + n], dv[n]);
+        }
+        if constexpr ((NI & 1) != 0) Eng::madd(aa, m.c[o], x[HI]);
+        if constexpr (SIGN > 0) {
+            Eng::sum_diff(bb, aa, y[o], y[NO - 1 - o]);   // b + a, a - b
+        } else {
+            Eng::sum_diff(aa, bb, y[o], y[NO - 1 - o]);   // a + b, b - a
+        }
+    }
+}
+
 // Even-odd sweep of direction DIR of the (X, Y, Z) box into extent NO along
 // DIR (see EORMat; in == out allowed).
 template <class Eng, class WB, int DIR, int X, int Y, int Z, int NO, int SIGN, class EM>
@@ -405,9 +443,7 @@ __device__ __forceinline__ void sweep_eor(const typename Eng::V* in, typename En
                                           int tid, int nt)
 {
     using V = typename Eng::V;
-    using A = typename Eng::A;
     constexpr int NI = DIR == 0 ? X : (DIR == 1 ? Y : Z);
-    constexpr int HI = NI / 2, HO = NO / 2;
     constexpr int LB = DIR == 2 ? Y : Z;
     constexpr int L = (X * Y * Z) / NI;
     constexpr int SD = DIR == 0 ? WB::PS : (DIR == 1 ? WB::ZP : 1);
@@ -418,42 +454,88 @@ __device__ __forceinline__ void sweep_eor(const typename Eng::V* in, typename En
         const int b = l - a * LB;
         int base = (DIR == 0) ? a * WB::ZP + b : (DIR == 1 ? a * WB::PS + b : a * WB::PS + b * WB::ZP);
         base += e * WB::size;
-        V x[NI];
+        V x[NI], y[NO];
 #pragma unroll
         for (int n = 0; n < NI; ++n) x[n] = in[base + n * SD];
-        V ev[HI > 0 ? HI : 1], dv[HI > 0 ? HI : 1];
+        eor_line<Eng, NI, NO, SIGN>(x, y, m);
 #pragma unroll
-        for (int n = 0; n < HI; ++n) {
-            ev[n] = Eng::vadd_in(x[n], x[NI - 1 - n]);
-            dv[n] = Eng::vsub_in(x[n], x[NI - 1 - n]);
-        }
-        V mid_out;
-        if constexpr ((NO & 1) != 0) {
-            A t = Eng::first(m.r[0], SIGN > 0 ? ev[0] : dv[0]);
+        for (int o = 0; o < NO; ++o) out[base + o * SD] = y[o];
+    }
+}
+
+// The first interpolation of BK1/BK3 straight from the dense staged u (P^3
+// values of S per element, k fastest): lines along i, (j, k)
+// consecutive across threads, so the stage reads are consecutive words; the
+// Q outputs of each line go to the padded box `out` as (Q, P, P).  Replaces
+// the load into a box and the sweep over it (one write and one read of
+// every value less).
+template <class Eng, class WB, int P, int Q, class EM>
+__device__ __forceinline__ void interp0_from_dense(const typename Eng::S* us, typename Eng::V* out, int ne,
+                                                   const EM& m, int tid, int nt)
+{
+    using V = typename Eng::V;
+    constexpr int L = P * P;
+    for (int w = tid; w < ne * L; w += nt) {
+        const int e = w / L;
+        const int l = w - e * L;
+        const int j = l / P;
+        const int kk = l - j * P;
+        const typename Eng::S* src = us + e * (P * P * P) + j * P + kk;
+        V x[P], y[Q];
 #pragma unroll
-            for (int n = 1; n < HI; ++n) Eng::madd(t, m.r[n], SIGN > 0 ? ev[n] : dv[n]);
-            if constexpr (SIGN > 0 && (NI & 1) != 0) Eng::madd(t, m.rm, x[HI]);
-            mid_out = Eng::result(t);
-        }
+        for (int n = 0; n < P; ++n) x[n] = Eng::load(src[n * P * P]);
+        eor_line<Eng, P, Q, +1>(x, y, m);
+        const int base = e * WB::size + j * WB::ZP + kk;
 #pragma unroll
-        for (int o = 0; o < HO; ++o) {
-            A aa = Eng::first(m.A[o * HI], ev[0]), bb = Eng::first(m.B[o * HI], dv[0]);
+        for (int o = 0; o < Q; ++o) out[base + o * WB::PS] = y[o];
+    }
+}
+
+// The last interpolation of BK1/BK3 (along i, (Q, P, P) box -> P^3) written
+// straight to v in global memory: (j, k) consecutive across threads, so each
+// output row is a coalesced store.  Replaces the sweep into a box and the
+// store pass.
+template <class Eng, class WB, int P, int Q, class EM>
+__device__ __forceinline__ void interp0_to_dense(const typename Eng::V* in, typename Eng::S* __restrict__ v,
+                                                 int ne, const EM& m, int tid, int nt)
+{
+    using V = typename Eng::V;
+    constexpr int L = P * P;
+    for (int w = tid; w < ne * L; w += nt) {
+        const int e = w / L;
+        const int l = w - e * L;
+        const int j = l / P;
+        const int kk = l - j * P;
+        const int base = e * WB::size + j * WB::ZP + kk;
+        V x[Q], y[P];
 #pragma unroll
-            for (int n = 1; n < HI; ++n) {
-                Eng::madd(aa, m.A[o * HI + n], ev[n]);
-                Eng::madd(bb, m.B[o * HI + n], dv[n]);
-            }
-            if constexpr ((NI & 1) != 0) Eng::madd(aa, m.c[o], x[HI]);
-            V s, d;
-            if constexpr (SIGN > 0) {
-                Eng::sum_diff(bb, aa, s, d);   // b + a, a - b
-            } else {
-                Eng::sum_diff(aa, bb, s, d);   // a + b, b - a
-            }
-            out[base + o * SD] = s;
-            out[base + (NO - 1 - o) * SD] = d;
-        }
-        if constexpr ((NO & 1) != 0) out[base + HO * SD] = mid_out;
+        for (int n = 0; n < Q; ++n) x[n] = in[base + n * WB::PS];
+        eor_line<Eng, Q, P, +1>(x, y, m);
+        typename Eng::S* dst = v + e * (P * P * P) + j * P + kk;
+#pragma unroll
+        for (int o = 0; o < P; ++o) dst[o * P * P] = Eng::store(y[o]);
+    }
+}
+
+// One pass over the lines along k (thread per (i, j) line of every element)
+// of a padded box holding (Q, Q, P): the line's P values are read once and
+// `f(e, i, j, x, base)` computes and writes from registers.  The fused
+// k-direction steps of BK1 and BK3 use it.
+template <class Eng, class WB, int Q, int P, class F>
+__device__ __forceinline__ void kline_pass(const typename Eng::V* in, int ne, int tid, int nt, F f)
+{
+    using V = typename Eng::V;
+    constexpr int L = Q * Q;
+    for (int w = tid; w < ne * L; w += nt) {
+        const int e = w / L;
+        const int l = w - e * L;
+        const int i = l / Q;
+        const int j = l - i * Q;
+        const int base = e * WB::size + WB::at(i, j, 0);
+        V x[P];
+#pragma unroll
+        for (int n = 0; n < P; ++n) x[n] = in[base + n];
+        f(e, i, j, x, base);
     }
 }
 
@@ -882,6 +964,11 @@ __global__ void __launch_bounds__(BK1Cfg<Eng, Q, EB>::NT)
     using V = typename Eng::V;
     using WB = typename Cfg::WB;
     constexpr int P = Cfg::P, Q3 = Cfg::Q3, P3 = Cfg::P3;
+    // u and v straight between the stage / HBM and the first / last
+    // interpolation when they need no conversion; the float-float engine's
+    // split and join are spread over all threads by the load and store passes
+    // instead (in the line passes a quarter of the threads would do them)
+    constexpr bool kDirectIO = std::is_same<S, V>::value;
     extern __shared__ __align__(16) unsigned char smem[];
     unsigned char* ustage = smem;
     unsigned char* jstage = ustage + Cfg::U_BYTES;
@@ -920,48 +1007,69 @@ __global__ void __launch_bounds__(BK1Cfg<Eng, Q, EB>::NT)
         const long long e0 = bt * EB;
         const int ne = int((E - e0) < EB ? (E - e0) : EB);
         if (batch_wait_failed(bar, phase, ctx, tid)) return;
-        load_box<Eng, WB, P, P, P>(us, P3, W0, ne, tid, nt);
-        __syncthreads();
         if constexpr (EO) {   // B centro-symmetric (GLL nodes, Gauss points)
-            sweep_eor<Eng, WB, 0, P, P, P, Q, +1>(W0, W1, ne, prm.bi, tid, nt);   // (Q,P,P)
+            if constexpr (kDirectIO) {
+                interp0_from_dense<Eng, WB, P, Q>(us, W1, ne, prm.bi, tid, nt);    // (Q,P,P)
+            } else {
+                load_box<Eng, WB, P, P, P>(us, P3, W0, ne, tid, nt);
+                __syncthreads();
+                sweep_eor<Eng, WB, 0, P, P, P, Q, +1>(W0, W1, ne, prm.bi, tid, nt);   // (Q,P,P)
+            }
             __syncthreads();
             sweep_eor<Eng, WB, 1, Q, P, P, Q, +1>(W1, W0, ne, prm.bi, tid, nt);   // (Q,Q,P)
             __syncthreads();
-            sweep_eor<Eng, WB, 2, Q, Q, P, Q, +1>(W0, W1, ne, prm.bi, tid, nt);   // (Q,Q,Q)
+            // along k in registers: interpolate to the points, times JxW,
+            // back to the nodes, (Q,Q,P) in place
+            kline_pass<Eng, WB, Q, P>(W0, ne, tid, nt, [&](int e, int i, int j, const V (&x)[P], int base) {
+                V y[Q], z[P];
+                eor_line<Eng, P, Q, +1>(x, y, prm.bi);
+                const S* jl = js + e * Q3 + (i * Q + j) * Q;
+#pragma unroll
+                for (int o = 0; o < Q; ++o) y[o] = Eng::mul(y[o], Eng::load(jl[o]));
+                eor_line<Eng, Q, P, +1>(y, z, prm.bb);
+#pragma unroll
+                for (int o = 0; o < P; ++o) W0[base + o] = z[o];
+            });
+            __syncthreads();
+            if (bt + gridDim.x < nbatch) issue(bt + gridDim.x);   // the stage is free
+            sweep_eor<Eng, WB, 1, Q, Q, P, P, +1>(W0, W1, ne, prm.bb, tid, nt);   // (Q,P,P)
+            __syncthreads();
+            if constexpr (kDirectIO) {
+                interp0_to_dense<Eng, WB, P, Q>(W1, v + e0 * P3, ne, prm.bb, tid, nt);  // -> v
+            } else {
+                sweep_eor<Eng, WB, 0, Q, P, P, P, +1>(W1, W0, ne, prm.bb, tid, nt);   // (P,P,P)
+                __syncthreads();
+                store_box<Eng, WB, P, P, P>(W0, v + e0 * P3, P3, ne, tid, nt);
+            }
+            __syncthreads();
         } else {
+            load_box<Eng, WB, P, P, P>(us, P3, W0, ne, tid, nt);
+            __syncthreads();
             sweep<Eng, WB, 0, P, P, P, Q>(W0, W1, ne, Bi, tid, nt);   // (Q,P,P)
             __syncthreads();
             sweep<Eng, WB, 1, Q, P, P, Q>(W1, W0, ne, Bi, tid, nt);   // (Q,Q,P)
             __syncthreads();
             sweep<Eng, WB, 2, Q, Q, P, Q>(W0, W1, ne, Bi, tid, nt);   // (Q,Q,Q)
-        }
-        __syncthreads();
-        for (int w = tid; w < ne * Q3; w += nt) {
-            const int e = w / Q3;
-            const int x = w - e * Q3;
-            const int i = x / (Q * Q), j = (x / Q) % Q, k = x % Q;
-            const int wi = e * WB::size + WB::at(i, j, k);
-            W1[wi] = Eng::mul(W1[wi], Eng::load(js[e * Q3 + x]));
-        }
-        __syncthreads();
-        if (bt + gridDim.x < nbatch) issue(bt + gridDim.x);   // the stage is free
-        if constexpr (EO) {
-            sweep_eor<Eng, WB, 2, Q, Q, Q, P, +1>(W1, W0, ne, prm.bb, tid, nt);   // (Q,Q,P)
             __syncthreads();
-            sweep_eor<Eng, WB, 1, Q, Q, P, P, +1>(W0, W1, ne, prm.bb, tid, nt);   // (Q,P,P)
+            for (int w = tid; w < ne * Q3; w += nt) {
+                const int e = w / Q3;
+                const int x = w - e * Q3;
+                const int i = x / (Q * Q), j = (x / Q) % Q, k = x % Q;
+                const int wi = e * WB::size + WB::at(i, j, k);
+                W1[wi] = Eng::mul(W1[wi], Eng::load(js[e * Q3 + x]));
+            }
             __syncthreads();
-            sweep_eor<Eng, WB, 0, Q, P, P, P, +1>(W1, W0, ne, prm.bb, tid, nt);   // (P,P,P)
-        } else {
+            if (bt + gridDim.x < nbatch) issue(bt + gridDim.x);   // the stage is free
             sweep<Eng, WB, 2, Q, Q, Q, P>(W1, W0, ne, Bb, tid, nt);   // (Q,Q,P)
             __syncthreads();
             sweep<Eng, WB, 1, Q, Q, P, P>(W0, W1, ne, Bb, tid, nt);   // (Q,P,P)
             __syncthreads();
             sweep<Eng, WB, 0, Q, P, P, P>(W1, W0, ne, Bb, tid, nt);   // (P,P,P)
+            __syncthreads();
+            // padded box -> v (consecutive threads, consecutive values)
+            store_box<Eng, WB, P, P, P>(W0, v + e0 * P3, P3, ne, tid, nt);
+            __syncthreads();
         }
-        __syncthreads();
-        // padded box -> v (consecutive threads, consecutive values)
-        store_box<Eng, WB, P, P, P>(W0, v + e0 * P3, P3, ne, tid, nt);
-        __syncthreads();
     }
 }
 
@@ -1001,6 +1109,11 @@ __global__ void __launch_bounds__(BK3Cfg<Eng, Q, EB, DPAR>::NT)
     using A = typename Eng::A;
     using WB = typename Cfg::WB;
     constexpr int P = Cfg::P, Q3 = Cfg::Q3, P3 = Cfg::P3;
+    // u and v straight between the stage / HBM and the first / last
+    // interpolation when they need no conversion; the float-float engine's
+    // split and join are spread over all threads by the load and store passes
+    // instead (in the line passes a quarter of the threads would do them)
+    constexpr bool kDirectIO = std::is_same<S, V>::value;
     extern __shared__ __align__(16) unsigned char smem[];
     unsigned char* ustage = smem;
     unsigned char* gstage = ustage + Cfg::U_BYTES;
@@ -1046,37 +1159,6 @@ __global__ void __launch_bounds__(BK3Cfg<Eng, Q, EB, DPAR>::NT)
         const long long e0 = bt * EB;
         const int ne = int((E - e0) < EB ? (E - e0) : EB);
         if (batch_wait_failed(bar, phase, ctx, tid)) return;
-        load_box<Eng, WB, P, P, P>(us, P3, W0, ne, tid, nt);
-        __syncthreads();
-        if constexpr (EO) {
-            sweep_eor<Eng, WB, 0, P, P, P, Q, +1>(W0, W1, ne, prm.bi, tid, nt);   // (Q,P,P)
-            __syncthreads();
-            sweep_eor<Eng, WB, 1, Q, P, P, Q, +1>(W1, W0, ne, prm.bi, tid, nt);   // (Q,Q,P)
-            __syncthreads();
-            sweep_eor<Eng, WB, 2, Q, Q, P, Q, +1>(W0, W2, ne, prm.bi, tid, nt);   // u at the points: W2
-            __syncthreads();
-            if constexpr (DPAR) {
-                const int grp = tid / Cfg::LINES;
-                if (grp < 3)
-                    sweep_eo_dyn<Eng, WB, Q>(W2, grp == 0 ? W0 : (grp == 1 ? W1 : W3), ne, prm.dg,
-                                             tid - grp * Cfg::LINES, Cfg::LINES, grp);   // qr, qs, qt
-            } else {
-                sweep_eor<Eng, WB, 0, Q, Q, Q, Q, -1>(W2, W0, ne, prm.dg, tid, nt);   // qr
-                sweep_eor<Eng, WB, 1, Q, Q, Q, Q, -1>(W2, W1, ne, prm.dg, tid, nt);   // qs
-                sweep_eor<Eng, WB, 2, Q, Q, Q, Q, -1>(W2, W3, ne, prm.dg, tid, nt);   // qt
-            }
-        } else {
-            sweep<Eng, WB, 0, P, P, P, Q>(W0, W1, ne, Bi, tid, nt);   // (Q,P,P)
-            __syncthreads();
-            sweep<Eng, WB, 1, Q, P, P, Q>(W1, W0, ne, Bi, tid, nt);   // (Q,Q,P)
-            __syncthreads();
-            sweep<Eng, WB, 2, Q, Q, P, Q>(W0, W2, ne, Bi, tid, nt);   // u at the points: W2
-            __syncthreads();
-            sweep<Eng, WB, 0, Q, Q, Q, Q>(W2, W0, ne, Dg, tid, nt);   // qr
-            sweep<Eng, WB, 1, Q, Q, Q, Q>(W2, W1, ne, Dg, tid, nt);   // qs
-            sweep<Eng, WB, 2, Q, Q, Q, Q>(W2, W3, ne, Dg, tid, nt);   // qt
-        }
-        __syncthreads();
         // fluxes (k G grad u with the coefficient); written twice, with and
         // without k, so that no point carries predicated-off products
         auto fluxes = [&](auto with_k) {
@@ -1104,78 +1186,156 @@ __global__ void __launch_bounds__(BK3Cfg<Eng, Q, EB, DPAR>::NT)
                 W3[wi] = Eng::result(r2);
             }
         };
-        if (ks != nullptr)
-            fluxes(std::true_type{});
-        else
-            fluxes(std::false_type{});
-        __syncthreads();
-        if (bt + gridDim.x < nbatch) issue(bt + gridDim.x);   // the stage is free
-        if constexpr (DPAR) {
-            const int grp = tid / Cfg::LINES;
-            if (grp < 3) {
-                V* Wg = grp == 0 ? W0 : (grp == 1 ? W1 : W3);
-                sweep_eo_dyn<Eng, WB, Q>(Wg, Wg, ne, prm.dtr, tid - grp * Cfg::LINES, Cfg::LINES, grp);
-            }
-        } else if constexpr (EO) {
-            sweep_eor<Eng, WB, 0, Q, Q, Q, Q, -1>(W0, W0, ne, prm.dtr, tid, nt);
-            sweep_eor<Eng, WB, 1, Q, Q, Q, Q, -1>(W1, W1, ne, prm.dtr, tid, nt);
-            sweep_eor<Eng, WB, 2, Q, Q, Q, Q, -1>(W3, W3, ne, prm.dtr, tid, nt);
-        } else {
-            sweep<Eng, WB, 0, Q, Q, Q, Q>(W0, W0, ne, Dtr, tid, nt);
-            sweep<Eng, WB, 1, Q, Q, Q, Q>(W1, W1, ne, Dtr, tid, nt);
-        }
-        __syncthreads();
-        // along r on W3 (already contracted when EO), plus the two other
-        // terms -> W2
-        {
-            constexpr int L = Q * Q;
-            for (int w = tid; w < ne * L; w += nt) {
-                const int e = w / L;
-                const int l = w - e * L;
-                const int i = l / Q;
-                const int j = l - i * Q;
-                const int base = e * WB::size + WB::at(i, j, 0);
-                V x[Q];
+        // the transposed k-direction derivative of the third flux plus the
+        // other two terms, at one (i, j) line: s = D^T x + W0 + W1
+        auto sum_line = [&](const V (&t)[Q], V (&sv)[Q], int base) {
 #pragma unroll
-                for (int n = 0; n < Q; ++n) x[n] = W3[base + n];
-#pragma unroll
-                for (int o = 0; o < Q; ++o) {
-                    A acc;
-                    if constexpr (EO) {
-                        acc = Eng::from(x[o]);
-                    } else {
-                        acc = Eng::first(Dtr(o, 0), x[0]);
-#pragma unroll
-                        for (int n = 1; n < Q; ++n) Eng::madd(acc, Dtr(o, n), x[n]);
-                    }
-                    if constexpr (HasSum3<Eng>::value) {
-                        W2[base + o] = Eng::sum3(Eng::result(acc), W0[base + o], W1[base + o]);
-                    } else {
-                        Eng::add(acc, W0[base + o]);
-                        Eng::add(acc, W1[base + o]);
-                        W2[base + o] = Eng::result(acc);
-                    }
+            for (int o = 0; o < Q; ++o) {
+                if constexpr (HasSum3<Eng>::value) {
+                    sv[o] = Eng::sum3(t[o], W0[base + o], W1[base + o]);
+                } else {
+                    A acc = Eng::from(t[o]);
+                    Eng::add(acc, W0[base + o]);
+                    Eng::add(acc, W1[base + o]);
+                    sv[o] = Eng::result(acc);
                 }
             }
-        }
-        __syncthreads();
+        };
         if constexpr (EO) {
-            sweep_eor<Eng, WB, 2, Q, Q, Q, P, +1>(W2, W0, ne, prm.bb, tid, nt);   // (Q,Q,P)
+            // B centro-symmetric, D centro-antisymmetric (GLL nodes, Gauss
+            // points).  u straight from the stage into the first
+            // interpolation, v straight from the last one to HBM.
+            if constexpr (kDirectIO) {
+                interp0_from_dense<Eng, WB, P, Q>(us, W1, ne, prm.bi, tid, nt);    // (Q,P,P)
+            } else {
+                load_box<Eng, WB, P, P, P>(us, P3, W0, ne, tid, nt);
+                __syncthreads();
+                sweep_eor<Eng, WB, 0, P, P, P, Q, +1>(W0, W1, ne, prm.bi, tid, nt);   // (Q,P,P)
+            }
+            __syncthreads();
+            sweep_eor<Eng, WB, 1, Q, P, P, Q, +1>(W1, W0, ne, prm.bi, tid, nt);   // (Q,Q,P)
+            __syncthreads();
+            if constexpr (DPAR) {
+                sweep_eor<Eng, WB, 2, Q, Q, P, Q, +1>(W0, W2, ne, prm.bi, tid, nt);   // u at the points: W2
+                __syncthreads();
+                const int grp = tid / Cfg::LINES;
+                if (grp < 3)
+                    sweep_eo_dyn<Eng, WB, Q>(W2, grp == 0 ? W0 : (grp == 1 ? W1 : W3), ne, prm.dg,
+                                             tid - grp * Cfg::LINES, Cfg::LINES, grp);   // qr, qs, qt
+            } else {
+                // along k in registers: u at the points (W2) and its
+                // k-derivative qt (W3)
+                kline_pass<Eng, WB, Q, P>(W0, ne, tid, nt, [&](int, int, int, const V (&x)[P], int base) {
+                    V y[Q], t[Q];
+                    eor_line<Eng, P, Q, +1>(x, y, prm.bi);
+                    eor_line<Eng, Q, Q, -1>(y, t, prm.dg);
+#pragma unroll
+                    for (int o = 0; o < Q; ++o) {
+                        W2[base + o] = y[o];
+                        W3[base + o] = t[o];
+                    }
+                });
+                __syncthreads();
+                sweep_eor<Eng, WB, 0, Q, Q, Q, Q, -1>(W2, W0, ne, prm.dg, tid, nt);   // qr
+                sweep_eor<Eng, WB, 1, Q, Q, Q, Q, -1>(W2, W1, ne, prm.dg, tid, nt);   // qs
+            }
+            __syncthreads();
+            if (ks != nullptr)
+                fluxes(std::true_type{});
+            else
+                fluxes(std::false_type{});
+            __syncthreads();
+            if (bt + gridDim.x < nbatch) issue(bt + gridDim.x);   // the stage is free
+            if constexpr (DPAR) {
+                const int grp = tid / Cfg::LINES;
+                if (grp < 3) {
+                    V* Wg = grp == 0 ? W0 : (grp == 1 ? W1 : W3);
+                    sweep_eo_dyn<Eng, WB, Q>(Wg, Wg, ne, prm.dtr, tid - grp * Cfg::LINES, Cfg::LINES, grp);
+                }
+                __syncthreads();
+                // the three terms summed into W2, then back along k
+                kline_pass<Eng, WB, Q, Q>(W3, ne, tid, nt, [&](int, int, int, const V (&x)[Q], int base) {
+                    V sv[Q];
+                    sum_line(x, sv, base);
+#pragma unroll
+                    for (int o = 0; o < Q; ++o) W2[base + o] = sv[o];
+                });
+                __syncthreads();
+                sweep_eor<Eng, WB, 2, Q, Q, Q, P, +1>(W2, W0, ne, prm.bb, tid, nt);   // (Q,Q,P)
+            } else {
+                sweep_eor<Eng, WB, 0, Q, Q, Q, Q, -1>(W0, W0, ne, prm.dtr, tid, nt);
+                sweep_eor<Eng, WB, 1, Q, Q, Q, Q, -1>(W1, W1, ne, prm.dtr, tid, nt);
+                __syncthreads();
+                // along k in registers: the transposed derivative of the
+                // third flux, plus the other two terms, back to the nodes;
+                // (Q,Q,P) into W0 (each line reads its own W0 values first)
+                kline_pass<Eng, WB, Q, Q>(W3, ne, tid, nt, [&](int, int, int, const V (&x)[Q], int base) {
+                    V t[Q], sv[Q], z[P];
+                    eor_line<Eng, Q, Q, -1>(x, t, prm.dtr);
+                    sum_line(t, sv, base);
+                    eor_line<Eng, Q, P, +1>(sv, z, prm.bb);
+#pragma unroll
+                    for (int o = 0; o < P; ++o) W0[base + o] = z[o];
+                });
+            }
             __syncthreads();
             sweep_eor<Eng, WB, 1, Q, Q, P, P, +1>(W0, W1, ne, prm.bb, tid, nt);   // (Q,P,P)
             __syncthreads();
-            sweep_eor<Eng, WB, 0, Q, P, P, P, +1>(W1, W0, ne, prm.bb, tid, nt);   // (P,P,P)
+            if constexpr (kDirectIO) {
+                interp0_to_dense<Eng, WB, P, Q>(W1, v + e0 * P3, ne, prm.bb, tid, nt);  // -> v
+            } else {
+                sweep_eor<Eng, WB, 0, Q, P, P, P, +1>(W1, W0, ne, prm.bb, tid, nt);   // (P,P,P)
+                __syncthreads();
+                store_box<Eng, WB, P, P, P>(W0, v + e0 * P3, P3, ne, tid, nt);
+            }
+            __syncthreads();
         } else {
+            load_box<Eng, WB, P, P, P>(us, P3, W0, ne, tid, nt);
+            __syncthreads();
+            sweep<Eng, WB, 0, P, P, P, Q>(W0, W1, ne, Bi, tid, nt);   // (Q,P,P)
+            __syncthreads();
+            sweep<Eng, WB, 1, Q, P, P, Q>(W1, W0, ne, Bi, tid, nt);   // (Q,Q,P)
+            __syncthreads();
+            sweep<Eng, WB, 2, Q, Q, P, Q>(W0, W2, ne, Bi, tid, nt);   // u at the points: W2
+            __syncthreads();
+            sweep<Eng, WB, 0, Q, Q, Q, Q>(W2, W0, ne, Dg, tid, nt);   // qr
+            sweep<Eng, WB, 1, Q, Q, Q, Q>(W2, W1, ne, Dg, tid, nt);   // qs
+            sweep<Eng, WB, 2, Q, Q, Q, Q>(W2, W3, ne, Dg, tid, nt);   // qt
+            __syncthreads();
+            if (ks != nullptr)
+                fluxes(std::true_type{});
+            else
+                fluxes(std::false_type{});
+            __syncthreads();
+            if (bt + gridDim.x < nbatch) issue(bt + gridDim.x);   // the stage is free
+            sweep<Eng, WB, 0, Q, Q, Q, Q>(W0, W0, ne, Dtr, tid, nt);
+            sweep<Eng, WB, 1, Q, Q, Q, Q>(W1, W1, ne, Dtr, tid, nt);
+            __syncthreads();
+            // along r on W3 plus the two other terms -> W2
+            kline_pass<Eng, WB, Q, Q>(W3, ne, tid, nt, [&](int, int, int, const V (&x)[Q], int base) {
+                V t[Q], sv[Q];
+#pragma unroll
+                for (int o = 0; o < Q; ++o) {
+                    A acc = Eng::first(Dtr(o, 0), x[0]);
+#pragma unroll
+                    for (int n = 1; n < Q; ++n) Eng::madd(acc, Dtr(o, n), x[n]);
+                    t[o] = Eng::result(acc);
+                }
+                sum_line(t, sv, base);
+#pragma unroll
+                for (int o = 0; o < Q; ++o) W2[base + o] = sv[o];
+            });
+            __syncthreads();
             sweep<Eng, WB, 2, Q, Q, Q, P>(W2, W0, ne, Bb, tid, nt);   // (Q,Q,P)
             __syncthreads();
             sweep<Eng, WB, 1, Q, Q, P, P>(W0, W1, ne, Bb, tid, nt);   // (Q,P,P)
             __syncthreads();
             sweep<Eng, WB, 0, Q, P, P, P>(W1, W0, ne, Bb, tid, nt);   // (P,P,P)
+            __syncthreads();
+            // padded box -> v (consecutive threads, consecutive values)
+            store_box<Eng, WB, P, P, P>(W0, v + e0 * P3, P3, ne, tid, nt);
+            __syncthreads();
         }
-        __syncthreads();
-        // padded box -> v (consecutive threads, consecutive values)
-        store_box<Eng, WB, P, P, P>(W0, v + e0 * P3, P3, ne, tid, nt);
-        __syncthreads();
     }
 }
 
