@@ -273,16 +273,32 @@ def run_reference(args):
 
 # ---- the other configurations ------------------------------------------------
 
-def _events_ms(fn, steps, warmup, torch):
+def _events_ms(fn, steps, warmup, torch, graph=False):
+    """Mean ms per call over `steps` calls after `warmup`, CUDA events on the
+    current stream.  graph: the steps are captured once into a CUDA graph
+    and replayed (the applies allocate and synchronize nothing), so that a
+    launch of a few microseconds is not timed behind the host's per-call
+    overhead."""
     for _ in range(warmup):
         fn()
     torch.cuda.synchronize()
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
-    t0.record()
-    for _ in range(steps):
-        fn()
-    t1.record()
+    if graph:
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            for _ in range(steps):
+                fn()
+        g.replay()   # one untimed replay
+        torch.cuda.synchronize()
+        t0.record()
+        g.replay()
+        t1.record()
+    else:
+        t0.record()
+        for _ in range(steps):
+            fn()
+        t1.record()
     torch.cuda.synchronize()
     return t0.elapsed_time(t1) / steps
 
@@ -315,23 +331,26 @@ def run_bk1(args):
     v = torch.empty_like(u)
     dofs = E * P ** 3
     steps, warm = max(args.steps, 20), max(args.warmup, 3)
-    ms = _events_ms(lambda: bk.bk1_apply(p, E, B, qd, u, v), steps, warm, torch)
+    # one apply is ~15 us: the applies are timed as one CUDA graph of `steps`
+    # launches (device time; a host-timed loop measured the ctypes call)
+    ms = _events_ms(lambda: bk.bk1_apply(p, E, B, qd, u, v), steps, warm, torch, graph=True)
     forms = {}
     ref = v.clone()
     vd = torch.empty_like(v)
-    md = _events_ms(lambda: bk.bk1_apply(p, E, B, qd, u, vd, engine=bk.ENGINE_DFMA), steps, warm, torch)
+    md = _events_ms(lambda: bk.bk1_apply(p, E, B, qd, u, vd, engine=bk.ENGINE_DFMA), steps, warm, torch, graph=True)
     forms["fp64_dfma"] = {"gdofs": dofs / md / 1e6, "rel_max_err": _rel(vd, ref)[0]}
     u32, q32 = u.float(), qd.float()
     v32 = torch.empty_like(u32)
     for name, pr in (("fp32", bk.PREC_FP32), ("mixed", bk.PREC_MIXED)):
-        m32 = _events_ms(lambda: bk.bk1_apply(p, E, B, q32, u32, v32, prec=pr), steps, warm, torch)
+        m32 = _events_ms(lambda: bk.bk1_apply(p, E, B, q32, u32, v32, prec=pr), steps, warm, torch, graph=True)
         forms[name] = {"gdofs": dofs / m32 / 1e6, "rel_max_err": _rel(v32, ref)[0]}
     import oracle
     t = time.perf_counter()
     host = oracle.bk1(Q, E, B, qd.cpu().numpy(), u.cpu().numpy(), fast=True)
     cpu_s = time.perf_counter() - t
     err = float(abs(torch.from_numpy(host) - ref.cpu()).max() / ref.abs().max())
-    _line(args, f"BK1 mass apply p={p} (P=4 GLL, Q=5 Gauss), E={E}, FP64 float-float, L2-resident (8.3 MB)",
+    _line(args, f"BK1 mass apply p={p} (P=4 GLL, Q=5 Gauss), E={E}, FP64 float-float, L2-resident (8.3 MB), "
+                f"timed as one CUDA graph of {steps} applies",
           dofs / ms / 1e6, ms, "f64",
           {"forms": forms, "rel_max_err_vs_oracle": err,
            "cpu_baseline": {"value": dofs / cpu_s / 1e9, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",

@@ -70,15 +70,17 @@ def _kij(Q, eb, zp, ps, es):
     return _warps(eb * Q ** 3, f)
 
 
-def _sweep(X, Y, Z, d, NO, eb, zp, ps, es):
+def _sweep(X, Y, Z, d, NO, eb, zp, ps, es, reads=True, writes=True, nread=None):
     """Accesses of a sweep along direction d of an (X, Y, Z) box into extent
-    NO (the line enumeration of sweep / sweep_eo / sweep_eor)."""
+    NO (the line enumeration of sweep / sweep_eo / sweep_eor): the NI reads
+    and the NO writes of every line (or only one side, or nread reads)."""
     NI = (X, Y, Z)[d]
     LB = Y if d == 2 else Z
     L = X * Y * Z // NI
     sd = ps if d == 0 else (zp if d == 1 else 1)
     out = []
-    for n in list(range(NI)) + list(range(NO)):
+    idx = (list(range(nread if nread is not None else NI)) if reads else []) + (list(range(NO)) if writes else [])
+    for n in idx:
         def f(w, n=n):
             e, l = divmod(w, L)
             a, b = divmod(l, LB)
@@ -90,7 +92,8 @@ def _sweep(X, Y, Z, d, NO, eb, zp, ps, es):
 
 def walks(op: int, Q: int, eb: int, zp: int, ps: int, es: int):
     """(weight, warps) of one batch of eb elements.  op 5: BK5 (Q points);
-    op 3: BK3 (P = Q - 1 nodes, Q points)."""
+    op 3: BK3 (P = Q - 1 nodes, Q points); op 31: BK3's flow fused along k
+    for the FP32-storage forms."""
     if op == 5:
         yield 4, _dense(Q, Q, Q, eb, zp, ps, es)         # load u, last pass (3 reads)
         yield 6, _kij(Q, eb, zp, ps, es)                 # pointwise: 3 reads, 3 writes
@@ -99,14 +102,30 @@ def walks(op: int, Q: int, eb: int, zp: int, ps: int, es: int):
             yield 1, _sweep(Q, Q, Q, d, Q, eb, zp, ps, es)
         return
     P = Q - 1
-    yield 2, _dense(P, P, P, eb, zp, ps, es)             # load u, store v
-    for _ in range(2):                                   # interpolation and its transpose
-        yield 1, _sweep(P, P, P, 0, Q, eb, zp, ps, es)
-        yield 1, _sweep(Q, P, P, 1, Q, eb, zp, ps, es)
-        yield 1, _sweep(Q, Q, P, 2, Q, eb, zp, ps, es)
-    for d in range(3):
-        yield 2, _sweep(Q, Q, Q, d, Q, eb, zp, ps, es)
-    yield 6, _dense(Q, Q, Q, eb, zp, ps, es)             # pointwise
+    if op == 3:
+        yield 2, _dense(P, P, P, eb, zp, ps, es)         # load u, store v
+        for _ in range(2):                               # interpolation and its transpose
+            yield 1, _sweep(P, P, P, 0, Q, eb, zp, ps, es)
+            yield 1, _sweep(Q, P, P, 1, Q, eb, zp, ps, es)
+            yield 1, _sweep(Q, Q, P, 2, Q, eb, zp, ps, es)
+        for d in range(3):
+            yield 2, _sweep(Q, Q, Q, d, Q, eb, zp, ps, es)
+        yield 6, _dense(Q, Q, Q, eb, zp, ps, es)         # pointwise
+        return
+    # op 31: BK3's even-odd flow fused along k, u and v straight from/to the
+    # stage and HBM (the FP32-storage forms)
+    yield 1, _sweep(P, P, P, 0, Q, eb, zp, ps, es, reads=False)          # first interpolation: writes
+    yield 1, _sweep(Q, P, P, 1, Q, eb, zp, ps, es)                       # second
+    yield 1, _sweep(Q, Q, P, 2, Q, eb, zp, ps, es, writes=False)         # k line: P reads
+    yield 2, _sweep(Q, Q, Q, 2, Q, eb, zp, ps, es, reads=False)          # ... u and qt written
+    for d in (0, 1):                                                     # gradient, transposed
+        yield 1, _sweep(Q, Q, Q, d, Q, eb, zp, ps, es)
+        yield 1, _sweep(Q, Q, Q, d, Q, eb, zp, ps, es)
+    yield 6, _dense(Q, Q, Q, eb, zp, ps, es)                             # pointwise
+    yield 3, _sweep(Q, Q, Q, 2, Q, eb, zp, ps, es, writes=False)         # k line: three terms read
+    yield 1, _sweep(Q, Q, P, 2, P, eb, zp, ps, es, reads=False)          # ... P written
+    yield 1, _sweep(Q, Q, P, 1, P, eb, zp, ps, es)                       # back along j
+    yield 1, _sweep(Q, P, P, 0, P, eb, zp, ps, es, writes=False)         # back along i: reads
 
 
 def score(op: int, Q: int, eb: int, vbytes: int, zp: int, ps: int, es: int) -> float:
@@ -138,6 +157,7 @@ EBS = {
     (5, 8): {2: [16], 3: [16, 14], 4: [8], 5: [4, 5], 6: [4, 3], 7: [2], 8: [2, 1], 9: [3, 1]},
     (3, 4): {3: [16], 4: [8], 5: [6], 6: [4], 7: [3], 8: [1], 9: [1], 10: [1]},
     (3, 8): {3: [12], 4: [8], 5: [8], 6: [3], 7: [3], 8: [1], 9: [3], 10: [1]},
+    (31, 4): {3: [16], 4: [8], 5: [6], 6: [4], 7: [3], 8: [1], 9: [1], 10: [1]},
 }
 
 
@@ -161,7 +181,7 @@ def search(op: int, Q: int, vbytes: int):
 
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
-    ap.add_argument("--op", type=int, choices=(3, 5), default=5)
+    ap.add_argument("--op", type=int, choices=(3, 5, 31), default=5)
     ap.add_argument("--vbytes", type=int, choices=(4, 8), default=4)
     args = ap.parse_args(argv)
     for Q in sorted(EBS[(args.op, args.vbytes)]):
