@@ -495,28 +495,35 @@ def run_helmholtz(args):
     plan.apply(G, M, 1.0, ustar, f, prec=bk.PREC_FP64)
     u32, v32, v64 = ustar.float(), torch.empty(plan.n, dtype=torch.float32, device="cuda"), torch.empty_like(ustar)
     steps, warm = max(args.steps // 4, 10), max(args.warmup, 3)
-    m_multi = _events_ms(lambda: plan.apply(G32, M32, 1.0, u32, v32, prec=bk.PREC_MIXED), steps, warm, torch)
-    m_multi64 = _events_ms(lambda: plan.apply(G, M, 1.0, ustar, v64, prec=bk.PREC_FP64), max(3, steps // 4), 2, torch)
+    # every apply below is timed as one CUDA graph of its launches (device
+    # time: the seven per-order launches of a Python loop would otherwise be
+    # timed behind the host)
+    m_multi = _events_ms(lambda: plan.apply(G32, M32, 1.0, u32, v32, prec=bk.PREC_MIXED), steps, warm, torch,
+                         graph=True)
+    m_multi64 = _events_ms(lambda: plan.apply(G, M, 1.0, ustar, v64, prec=bk.PREC_FP64), max(3, steps // 4), 2,
+                           torch, graph=True)
+    Dp = {p: bk.bk5_matrices(p)[0] for p in plan.p}
 
     def per_order(prec, GG, MM, uu, vv):
         for kk, p in enumerate(plan.p):
             q, E = p + 1, plan.E[kk]
             su = slice(plan.uoff[kk], plan.uoff[kk] + E * q ** 3)
             sg = slice(plan.goff[kk], plan.goff[kk] + 6 * E * q ** 3)
-            bk.bk5_apply(p, E, bk.bk5_matrices(p)[0], GG[sg], uu[su], vv[su], prec=prec,
-                         layout=bk.LAYOUT_COLUMN, mass=MM[su], lam=1.0)
+            bk.bk5_apply(p, E, Dp[p], GG[sg], uu[su], vv[su], prec=prec, layout=bk.LAYOUT_COLUMN, mass=MM[su],
+                         lam=1.0)
 
     aligned = all((o * 8) % 16 == 0 for o in plan.uoff) and all((o * 8) % 16 == 0 for o in plan.goff)
-    m_per64 = _events_ms(lambda: per_order(bk.PREC_FP64, G, M, ustar, v64), max(3, steps // 4), 2, torch) \
-        if aligned else None
+    m_per64 = _events_ms(lambda: per_order(bk.PREC_FP64, G, M, ustar, v64), max(3, steps // 4), 2, torch,
+                         graph=True) if aligned else None
     aligned32 = all((o * 4) % 16 == 0 for o in plan.uoff) and all((o * 4) % 16 == 0 for o in plan.goff)
-    m_per32 = _events_ms(lambda: per_order(bk.PREC_MIXED, G32, M32, u32, v32), steps, warm, torch) \
+    m_per32 = _events_ms(lambda: per_order(bk.PREC_MIXED, G32, M32, u32, v32), steps, warm, torch, graph=True) \
         if aligned32 else None
     # the column body of the same launch (tiles tuned for it)
     best_col = tune.tune(orders, kernel=bk.KERNEL_COLUMN)
     plan_col = hz.HelmholtzPlan([(p, E, best_col[p]) for p, E in orders])
     plan_col.set_kernel(bk.KERNEL_COLUMN)
-    m_col = _events_ms(lambda: plan_col.apply(G32, M32, 1.0, u32, v32, prec=bk.PREC_MIXED), steps, warm, torch)
+    m_col = _events_ms(lambda: plan_col.apply(G32, M32, 1.0, u32, v32, prec=bk.PREC_MIXED), steps, warm, torch,
+                       graph=True)
     plan_col.close()
     x = torch.zeros_like(ustar)
     plan.cg(G, M, G32, M32, 1.0, f, x, rtol=1e-10, allow_noconv=True)   # builds the graph

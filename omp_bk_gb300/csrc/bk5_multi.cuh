@@ -240,8 +240,8 @@ inline int multi_wbox_bytes(int q, int eb, int vbytes)
 }
 
 // Shared memory of the even-odd launch: u stage (followed by the mass stage,
-// of the same size), G stage, three work boxes (each the largest tile's), one
-// mbarrier.
+// of the same size), G stage (FP64 forms only), three work boxes (each the
+// largest tile's), one mbarrier.
 template <class Eng>
 inline void multi_eo_smem(const MultiSeg* seg, int nseg, int& u_bytes, int& g_bytes, int& w_bytes, int& total)
 {
@@ -252,7 +252,8 @@ inline void multi_eo_smem(const MultiSeg* seg, int nseg, int& u_bytes, int& g_by
     w_bytes = 16;
     for (int s = 0; s < nseg; ++s) {
         const int q = seg[s].q, eb = seg[s].eb, q3 = q * q * q;
-        const int ub = stage_bytes<S>(eb * q3), gb = stage_bytes<S>(eb * 6 * q3);
+        // FP32 storage: G is read straight from HBM (no G stage)
+        const int ub = stage_bytes<S>(eb * q3), gb = (sizeof(S) == 4) ? 16 : stage_bytes<S>(eb * 6 * q3);
         const int wb = (multi_wbox_bytes(q, eb, int(sizeof(V))) + 15) / 16 * 16;
         u_bytes = ub > u_bytes ? ub : u_bytes;
         g_bytes = gb > g_bytes ? gb : g_bytes;
@@ -273,6 +274,10 @@ __global__ void __launch_bounds__(NT, MINB)
 {
     using S = typename Eng::S;
     using V = typename Eng::V;
+    // FP32 storage: the pointwise stage reads G straight from HBM (coalesced:
+    // G's column layout walks with the points), which leaves the largest
+    // stage out of shared memory and more blocks per SM; the FP64 forms stage it
+    constexpr bool GD = sizeof(S) == 4;
     extern __shared__ __align__(16) unsigned char smem[];
     unsigned char* ustage = smem;
     unsigned char* mstage = smem + u_bytes;
@@ -298,6 +303,7 @@ __global__ void __launch_bounds__(NT, MINB)
     // copied while the current tile finishes its transposed sweeps, u and the
     // mass (read by the last pass) right after
     auto issue_g = [&](int t) {
+        if constexpr (GD) return;
         const MultiTile tl = tiles[t];
         const MultiSeg& sg = prm.seg[tl.seg];
         const int q3 = sg.q * sg.q * sg.q;
@@ -332,7 +338,7 @@ __global__ void __launch_bounds__(NT, MINB)
         const int tn = t + gridDim.x;
         S* vb = v + sg.uoff + tl.e_first * q3;
         const S* ub = us;
-        const S* gb = gs;
+        const S* gb = GD ? G + sg.goff + tl.e_first * 6 * q3 : gs;
         const S* mb = ms;
         auto early = [&]() {
             if (tn < ntiles) issue_g(tn);
