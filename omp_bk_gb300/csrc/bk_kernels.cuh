@@ -81,10 +81,11 @@ constexpr int bk5_box(int q, int vbytes, int what)   // what: 0 ZP, 1 PS, 2 elem
 // the same model over their walks (the dense P^3 load and store, the
 // interpolation sweeps through the (Q,P,P) and (Q,Q,P) boxes and back, the
 // gradient sweeps and the dense pointwise walk; box_model.py --op 3).  At
-// 4-byte Q = 8 the model ties the first strides with {8, 71, 568}; the
-// first strides measured faster (BK3 p=6 mixed 87.6 against 83.0 GDoF/s)
-// and are kept.  Model wavefronts per access, Q = 3..10, against the first
-// strides:
+// 4-byte Q = 8 the model of the flow fused along k (--op 31, the FP32
+// forms' BK3 since the fusion) picks {8, 71, 568}: BK3 p=6 mixed 110.2
+// against 109.8 GDoF/s with the first strides (before the fusion the same
+// box had measured 83.0 against 87.6).  Model wavefronts per access,
+// Q = 3..10, against the first strides:
 //   4-byte values: 1.45 1.55 1.48 1.67 1.64 1.49 1.31 1.48
 //                 (2.49 2.21 1.96 1.86 1.73 1.49 1.61 1.81)
 //   8-byte values: 1.44 1.25 1.43 1.58 1.58 1.55 1.40 1.47
@@ -93,7 +94,7 @@ constexpr int bk3_box(int q, int vbytes, int what)   // what: 0 ZP, 1 PS, 2 elem
 {
     // {ZP, PS, element stride} for q = 3..10
     constexpr int b4[8][3] = {{3, 9, 27}, {4, 19, 80}, {5, 25, 125}, {6, 36, 216},
-                              {7, 49, 343}, {9, 72, 576}, {9, 81, 729}, {10, 105, 1050}};
+                              {7, 49, 343}, {8, 71, 568}, {9, 81, 729}, {10, 105, 1050}};
     constexpr int b8[8][3] = {{3, 9, 27}, {4, 19, 76}, {5, 25, 125}, {9, 54, 324},
                               {7, 54, 385}, {9, 72, 576}, {9, 81, 729}, {10, 105, 1050}};
     return (q < 3 || q > 10) ? (what == 0 ? box_zp(q) : (what == 1 ? box_ps(q, vbytes) : q * box_ps(q, vbytes)))
