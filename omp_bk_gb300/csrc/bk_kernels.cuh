@@ -5,24 +5,26 @@
 //   1. stage: the batch's slices of u and of the geometric data (qdata or G)
 //      are contiguous in HBM (element-major E-vectors); each is copied into
 //      shared memory by one 1-D TMA bulk copy (cp.async.bulk, completion on an
-//      mbarrier with a bounded wait).  The copy starts at the first 16-byte
-//      boundary of the slice; the few values before it and after the last
-//      boundary are loaded by threads, so any element count and any odd
-//      extent is staged without an alignment condition on the batch.
+//      mbarrier with a bounded wait), rounded out to 16-byte boundaries inside
+//      the array, so any element count and any odd extent is staged without
+//      synchronous loads (stage_issue).
 //   2. load pass: u is converted to the working type (float-float split for
-//      the FP64 engine) into a padded work box.
+//      the FP64 engine) into a padded work box -- or, for BK1/BK3 forms that
+//      need no conversion, read by the first interpolation straight from the
+//      stage.
 //   3. sweeps: every 1-D contraction (interpolation with B, derivative with
 //      D, and their transposes) is a "sweep" of one direction: one thread per
 //      line of the box loads the line into registers, forms all outputs of the
-//      line and writes them back.  The 1-D matrices are kernel parameters
-//      (__grid_constant__), so every coefficient is an operand of the FMA
-//      straight from the constant bank.
+//      line and writes them back.  Steps along k, whose lines one thread owns,
+//      are chained in registers (kline_pass).  The 1-D matrices are kernel
+//      parameters (__grid_constant__), so every coefficient is an operand of
+//      the FMA straight from the constant bank.
 //   4. pointwise: qdata (BK1) or G (BK3, BK5, with the optional coefficient k
 //      of BK3) at every quadrature point.
-//   5. the result is assembled densely in shared memory and written to HBM
-//      with coalesced stores.
-// Work boxes are padded (row stride ZP, plane stride PS) so that the
-// thread-per-line accesses of all three directions spread over the 32 banks.
+//   5. the result is written to HBM with coalesced stores (from the box, or
+//      from the last interpolation's registers).
+// Work boxes are padded (row stride ZP, plane stride PS, element stride) per
+// Q from a model of the warps' shared-memory wavefronts (bk5_box, bk3_box).
 #pragma once
 
 #include <cstdint>
