@@ -198,6 +198,16 @@ int bk3_adjoint(int p, int64_t E, const double* B, const double* D, const void* 
                 const void* u, const void* res, void* dk, void* dG, const bk_options* opt,
                 bk_stream_t stream);
 
+/* make_bk5_G on the device (replaces include/bk_harness.h:220-244): G6i,
+ * the six symmetric factors interleaved as BK5.cpp stores them,
+ * G6i(e, i, j, s, k) (g6i_index, bk_harness.h:210), into G with nfactors = 6
+ * (rr rs rt ss st tt) or 9 (the full 3 x 3 tensor, row-major, bk5_sym :215)
+ * in layout 0, 1 or 2 (bk_layout), for BK5 with Q = p + 1 points per
+ * direction.  Both in the storage type of prec (double for FP64, float
+ * otherwise), device, 16-byte aligned, distinct.  Asynchronous on stream. */
+int bk5_make_g(int p, int64_t E, const void* G6i, void* G, int nfactors, int layout, int prec,
+               bk_stream_t stream);
+
 /* Splits n doubles G (device) into float-float pairs Gff (device, n x 8
  * bytes; may be G itself: the conversion is in place value by value): hi =
  * the value truncated to 24 significant bits, lo = the rest rounded to a

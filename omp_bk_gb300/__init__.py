@@ -47,7 +47,7 @@ EXPORTS = [
     "bk_hplan_create", "bk_hplan_destroy", "bk_hplan_size", "bk_hplan_set_kernel", "bk_hplan_apply", "bk_hplan_cg",
     "bk_dot_noalloc",
     "bk_host_plan_create", "bk_host_plan_destroy", "bk1_apply_host", "bk3_apply_host", "bk5_apply_host",
-    "bk_g_to_ff",
+    "bk_g_to_ff", "bk5_make_g",
 ]
 
 
@@ -109,6 +109,7 @@ def lib():
         "bk_dot": [C.c_longlong, _vp, _vp, C.c_int, _vp, _vp, C.c_longlong, C.c_int, _vp],
         "bk_axpby": [C.c_longlong, C.c_double, _vp, C.c_double, _vp, C.c_int, _vp],
         "bk_g_to_ff": [_vp, _vp, _i64, _vp],
+        "bk5_make_g": [C.c_int, _i64, _vp, _vp, C.c_int, C.c_int, C.c_int, _vp],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -210,6 +211,19 @@ def bk5_apply(p, E, D, G, u, v, prec=PREC_FP64, engine=ENGINE_AUTO, layout=LAYOU
                      elems_per_block=elems_per_block, gform=gform).c()
     check(lib().bk5_apply_ex(p, E, Dp, _ptr(G), _ptr(u), _ptr(mass), float(lam), _ptr(v), C.byref(o),
                              _stream(stream)), "bk5_apply")
+
+
+def bk5_make_g(p, E, G6i, nfactors=6, layout=LAYOUT_COLUMN, out=None, stream=None):
+    """make_bk5_G (include/bk_harness.h:220-244) on the device: G6i in
+    BK5.cpp's interleaved layout G6i(e, i, j, s, k) -> G with nfactors (6 or
+    9) in `layout`; float64 tensors for FP64, float32 for the FP32 forms."""
+    import torch
+    q = p + 1
+    if out is None:
+        out = torch.empty(E * nfactors * q ** 3, dtype=G6i.dtype, device=G6i.device)
+    prec = PREC_FP64 if G6i.dtype == torch.float64 else PREC_FP32
+    check(lib().bk5_make_g(p, E, _ptr(G6i), _ptr(out), nfactors, layout, prec, _stream(stream)), "bk5_make_g")
+    return out
 
 
 def g_to_ff(G, out=None, stream=None):

@@ -121,6 +121,54 @@ __global__ void g_to_ff_kernel(const double* G, bkg::ff2* out, long long n)
     }
 }
 
+// make_bk5_G on the device: one block per element (grid-stride), the
+// element's six interleaved factors G6i(i, j, s, k) staged in shared memory
+// with coalesced loads, the F factors of the target layout written with
+// coalesced stores.  Full tensor (F = 9, row-major): factor f = (a, b) is the
+// stored symmetric factor of (min(a, b), max(a, b)).
+template <class T>
+__global__ void make_g_kernel(const T* __restrict__ g6i, T* __restrict__ g, long long E, int q, int F, int layout)
+{
+    extern __shared__ __align__(16) unsigned char sm[];
+    T* s = reinterpret_cast<T*>(sm);
+    const int q2 = q * q, q3 = q2 * q, n6 = 6 * q3, nf = F * q3;
+    for (long long e = blockIdx.x; e < E; e += gridDim.x) {
+        const T* src = g6i + e * n6;
+        for (int x = threadIdx.x; x < n6; x += blockDim.x) s[x] = src[x];
+        __syncthreads();
+        T* dst = g + e * nf;
+        for (int y = threadIdx.x; y < nf; y += blockDim.x) {
+            int f, i, j, k;
+            if (layout == 0) {   // (f, i, j, k)
+                f = y / q3;
+                const int r = y - f * q3;
+                i = r / q2;
+                j = (r - i * q2) / q;
+                k = r - i * q2 - j * q;
+            } else if (layout == 1) {   // (i, j, f, k)
+                k = y % q;
+                const int r = y / q;
+                f = r % F;
+                j = (r / F) % q;
+                i = r / (F * q);
+            } else {   // (f, k, i, j)
+                j = y % q;
+                i = (y / q) % q;
+                k = (y / q2) % q;
+                f = y / q3;
+            }
+            int sf = f;
+            if (F == 9) {
+                const int a = f / 3, b = f - 3 * (f / 3);
+                const int lo = a < b ? a : b, hi = a < b ? b : a;
+                sf = (lo == 0) ? hi : (lo == 1 ? hi + 2 : 5);
+            }
+            dst[y] = s[((i * q + j) * 6 + sf) * q + k];
+        }
+        __syncthreads();
+    }
+}
+
 int ok() { return cudaGetLastError() == cudaSuccess ? BK_OK : BK_ERR_CUDA; }
 
 int dot_blocks(long long n)
@@ -194,6 +242,31 @@ int bk_axpby(long long n, double a, const void* x, double b, void* y, int f64, b
         axpby_kernel<double><<<g, 256, 0, s>>>(n, a, static_cast<const double*>(x), b, static_cast<double*>(y));
     else
         axpby_kernel<float><<<g, 256, 0, s>>>(n, a, static_cast<const float*>(x), b, static_cast<float*>(y));
+    return ok();
+}
+
+int bk5_make_g(int p, int64_t E, const void* G6i, void* G, int nfactors, int layout, int prec, bk_stream_t stream)
+{
+    if (p < 1 || p > 8) return BK_ERR_ORDER;
+    if (E < 0) return BK_ERR_SIZE;
+    if ((nfactors != 6 && nfactors != 9) || layout < 0 || layout > 2) return BK_ERR_PREC;
+    if (prec != BK_PREC_FP64 && prec != BK_PREC_FP32 && prec != BK_PREC_MIXED) return BK_ERR_PREC;
+    if (E == 0) return BK_OK;
+    if (!G6i || !G) return BK_ERR_NULL;
+    if ((reinterpret_cast<uintptr_t>(G6i) | reinterpret_cast<uintptr_t>(G)) & 15) return BK_ERR_ALIGN;
+    const int q = p + 1;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long cap = 8LL * sms;
+    const int grid = int(E < cap ? E : cap);
+    if (prec == BK_PREC_FP64)
+        make_g_kernel<double><<<grid, 256, 6 * q * q * q * sizeof(double), s>>>(
+            static_cast<const double*>(G6i), static_cast<double*>(G), E, q, nfactors, layout);
+    else
+        make_g_kernel<float><<<grid, 256, 6 * q * q * q * sizeof(float), s>>>(
+            static_cast<const float*>(G6i), static_cast<float*>(G), E, q, nfactors, layout);
     return ok();
 }
 

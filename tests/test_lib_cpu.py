@@ -73,6 +73,15 @@ def test_host_argument_errors(bklib):
     assert L.bk_g_to_ff(None, a16, 4, None) == bklib.BK_ERR_NULL
     assert L.bk_g_to_ff(a16, a8, 4, None) == bklib.BK_ERR_ALIGN
     assert L.bk_g_to_ff(None, None, 0, None) == bklib.BK_OK
+    # device make_bk5_G: order, factor count, layout, precision, pointers
+    assert L.bk5_make_g(9, 4, a16, a16, 6, 2, 0, None) == bklib.BK_ERR_ORDER
+    assert L.bk5_make_g(3, -1, a16, a16, 6, 2, 0, None) == bklib.BK_ERR_SIZE
+    assert L.bk5_make_g(3, 4, a16, a16, 7, 2, 0, None) == bklib.BK_ERR_PREC
+    assert L.bk5_make_g(3, 4, a16, a16, 6, 3, 0, None) == bklib.BK_ERR_PREC
+    assert L.bk5_make_g(3, 4, a16, a16, 6, 2, 9, None) == bklib.BK_ERR_PREC
+    assert L.bk5_make_g(3, 4, None, a16, 6, 2, 0, None) == bklib.BK_ERR_NULL
+    assert L.bk5_make_g(3, 4, a16, a8, 9, 0, 0, None) == bklib.BK_ERR_ALIGN
+    assert L.bk5_make_g(3, 0, None, None, 6, 2, 0, None) == bklib.BK_OK
     # E = 0 is a no-op, even with null device pointers
     assert L.bk5_apply(3, 0, dp, None, None, None, 0, None) == bklib.BK_OK
     assert L.bk1_apply(8, 0, dp, None, None, None, 0, None) == bklib.BK_OK

@@ -365,3 +365,41 @@ def test_bk3_split_g_is_bitwise(bklib, p, coef):
     assert torch.equal(v0, v1)
     with pytest.raises(bklib.BKError, match="precision"):
         bklib.bk3_apply(p, E, B, D, g, u, v1, prec=bklib.PREC_MIXED, gform=bklib.G_FF)
+
+
+@pytest.mark.parametrize("p", [1, 3, 6, 7, 8])
+@pytest.mark.parametrize("nfactors", [6, 9])
+@pytest.mark.parametrize("layout", [0, 1, 2])
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_bk5_make_g_matches_oracle(bklib, p, nfactors, layout, prec):
+    """The device make_bk5_G is a permutation (and, for 9 factors, a
+    duplication) of G6i: bitwise the oracle's restatement of
+    include/bk_harness.h:220-244."""
+    E = 5
+    q = p + 1
+    g6i = np.random.default_rng(500 + p).uniform(-1, 1, E * 6 * q ** 3)
+    ref = oracle.make_bk5_G(g6i, E, q, nfactors, layout)
+    src = dev(g6i, prec)
+    out = bklib.bk5_make_g(p, E, src, nfactors=nfactors, layout=layout)
+    torch.cuda.synchronize()
+    want = ref if prec == "f64" else ref.astype(np.float32).astype(np.float64)
+    assert np.array_equal(host(out), want)
+
+
+def test_bk5_make_g_feeds_the_apply(bklib):
+    """G6i relaid on the device to each layout, 6 and 9 factors: the BK5
+    apply agrees with the oracle on the interleaved G6."""
+    p, E = 7, 6
+    q = p + 1
+    D, _, _ = bklib.bk5_matrices(p)
+    rng = np.random.default_rng(9)
+    u = rng.uniform(-1, 1, E * q ** 3)
+    g6i = rng.uniform(0.5, 1.5, E * 6 * q ** 3)
+    ref = oracle.bk5(q, E, D, g6i, u)
+    for nf in (6, 9):
+        for layout in (0, 1, 2):
+            G = bklib.bk5_make_g(p, E, dev(g6i, "f64"), nfactors=nf, layout=layout)
+            v = torch.empty(E * q ** 3, dtype=torch.float64, device="cuda")
+            bklib.bk5_apply(p, E, D, G, dev(u, "f64"), v, layout=layout, nfactors=nf)
+            torch.cuda.synchronize()
+            assert oracle.rel_maxdiff(host(v), ref) < TOL64, (nf, layout)
