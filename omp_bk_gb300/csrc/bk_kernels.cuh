@@ -252,13 +252,44 @@ inline bool make_eo(const double* m, bool trans, EOMat<C, Q>& out, Conv conv)
 // Even-odd sweep of direction DIR of a Q x Q x Q box (in == out allowed);
 // see EOMat.  When ADD is set, out(o) = M x + X(o) + Y(o) for the lines of
 // direction 2 (BK5's last transposed derivative plus the other two terms).
+// The Q outputs y of one line x through the square even-odd form m (see
+// EOMat); x and y are register arrays of the caller.
+template <class Eng, int Q, class EM>
+__device__ __forceinline__ void eo_line(const typename Eng::V (&x)[Q], typename Eng::V (&y)[Q], const EM& m)
+{
+    using V = typename Eng::V;
+    using A = typename Eng::A;
+    constexpr int H = Q / 2;
+    V ev[H > 0 ? H : 1], dv[H > 0 ? H : 1];
+#pragma unroll
+    for (int n = 0; n < H; ++n) {
+        ev[n] = Eng::vadd_in(x[n], x[Q - 1 - n]);
+        dv[n] = Eng::vsub_in(x[n], x[Q - 1 - n]);
+    }
+#pragma unroll
+    for (int o = 0; o < H; ++o) {
+        A aa = Eng::first(m.A[o * H], ev[0]), bb = Eng::first(m.B[o * H], dv[0]);
+#pragma unroll
+        for (int n = 1; n < H; ++n) {
+            Eng::madd(aa, m.A[o * H + n], ev[n]);
+            Eng::madd(bb, m.B[o * H + n], dv[n]);
+        }
+        if (Q & 1) Eng::madd(aa, m.c[o], x[H]);
+        Eng::sum_diff(aa, bb, y[o], y[Q - 1 - o]);   // a + b, b - a
+    }
+    if constexpr ((Q & 1) != 0) {
+        A t = Eng::first(m.r[0], dv[0]);
+#pragma unroll
+        for (int n = 1; n < H; ++n) Eng::madd(t, m.r[n], dv[n]);
+        y[H] = Eng::result(t);
+    }
+}
+
 template <class Eng, class WB, int DIR, int Q, class EM>
 __device__ __forceinline__ void sweep_eo(const typename Eng::V* in, typename Eng::V* out, int ne, const EM& m,
                                          int tid, int nt)
 {
     using V = typename Eng::V;
-    using A = typename Eng::A;
-    constexpr int H = Q / 2;
     constexpr int LB = Q;
     constexpr int L = Q * Q;
     constexpr int SD = DIR == 0 ? WB::PS : (DIR == 1 ? WB::ZP : 1);
@@ -269,35 +300,12 @@ __device__ __forceinline__ void sweep_eo(const typename Eng::V* in, typename Eng
         const int b = l - a * LB;
         int base = (DIR == 0) ? a * WB::ZP + b : (DIR == 1 ? a * WB::PS + b : a * WB::PS + b * WB::ZP);
         base += e * WB::size;
-        V x[Q];
+        V x[Q], y[Q];
 #pragma unroll
         for (int n = 0; n < Q; ++n) x[n] = in[base + n * SD];
-        V ev[H > 0 ? H : 1], dv[H > 0 ? H : 1];
+        eo_line<Eng, Q>(x, y, m);
 #pragma unroll
-        for (int n = 0; n < H; ++n) {
-            ev[n] = Eng::vadd_in(x[n], x[Q - 1 - n]);
-            dv[n] = Eng::vsub_in(x[n], x[Q - 1 - n]);
-        }
-#pragma unroll
-        for (int o = 0; o < H; ++o) {
-            A aa = Eng::first(m.A[o * H], ev[0]), bb = Eng::first(m.B[o * H], dv[0]);
-#pragma unroll
-            for (int n = 1; n < H; ++n) {
-                Eng::madd(aa, m.A[o * H + n], ev[n]);
-                Eng::madd(bb, m.B[o * H + n], dv[n]);
-            }
-            if (Q & 1) Eng::madd(aa, m.c[o], x[H]);
-            V s, d;
-            Eng::sum_diff(aa, bb, s, d);   // a + b, b - a
-            out[base + o * SD] = s;
-            out[base + (Q - 1 - o) * SD] = d;
-        }
-        if (Q & 1) {
-            A t = Eng::first(m.r[0], dv[0]);
-#pragma unroll
-            for (int n = 1; n < H; ++n) Eng::madd(t, m.r[n], dv[n]);
-            out[base + H * SD] = Eng::result(t);
-        }
+        for (int o = 0; o < Q; ++o) out[base + o * SD] = y[o];
     }
 }
 
@@ -701,6 +709,13 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
     const Mat<typename Eng::C, Q, false> Dm{Dp};   // D(i, n)
     const Mat<typename Eng::C, Q, true> Dt{Dp};    // D(n, i)
     const S lam = S(lambda);
+    // the k-direction transposed sweep fused into the last pass (even-odd,
+    // one thread per line): one write and one read of the box fewer and one
+    // barrier less (BK5 mixed q = 6, interleaved G: 113 -> 126 GDoF/s; the
+    // Helmholtz launch 100 -> 107).  Not for FP32 storage at Q = 8, where
+    // the apply runs at the HBM roofline and a thread's Q consecutive stores
+    // (strided across the warp) cost more than the traffic saved (199 -> 190)
+    constexpr bool KFUSE = EO && DPAR == 0 && !(sizeof(S) == 4 && Q == 8);
     // thread group of the direction-parallel stages
     const int ntd = DPAR ? nt / 3 : nt;
     const int grp = DPAR ? tid / ntd : 0;
@@ -778,8 +793,9 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
     } else if constexpr (EO) {
         sweep_eo<Eng, WB, 0, Q>(W0, W0, ne, eot, tid, nt);
         sweep_eo<Eng, WB, 1, Q>(W1, W1, ne, eot, tid, nt);
-        __syncthreads();
-        sweep_eo<Eng, WB, 2, Q>(W2, W2, ne, eot, tid, nt);
+        // the k direction: in registers in the last pass (KFUSE, below), or
+        // here
+        if constexpr (!KFUSE) sweep_eo<Eng, WB, 2, Q>(W2, W2, ne, eot, tid, nt);
     } else {
         sweep<Eng, WB, 0, Q, Q, Q, Q>(W0, W0, ne, Dt, tid, nt);
         sweep<Eng, WB, 1, Q, Q, Q, Q>(W1, W1, ne, Dt, tid, nt);
@@ -849,10 +865,43 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
             if constexpr (DOT) acc_madd_f(*dot, us[w], out);   // u . A u for CG, compensated
         }
     };
-    if (mb != nullptr)
-        last_pass(std::true_type{});
-    else
-        last_pass(std::false_type{});
+    // 7'. (KFUSE) one thread per k line: the transposed k-derivative of the
+    //    third flux in registers (no write and re-read of the box), the sum,
+    //    the mass term, each thread storing its line's Q values
+    auto kline_last = [&](auto with_mass) {
+        kline_pass<Eng, WB, Q, Q>(QT, ne, tid, nt, [&](int e, int i, int j, const V (&x)[Q], int base) {
+            V t[Q];
+            eo_line<Eng, Q>(x, t, eot);
+            const int w0 = e * Q3 + (i * Q + j) * Q;
+#pragma unroll
+            for (int o = 0; o < Q; ++o) {
+                V res;
+                if constexpr (HasSum3<Eng>::value) {
+                    res = Eng::sum3(t[o], W0[base + o], W1[base + o]);
+                } else {
+                    A acc = Eng::from(t[o]);
+                    Eng::add(acc, W0[base + o]);
+                    Eng::add(acc, W1[base + o]);
+                    res = Eng::loose(acc);   // store() renormalises
+                }
+                S out = Eng::store(res);
+                if constexpr (decltype(with_mass)::value) out += lam * mb[w0 + o] * us[w0 + o];
+                vb[w0 + o] = out;
+                if constexpr (DOT) acc_madd_f(*dot, us[w0 + o], out);
+            }
+        });
+    };
+    if constexpr (KFUSE) {
+        if (mb != nullptr)
+            kline_last(std::true_type{});
+        else
+            kline_last(std::false_type{});
+    } else {
+        if (mb != nullptr)
+            last_pass(std::true_type{});
+        else
+            last_pass(std::false_type{});
+    }
     __syncthreads();
 }
 
