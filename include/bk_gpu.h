@@ -123,7 +123,7 @@ enum bk_gform {
 enum bk_kernel_shape {
     BK_KERNEL_AUTO = 0,   /* the faster of the two as measured on GB300: the
                              column kernel for the FP32-storage forms at
-                             p <= 6 with G in the column layout, the sweep
+                             p <= 5 with G in the column layout, the sweep
                              kernel otherwise */
     BK_KERNEL_SWEEP = 1,  /* one thread per line of the box per 1-D contraction,
                              all intermediates in shared memory */

@@ -416,15 +416,15 @@ int BK_CAT(launch_bk5, BK_SFX)(int p, long long E, const double* D, const void* 
     if (p < 1 || p > 8) return BK_ERR_ORDER;
     if (gform != BK_G_STORAGE && kernel == BK_KERNEL_COLUMN) return BK_ERR_PREC;   // sweep kernel only
     // AUTO, as measured on GB300 (E_p = 2^(8-p) * 4096, with and without the
-    // mass term): the column kernel for the FP32-storage forms at p <= 6 with
+    // mass term): the column kernel for the FP32-storage forms at p <= 5 with
     // G in the column layout, which it reads straight from HBM; their sweeps
     // are bound by shared-memory traffic the column kernel keeps in registers
-    // (mixed p = 5: 136 against 110 GDoF/s).  The sweep kernel otherwise: at
-    // p = 7 (mixed 141 against 117), for the float-float engine at every p
-    // (34 against 25 at p = 5), and for the other layouts, where the column
-    // kernel re-lays G through shared memory (mixed q = 4 at 1e8 DoFs,
-    // interleaved G: 102 against 133)
-    const bool auto_col = (kernel == BK_KERNEL_AUTO) && !eng_is_ff() && !eng_is_dfma() && p <= 6 && layout == 2;
+    // (mixed p = 5: 136 against 118 GDoF/s).  The sweep kernel otherwise: at
+    // p >= 6 (p = 6 mixed: 122 against 110; p = 7: 147 against 117), for the
+    // float-float engine at every p (34 against 25 at p = 5), and for the
+    // other layouts, where the column kernel re-lays G through shared memory
+    // (mixed q = 4 at 1e8 DoFs, interleaved G: 102 against 133)
+    const bool auto_col = (kernel == BK_KERNEL_AUTO) && !eng_is_ff() && !eng_is_dfma() && p <= 5 && layout == 2;
     if (kernel == BK_KERNEL_SWEEP || (kernel == BK_KERNEL_AUTO && !auto_col)) {
         switch (layout) {
             case 0: return BK_CATL(bk5_sweep, BK_SFX, 0)(p, F, D, E, u, G, mass, lambda, v, gform, s);
