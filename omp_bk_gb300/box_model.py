@@ -93,13 +93,26 @@ def _sweep(X, Y, Z, d, NO, eb, zp, ps, es, reads=True, writes=True, nread=None):
 def walks(op: int, Q: int, eb: int, zp: int, ps: int, es: int):
     """(weight, warps) of one batch of eb elements.  op 5: BK5 (Q points);
     op 3: BK3 (P = Q - 1 nodes, Q points); op 31: BK3's flow fused along k
-    for the FP32-storage forms."""
+    for the FP32-storage forms; op 51: BK5 with the fused k-direction last
+    pass."""
     if op == 5:
         yield 4, _dense(Q, Q, Q, eb, zp, ps, es)         # load u, last pass (3 reads)
         yield 6, _kij(Q, eb, zp, ps, es)                 # pointwise: 3 reads, 3 writes
         for d in range(3):                               # gradient and transposed
             yield 1, _sweep(Q, Q, Q, d, Q, eb, zp, ps, es)
             yield 1, _sweep(Q, Q, Q, d, Q, eb, zp, ps, es)
+        return
+    if op == 51:
+        # BK5 with the k-direction last pass fused (KFUSE): the transposed
+        # k sweep and the dense last pass become one k-line pass reading
+        # the three terms
+        yield 1, _dense(Q, Q, Q, eb, zp, ps, es)         # load u
+        yield 6, _kij(Q, eb, zp, ps, es)                 # pointwise
+        for d in range(3):                               # gradient
+            yield 1, _sweep(Q, Q, Q, d, Q, eb, zp, ps, es)
+        for d in (0, 1):                                 # transposed i, j
+            yield 1, _sweep(Q, Q, Q, d, Q, eb, zp, ps, es)
+        yield 3, _sweep(Q, Q, Q, 2, Q, eb, zp, ps, es, writes=False)   # last pass: three k lines read
         return
     P = Q - 1
     if op == 3:
@@ -158,6 +171,7 @@ EBS = {
     (3, 4): {3: [16], 4: [8], 5: [6], 6: [4], 7: [3], 8: [1], 9: [1], 10: [1]},
     (3, 8): {3: [12], 4: [8], 5: [8], 6: [3], 7: [3], 8: [1], 9: [3], 10: [1]},
     (31, 4): {3: [16], 4: [8], 5: [6], 6: [4], 7: [3], 8: [1], 9: [1], 10: [1]},
+    (51, 4): {2: [12], 3: [12, 14], 4: [8, 8], 5: [4, 5], 6: [3, 3], 7: [2, 2], 9: [1, 1]},
 }
 
 
@@ -181,7 +195,7 @@ def search(op: int, Q: int, vbytes: int):
 
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
-    ap.add_argument("--op", type=int, choices=(3, 5, 31), default=5)
+    ap.add_argument("--op", type=int, choices=(3, 5, 31, 51), default=5)
     ap.add_argument("--vbytes", type=int, choices=(4, 8), default=4)
     args = ap.parse_args(argv)
     for Q in sorted(EBS[(args.op, args.vbytes)]):
