@@ -674,7 +674,13 @@ struct BK5Cfg {
 // the sum compensated (float-float: about 44 bits).  after_pw: called by every
 // thread after the pointwise stage, when the G stage is no longer read (nor
 // u, unless the mass term or dot reads it at the end).  Ends with a block
-// barrier (after which the stages may be reused).
+// barrier (after which the stages may be reused).  GS: the type G is stored
+// in (the storage type, or float-float pairs split ahead of time).
+//
+// Stages: load u into a box; gradient (three sweeps); pointwise fluxes;
+// transposed sweeps; last pass (sum of the three terms, mass term, store).
+// Even-odd without DPAR (KFUSE): the transposed k sweep and the last pass
+// are one pass over k lines in registers.
 //
 // DPAR (even-odd only): the three sweeps of a stage run at the same time on
 // three thread groups of nt/3 threads, one direction per group (warp-uniform
