@@ -443,6 +443,14 @@ def run_adjoint(args):
     steps, warm = max(args.steps // 4, 10), max(args.warmup, 3)
     mf = _events_ms(lambda: fwd(k, G, r), steps, warm, torch)
     mb = _events_ms(lambda: bk.bk3_adjoint(p, E, B, D, G, k, u, r, dk, dG), steps, warm, torch)
+    # the backward on G split once into float-float pairs (bitwise the same
+    # gradients)
+    Gff = bk.g_to_ff(G)
+    dk2, dG2 = torch.empty_like(dk), torch.empty_like(dG)
+    mbg = _events_ms(lambda: bk.bk3_adjoint(p, E, B, D, Gff, k, u, r, dk2, dG2, gform=bk.G_FF), steps, warm, torch)
+    bk.bk3_adjoint(p, E, B, D, G, k, u, r, dk, dG)
+    split_same = bool(torch.equal(dk, dk2) and torch.equal(dG, dG2))
+    del Gff, dk2, dG2
     ws = bk.dot_workspace(6 * E * Q ** 3)
     out = torch.zeros(1, dtype=torch.float64, device="cuda")
     fwd(k, G, r, bk.ENGINE_DFMA)
@@ -469,6 +477,7 @@ def run_adjoint(args):
           qdofs / mb / 1e6, mb, "f64",
           {"adjoint": {"backward_ms": mb, "forward_ms": mf, "backward_gpoints_s": qdofs / mb / 1e6,
                        "backward_hbm_gbs": 8 * (2 * E * P ** 3 + 14 * qdofs) / mb / 1e6,
+                       "backward_split_g_gpoints_s": qdofs / mbg / 1e6, "split_g_bitwise": split_same,
                        "fd_directions": 64, "fd_step": h, "fd_max_rel_err": worst},
            "unit_note": "value = quadrature points per second of the backward kernel (G points/s)"})
 

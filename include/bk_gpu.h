@@ -100,7 +100,7 @@ typedef struct bk_options {
                             sweep kernels use per-order tables measured on
                             GB300 and ignore it */
     int kernel;    /* bk_kernel_shape (BK5); BK1/BK3 have the sweep kernel only */
-    int gform;     /* bk_gform (BK5, BK3): how G is stored */
+    int gform;     /* bk_gform (BK5, BK3, the adjoint): how G is stored */
 } bk_options;
 
 /* Geometric-factor storage forms (BK5, BK3). */
@@ -114,9 +114,9 @@ enum bk_gform {
                          result is bitwise that of the double G.  FP64 with
                          engine AUTO or FF and the even-odd path: BK5 with 6
                          factors, D on points symmetric about 0 (GLL), sweep
-                         kernel; BK3 with B and D of GLL nodes and Gauss
-                         points.  Otherwise (and for BK1 and the adjoint,
-                         which take no split G) BK_ERR_PREC */
+                         kernel; BK3 and its adjoint with B and D of GLL
+                         nodes and Gauss points.  Otherwise (and for BK1,
+                         which takes no G) BK_ERR_PREC */
 };
 
 /* BK5 kernel shapes. */

@@ -360,13 +360,15 @@ def convert(src, dst, stream=None):
 
 # ---- adjoint, vector kernels ---------------------------------------------------
 
-def bk3_adjoint(p, E, B, D, G, k, u, res, dk, dG, prec=PREC_FP64, engine=ENGINE_AUTO, stream=None):
+def bk3_adjoint(p, E, B, D, G, k, u, res, dk, dG, prec=PREC_FP64, engine=ENGINE_AUTO, gform=G_STORAGE,
+                stream=None):
     """dL/dk (E x Q^3) and dL/dG (E x 6 x Q^3) of L = 1/2 |A(k) u - f|^2 given
-    res = A(k) u - f; the forward kernel is bk3_apply(..., k=k)."""
+    res = A(k) u - f; the forward kernel is bk3_apply(..., k=k).  gform=G_FF:
+    G holds the float-float pairs made by g_to_ff."""
     _order(p, "bk3_adjoint")
     Bh, Bp = _host(B)
     Dh, Dp = _host(D)
-    o = ApplyOptions(prec=prec, engine=engine).c()
+    o = ApplyOptions(prec=prec, engine=engine, gform=gform).c()
     check(lib().bk3_adjoint(p, E, Bp, Dp, _ptr(G), _ptr(k), _ptr(u), _ptr(res), _ptr(dk), _ptr(dG), C.byref(o),
                             _stream(stream)), "bk3_adjoint")
 

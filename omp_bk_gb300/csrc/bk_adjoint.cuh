@@ -90,15 +90,16 @@ __device__ __forceinline__ void grad_at_points(const typename Eng::S* src, typen
     __syncthreads();
 }
 
-template <class Eng, int Q, int EB, bool EO = false, int DPAR = 0>
+template <class Eng, int Q, int EB, bool EO = false, int DPAR = 0, class GS = typename Eng::S>
 __global__ void __launch_bounds__(BK3AdjCfg<Eng, Q, EB, DPAR>::NT)
     bk3_adjoint_kernel(const __grid_constant__ P13<typename Eng::C, Q> prm, const long long E,
                        const typename Eng::S* __restrict__ u, const typename Eng::S* __restrict__ res,
-                       const typename Eng::S* __restrict__ G, const typename Eng::S* __restrict__ kq,
+                       const GS* __restrict__ G, const typename Eng::S* __restrict__ kq,
                        typename Eng::S* __restrict__ dk, typename Eng::S* __restrict__ dG, const DevCtx ctx)
 {
     using Cfg = BK3AdjCfg<Eng, Q, EB, DPAR>;
     using S = typename Eng::S;
+    static_assert(sizeof(GS) == sizeof(S), "G is staged in the footprint of the storage type");
     using V = typename Eng::V;
     using A = typename Eng::A;
     using WB = typename Cfg::WB;
@@ -132,7 +133,7 @@ __global__ void __launch_bounds__(BK3AdjCfg<Eng, Q, EB, DPAR>::NT)
     // arrives): the copies overlap the products and the gradients.
     const S* us = nullptr;
     const S* rs = nullptr;
-    const S* gs = nullptr;
+    const GS* gs = nullptr;
     const S* ks = nullptr;
     auto issue_ur = [&](long long bt, bool arrive) {
         const long long e0 = bt * EB;
@@ -153,7 +154,7 @@ __global__ void __launch_bounds__(BK3AdjCfg<Eng, Q, EB, DPAR>::NT)
         const int ne = int((E - e0) < EB ? (E - e0) : EB);
         uint32_t tx = 0;
         if (tid == 0) fence_proxy_async();
-        gs = stage_issue<S>(gstage, G + e0 * 6 * Q3, ne * 6 * Q3, G + E * 6 * Q3, bar, tx, tid, nt);
+        gs = stage_issue<GS>(gstage, G + e0 * 6 * Q3, ne * 6 * Q3, G + E * 6 * Q3, bar, tx, tid, nt);
         ks = stage_issue<S>(kstage, kq + e0 * Q3, ne * Q3, kq + E * Q3, bar, tx, tid, nt);
         if (tid == 0) mbar_arrive_expect_tx(bar, tx);
     };
@@ -179,7 +180,7 @@ __global__ void __launch_bounds__(BK3AdjCfg<Eng, Q, EB, DPAR>::NT)
             const int wi = e * WB::size + WB::at(i, j, k);
             const V ur = W1[wi], us_ = W2[wi], ut = W3[wi];
             const V rr = W4[wi], rs_ = W5[wi], rt = W6[wi];
-            const S* ge = gs + e * 6 * Q3 + x;   // factor-major
+            const GS* ge = gs + e * 6 * Q3 + x;   // factor-major
             const V g0 = Eng::load(ge[0]), g1 = Eng::load(ge[Q3]), g2 = Eng::load(ge[2 * Q3]);
             const V g3 = Eng::load(ge[3 * Q3]), g4 = Eng::load(ge[4 * Q3]), g5 = Eng::load(ge[5 * Q3]);
             const V kk = Eng::load(ks[e * Q3 + x]);

@@ -263,15 +263,17 @@ int bk3_adjoint(int p, int64_t E, const double* B, const double* D, const void* 
     if (B == nullptr || D == nullptr) return BK_ERR_NULL;
     if ((rc = check_ptrs(E, {G, k, u, res, dk, dG}))) return rc;
     const int eng = engine_of(o);
-    if (eng < 0 || o.gform != BK_G_STORAGE) return BK_ERR_PREC;
+    if (eng < 0) return BK_ERR_PREC;
+    // G split ahead of time: the float-float engine (FP64, engine AUTO or FF)
+    if (o.gform != BK_G_STORAGE && (o.gform != BK_G_FF || eng != 1)) return BK_ERR_PREC;
     if (E == 0) return BK_OK;
     if ((rc = status_or_null())) return rc;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     switch (eng) {
-        case 0: return launch_bk3_adjoint_dfma(p, E, B, D, G, k, u, res, dk, dG, s);
-        case 1: return launch_bk3_adjoint_ff(p, E, B, D, G, k, u, res, dk, dG, s);
-        case 2: return launch_bk3_adjoint_f32(p, E, B, D, G, k, u, res, dk, dG, s);
-        default: return launch_bk3_adjoint_mixed(p, E, B, D, G, k, u, res, dk, dG, s);
+        case 0: return launch_bk3_adjoint_dfma(p, E, B, D, G, k, u, res, dk, dG, o.gform, s);
+        case 1: return launch_bk3_adjoint_ff(p, E, B, D, G, k, u, res, dk, dG, o.gform, s);
+        case 2: return launch_bk3_adjoint_f32(p, E, B, D, G, k, u, res, dk, dG, o.gform, s);
+        default: return launch_bk3_adjoint_mixed(p, E, B, D, G, k, u, res, dk, dG, o.gform, s);
     }
 }
 

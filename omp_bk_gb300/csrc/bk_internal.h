@@ -35,7 +35,7 @@ DevCtx dev_ctx();              // status word and wait limit of the current devi
                            const void* mass, double lambda, void* v, cudaStream_t s);                            \
     int launch_bk3_adjoint_##sfx(int p, long long E, const double* B, const double* D, const void* G,           \
                                  const void* k, const void* u, const void* res, void* dk, void* dG,              \
-                                 cudaStream_t s);                                                                \
+                                 int gform, cudaStream_t s);                                                                \
     int bk5_col_##sfx##_L2(int p, int F, int eb, const double* D, long long E, const void* u, const void* G,    \
                            const void* mass, double lambda, void* v, cudaStream_t s);
 

@@ -284,19 +284,19 @@ int bk3_q(const double* B, const double* D, long long E, const void* G, const vo
 #endif  // BK_OP_TU == 3
 
 #if BK_OP_TU == 7
-template <int Q, int EB, bool EO, int DPAR>
+template <int Q, int EB, bool EO, int DPAR, class GS = typename Eng::S>
 int bk3adj_launch(const P13<typename Eng::C, Q>& prm, long long E, const void* G, const void* k, const void* u,
                   const void* res, void* dk, void* dG, cudaStream_t s)
 {
     using Cfg = BK3AdjCfg<Eng, Q, EB, DPAR>;
     using S = typename Eng::S;
     static_assert(Cfg::SMEM <= 232448, "BK3 adjoint block exceeds the shared memory of an SM");
-    auto kern = bk3_adjoint_kernel<Eng, Q, EB, EO, DPAR>;
+    auto kern = bk3_adjoint_kernel<Eng, Q, EB, EO, DPAR, GS>;
     const int occ = prepare<EoTag<Cfg, EO>>(kern, Cfg::SMEM, Cfg::NT);
     if (occ <= 0) return BK_ERR_CUDA;
     const int grid = grid_for((E + EB - 1) / EB, occ);
     kern<<<grid, Cfg::NT, Cfg::SMEM, s>>>(prm, E, static_cast<const S*>(u), static_cast<const S*>(res),
-                                          static_cast<const S*>(G), static_cast<const S*>(k), static_cast<S*>(dk),
+                                          static_cast<const GS*>(G), static_cast<const S*>(k), static_cast<S*>(dk),
                                           static_cast<S*>(dG), dev_ctx());
     return cudaGetLastError() == cudaSuccess ? BK_OK : BK_ERR_CUDA;
 }
@@ -307,7 +307,7 @@ constexpr int adj_eb_dpar(int q) { return q <= 6 ? 2 : 1; }
 
 template <int Q>
 int bk3adj_q(const double* B, const double* D, long long E, const void* G, const void* k, const void* u,
-             const void* res, void* dk, void* dG, cudaStream_t s)
+             const void* res, void* dk, void* dG, int gform, cudaStream_t s)
 {
     constexpr int EB = default_eb(Q) / 2 > 0 ? default_eb(Q) / 2 : 1;
     P13<typename Eng::C, Q> prm;
@@ -315,8 +315,15 @@ int bk3adj_q(const double* B, const double* D, long long E, const void* G, const
     for (int i = 0; i < Q * Q; ++i) prm.D[i] = Eng::coef(D[i]);
     if (make_p13_eo<typename Eng::C, Q>(prm, B, D, &Eng::coef)) {
         constexpr int DP = adj_dpar(Q) ? 2 : 0;
+        if (gform == BK_G_FF) {
+            // G split ahead of time: the float-float engine's even-odd path
+            if constexpr (eng_is_ff())
+                return bk3adj_launch<Q, DP ? adj_eb_dpar(Q) : EB, true, DP, ff2>(prm, E, G, k, u, res, dk, dG, s);
+            return BK_ERR_PREC;
+        }
         return bk3adj_launch<Q, DP ? adj_eb_dpar(Q) : EB, true, DP>(prm, E, G, k, u, res, dk, dG, s);
     }
+    if (gform != BK_G_STORAGE) return BK_ERR_PREC;
     return bk3adj_launch<Q, EB, false, 0>(prm, E, G, k, u, res, dk, dG, s);
 }
 #endif  // BK_OP_TU == 7
@@ -443,17 +450,17 @@ int BK_CAT(launch_bk5, BK_SFX)(int p, long long E, const double* D, const void* 
 
 int BK_CAT(launch_bk3_adjoint, BK_SFX)(int p, long long E, const double* B, const double* D, const void* G,
                                         const void* k, const void* u, const void* res, void* dk, void* dG,
-                                        cudaStream_t s)
+                                        int gform, cudaStream_t s)
 {
     switch (p + 2) {
-        case 3: return bk3adj_q<3>(B, D, E, G, k, u, res, dk, dG, s);
-        case 4: return bk3adj_q<4>(B, D, E, G, k, u, res, dk, dG, s);
-        case 5: return bk3adj_q<5>(B, D, E, G, k, u, res, dk, dG, s);
-        case 6: return bk3adj_q<6>(B, D, E, G, k, u, res, dk, dG, s);
-        case 7: return bk3adj_q<7>(B, D, E, G, k, u, res, dk, dG, s);
-        case 8: return bk3adj_q<8>(B, D, E, G, k, u, res, dk, dG, s);
-        case 9: return bk3adj_q<9>(B, D, E, G, k, u, res, dk, dG, s);
-        case 10: return bk3adj_q<10>(B, D, E, G, k, u, res, dk, dG, s);
+        case 3: return bk3adj_q<3>(B, D, E, G, k, u, res, dk, dG, gform, s);
+        case 4: return bk3adj_q<4>(B, D, E, G, k, u, res, dk, dG, gform, s);
+        case 5: return bk3adj_q<5>(B, D, E, G, k, u, res, dk, dG, gform, s);
+        case 6: return bk3adj_q<6>(B, D, E, G, k, u, res, dk, dG, gform, s);
+        case 7: return bk3adj_q<7>(B, D, E, G, k, u, res, dk, dG, gform, s);
+        case 8: return bk3adj_q<8>(B, D, E, G, k, u, res, dk, dG, gform, s);
+        case 9: return bk3adj_q<9>(B, D, E, G, k, u, res, dk, dG, gform, s);
+        case 10: return bk3adj_q<10>(B, D, E, G, k, u, res, dk, dG, gform, s);
         default: return BK_ERR_ORDER;
     }
 }

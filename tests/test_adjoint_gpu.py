@@ -161,3 +161,25 @@ def test_stream_kernels(bklib):
     assert torch.allclose(a, b[:n] + 3 * c, rtol=1e-6, atol=1e-6)
     bk.stream_kernel(bk.STREAM_MIX, a, b, reads=7)
     assert torch.allclose(a, b.view(7, n).sum(0), atol=1e-5)
+
+
+@pytest.mark.parametrize("p", [1, 3, 4, 6, 8])
+def test_adjoint_split_g_is_bitwise(bklib, p):
+    """The backward kernel on G split once into float-float pairs
+    (bk_g_to_ff) gives bitwise the gradients of the double G."""
+    bk = bklib
+    E = 7
+    Q, P = p + 2, p + 1
+    B, D, G = _geom(bk, p, E, 13)
+    rng = np.random.default_rng(40 + p)
+    k = dev(np.exp(rng.normal(0, 0.5, E * Q ** 3)), "f64")
+    u = dev(rng.uniform(-1, 1, E * P ** 3), "f64")
+    res = dev(rng.uniform(-1, 1, E * P ** 3), "f64")
+    dk0, dk1 = (torch.empty(E * Q ** 3, dtype=torch.float64, device="cuda") for _ in range(2))
+    dG0, dG1 = (torch.empty(E * 6 * Q ** 3, dtype=torch.float64, device="cuda") for _ in range(2))
+    bk.bk3_adjoint(p, E, B, D, G, k, u, res, dk0, dG0)
+    bk.bk3_adjoint(p, E, B, D, bk.g_to_ff(G), k, u, res, dk1, dG1, gform=bk.G_FF)
+    torch.cuda.synchronize()
+    assert torch.equal(dk0, dk1) and torch.equal(dG0, dG1)
+    with pytest.raises(bk.BKError, match="precision"):
+        bk.bk3_adjoint(p, E, B, D, G, k, u, res, dk1, dG1, engine=bk.ENGINE_DFMA, gform=bk.G_FF)
