@@ -20,7 +20,14 @@ conflict-free count (1 for 4-byte values, 2 for full 8-byte warps): 1.0 is
 conflict-free.  For small Q a warp spans several elements, so the element
 stride ES matters as much as ZP and PS.
 
+A warp's 128-bit access is four passes of 8 lanes, each one wavefront
+when its lanes' 16-byte groups fall in distinct quarters of the 128-byte
+bank window.  Op 32 scores BK3's fused flow (op 31) at Q = 8, 4-byte values,
+on a box whose rows swap their two 16-byte halves when bit 2 of j is set
+(k ^ 4) and whose k lines are 128-bit accesses (WBox3's swizzled form).
+
     python -m omp_bk_gb300.box_model --op 5 --vbytes 4        # search, prints the table rows
+    python -m omp_bk_gb300.box_model --op 32                  # the swizzled Q = 8 box
 """
 from __future__ import annotations
 
@@ -141,6 +148,85 @@ def walks(op: int, Q: int, eb: int, zp: int, ps: int, es: int):
     yield 1, _sweep(Q, P, P, 0, P, eb, zp, ps, es, writes=False)         # back along i: reads
 
 
+def wavefronts128(addrs) -> int:
+    """Wavefronts of one warp's 128-bit access at the (16-byte aligned)
+    4-byte value indices `addrs`: four passes of 8 lanes."""
+    total = 0
+    for ph in range(4):
+        groups: dict = {}
+        for a in addrs[8 * ph:8 * ph + 8]:
+            if a is not None:
+                groups.setdefault((a // 4) % 8, set()).add(a)
+        total += max((len(s) for s in groups.values()), default=0)
+    return total
+
+
+def swizzled_at(zp: int, ps: int, es: int, x: int, sb: int):
+    """Value index of (e, i, j, k) in a box whose rows have k ^ x when bit
+    sb of j is set."""
+    def at(e, i, j, k):
+        return e * es + i * ps + j * zp + (k ^ (x if (j >> sb) & 1 else 0))
+    return at
+
+
+def _line_walk(at, X, Y, Z, d, NO, eb, reads=True, writes=True, vec=False):
+    """(wavefronts, conflict-free count, instructions) of a sweep along d
+    through the box addressed by `at`; vec: 128-bit accesses along k."""
+    NI = (X, Y, Z)[d]
+    LB = Y if d == 2 else Z
+    L = X * Y * Z // NI
+    step = 4 if vec else 1
+    idx = (list(range(0, NI, step)) if reads else []) + (list(range(0, NO, step)) if writes else [])
+    wf = ideal = ins = 0
+    for n in idx:
+        def f(w, n=n):
+            e, l = divmod(w, L)
+            a, b = divmod(l, LB)
+            return at(e, n, a, b) if d == 0 else (at(e, a, n, b) if d == 1 else at(e, a, b, n))
+        for ws in _warps(eb * L, f):
+            wf += wavefronts128(ws) if vec else wavefronts(ws, 4)
+            ideal += 4 if vec else 1
+            ins += 1
+    return wf, ideal, ins
+
+
+def score32(zp: int = 8, ps: int = 72, es: int = 576, x: int = 4, sb: int = 2, vec: bool = True, eb: int = 1):
+    """Op 31's walks at Q = 8 on the swizzled box with 128-bit k lines:
+    (score, wavefronts, conflict-free wavefronts, shared instructions) of
+    one element."""
+    Q, P = 8, 7
+    at = swizzled_at(zp, ps, es, x, sb)
+
+    def dense(X, Y, Z):
+        n = X * Y * Z
+
+        def f(w):
+            e, r = divmod(w, n)
+            i, r = divmod(r, Y * Z)
+            j, k = divmod(r, Z)
+            return at(e, i, j, k)
+        ws = _warps(eb * n, f)
+        return sum(wavefronts(a, 4) for a in ws), len(ws), len(ws)
+
+    parts = [
+        (1, _line_walk(at, P, P, P, 0, Q, eb, reads=False)),
+        (1, _line_walk(at, Q, P, P, 1, Q, eb)),
+        (1, _line_walk(at, Q, Q, P, 2, Q, eb, writes=False, vec=vec)),
+        (2, _line_walk(at, Q, Q, Q, 2, Q, eb, reads=False, vec=vec)),
+        (2, _line_walk(at, Q, Q, Q, 0, Q, eb)),
+        (2, _line_walk(at, Q, Q, Q, 1, Q, eb)),
+        (6, dense(Q, Q, Q)),
+        (3, _line_walk(at, Q, Q, Q, 2, Q, eb, writes=False, vec=vec)),
+        (1, _line_walk(at, Q, Q, P, 2, P, eb, reads=False, vec=vec)),
+        (1, _line_walk(at, Q, Q, P, 1, P, eb)),
+        (1, _line_walk(at, Q, P, P, 0, P, eb, writes=False)),
+    ]
+    wf = sum(w * p[0] for w, p in parts)
+    ideal = sum(w * p[1] for w, p in parts)
+    ins = sum(w * p[2] for w, p in parts)
+    return wf / ideal, wf, ideal, ins
+
+
 def score(op: int, Q: int, eb: int, vbytes: int, zp: int, ps: int, es: int) -> float:
     ideal = 1 if vbytes == 4 else 2
     tot = norm = 0.0
@@ -195,9 +281,15 @@ def search(op: int, Q: int, vbytes: int):
 
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
-    ap.add_argument("--op", type=int, choices=(3, 5, 31, 51), default=5)
+    ap.add_argument("--op", type=int, choices=(3, 5, 31, 32, 51), default=5)
     ap.add_argument("--vbytes", type=int, choices=(4, 8), default=4)
     args = ap.parse_args(argv)
+    if args.op == 32:
+        s, wf, ideal, ins = score32()
+        s0, wf0, ideal0, ins0 = score32(8, 71, 568, 0, 2, vec=False)
+        print(f"Q=8 swizzled {{8, 72, 576}}, 128-bit k lines: score {s:.2f}, {wf} wavefronts, "
+              f"{ins} instructions per element ({{8, 71, 568}} unswizzled: {s0:.2f}, {wf0}, {ins0})")
+        return
     for Q in sorted(EBS[(args.op, args.vbytes)]):
         zp, ps, es, s = search(args.op, Q, args.vbytes)
         lz, lp, le = legacy(Q, args.vbytes)

@@ -83,10 +83,11 @@ constexpr int bk5_box(int q, int vbytes, int what)   // what: 0 ZP, 1 PS, 2 elem
 // the same model over their walks (the dense P^3 load and store, the
 // interpolation sweeps through the (Q,P,P) and (Q,Q,P) boxes and back, the
 // gradient sweeps and the dense pointwise walk; box_model.py --op 3).  At
-// 4-byte Q = 8 the model of the flow fused along k (--op 31, the FP32
-// forms' BK3 since the fusion) picks {8, 71, 568}: BK3 p=6 mixed 110.2
-// against 109.8 GDoF/s with the first strides (before the fusion the same
-// box had measured 83.0 against 87.6).  Model wavefronts per access,
+// 4-byte Q = 8 the model of the flow fused along k (--op 31) picks
+// {8, 71, 568}: BK3 p=6 mixed 110.2 against 109.8 GDoF/s with the first
+// strides (before the fusion the same box had measured 83.0 against 87.6);
+// BK3's FP32-storage forms now use the swizzled box below at Q = 8, the
+// table's entry serves BK1 and the adjoint.  Model wavefronts per access,
 // Q = 3..10, against the first strides:
 //   4-byte values: 1.45 1.55 1.48 1.67 1.64 1.49 1.31 1.48
 //                 (2.49 2.21 1.96 1.86 1.73 1.49 1.61 1.81)
@@ -103,23 +104,121 @@ constexpr int bk3_box(int q, int vbytes, int what)   // what: 0 ZP, 1 PS, 2 elem
                              : (vbytes == 8 ? b8[q - 3][what] : b4[q - 3][what]);
 }
 
-template <int Q, class V>
+// Row swizzle of a work box: value k of row (i, j) sits at i*PS + j*ZP +
+// (k ^ swz(j)), swz(j) = X when bit SB of j is set, else 0 (X = 0: no
+// swizzle).  With rows of 8 four-byte values (ZP = 8) a warp of 32 k lines
+// (j = 0..7 at each of 4 i) otherwise meets rows j and j + 4 in the same
+// banks; swapping the two halves of every row whose j has bit 2 set makes
+// the 128-bit k-line accesses (VEC) and, with PS = 8 mod 32, the j-direction
+// sweeps conflict-free.  Only BK3's FP32-storage forms at Q = 8 use it
+// (box_model.py --op 32): the model's wavefronts per element fall from 612
+// to 474, its shared-memory instructions from 424 to 344, and BK3 p=6 mixed
+// went from 110.2 to 120.1 GDoF/s (same results).
+constexpr int bk3_swz(int q, int vbytes) { return (q == 8 && vbytes == 4) ? 4 : 0; }
+
+template <int Q, class V, bool SWZ = false>
 struct WBox3 {
-    static constexpr int ZP = bk3_box(Q, int(sizeof(V)), 0);
-    static constexpr int PS = bk3_box(Q, int(sizeof(V)), 1);
-    static constexpr int size = bk3_box(Q, int(sizeof(V)), 2);
+    static constexpr int X = SWZ ? bk3_swz(Q, int(sizeof(V))) : 0;
+    static constexpr int SB = 2;
+    static constexpr int ZP = X ? 8 : bk3_box(Q, int(sizeof(V)), 0);
+    static constexpr int PS = X ? 72 : bk3_box(Q, int(sizeof(V)), 1);
+    static constexpr int size = X ? 576 : bk3_box(Q, int(sizeof(V)), 2);
+    // k lines as 128-bit accesses (16-byte aligned rows of 4-byte values)
+    static constexpr bool VEC = X != 0;
     static_assert((Q - 1) * ZP + Q <= PS && (Q - 1) * PS + PS <= size, "box strides overlap");
-    __device__ static __forceinline__ int at(int i, int j, int k) { return i * PS + j * ZP + k; }
+    static_assert(!X || (Q <= 2 * X && ZP % 4 == 0 && PS % 4 == 0 && size % 4 == 0 && sizeof(V) == 4),
+                  "swizzled rows hold two 16-byte halves");
+    __device__ static __forceinline__ int swz(int j) { return X ? ((j >> SB) & 1) * X : 0; }
+    __device__ static __forceinline__ int at(int i, int j, int k) { return i * PS + j * ZP + (k ^ swz(j)); }
 };
 
 template <int Q, class V>
 struct WBox5 {
+    static constexpr int X = 0, SB = 0;
+    static constexpr bool VEC = false;
     static constexpr int ZP = bk5_box(Q, int(sizeof(V)), 0);
     static constexpr int PS = bk5_box(Q, int(sizeof(V)), 1);
     static constexpr int size = bk5_box(Q, int(sizeof(V)), 2);
     static_assert((Q - 1) * ZP + Q <= PS && (Q - 1) * PS + PS <= size, "box strides overlap");
+    __device__ static __forceinline__ int swz(int) { return 0; }
     __device__ static __forceinline__ int at(int i, int j, int k) { return i * PS + j * ZP + k; }
 };
+
+// Addresses along one line of direction DIR of element e's box, the line
+// given by its two other indices (a, b) in (i, j, k) order: (*this)(n) is
+// the n-th value.  With a swizzle the index n, a compile-time constant in
+// the unrolled loops, picks one of two per-line bases, so the swizzle costs
+// no instruction per access:
+//   DIR 0: (n, a, b) at b0 + n*PS (the row a is fixed);
+//   DIR 1: (a, n, b) at b0 or b1 (b ^ X) + n*ZP, by bit SB of n;
+//   DIR 2: (a, b, n) at b0 (= base + m) or b1 (= base - m) + n, by bit X of
+//          n, m = swz(b): n ^ m = n + m or n - m.
+template <class WB, int DIR>
+struct BoxLine {
+    int b0, b1;
+    __device__ __forceinline__ BoxLine(int e, int a, int b)
+    {
+        const int eb = e * WB::size;
+        if constexpr (DIR == 0) {
+            b0 = eb + a * WB::ZP + (b ^ WB::swz(a));
+            b1 = b0;
+        } else if constexpr (DIR == 1) {
+            b0 = eb + a * WB::PS + b;
+            b1 = eb + a * WB::PS + (b ^ WB::X);
+        } else {
+            const int m = WB::swz(b);
+            b0 = eb + a * WB::PS + b * WB::ZP + m;
+            b1 = eb + a * WB::PS + b * WB::ZP - m;
+        }
+    }
+    __device__ __forceinline__ int operator()(int n) const
+    {
+        if constexpr (DIR == 0) return b0 + n * WB::PS;
+        else if constexpr (DIR == 1) return ((WB::X && ((n >> WB::SB) & 1)) ? b1 : b0) + n * WB::ZP;
+        else return ((WB::X && (n & WB::X)) ? b1 : b0) + n;
+    }
+};
+
+// The N values of a k line into registers / from registers; 128-bit
+// accesses when the box allows them (WB::VEC: the line's halves are 16-byte
+// aligned; the last half of a line of N < 8 values reads, or writes, the
+// row's padding).
+template <class WB, int N, class V>
+__device__ __forceinline__ void line_load(const V* W, const BoxLine<WB, 2>& la, V (&x)[N])
+{
+    if constexpr (WB::VEC) {
+        static_assert(sizeof(V) == 4 && N <= 8, "128-bit k lines of 4-byte values");
+#pragma unroll
+        for (int c = 0; c < (N + 3) / 4; ++c) {
+            const float4 t = *reinterpret_cast<const float4*>(W + la(4 * c));
+            const V tv[4] = {t.x, t.y, t.z, t.w};
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (4 * c + q < N) x[4 * c + q] = tv[q];
+        }
+    } else {
+#pragma unroll
+        for (int n = 0; n < N; ++n) x[n] = W[la(n)];
+    }
+}
+
+template <class WB, int N, class V>
+__device__ __forceinline__ void line_store(V* W, const BoxLine<WB, 2>& la, const V (&y)[N])
+{
+    if constexpr (WB::VEC) {
+        static_assert(sizeof(V) == 4 && N <= 8, "128-bit k lines of 4-byte values");
+#pragma unroll
+        for (int c = 0; c < (N + 3) / 4; ++c) {
+            V tv[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) tv[q] = y[(4 * c + q < N) ? 4 * c + q : N - 1];
+            *reinterpret_cast<float4*>(W + la(4 * c)) = make_float4(tv[0], tv[1], tv[2], tv[3]);
+        }
+    } else {
+#pragma unroll
+        for (int n = 0; n < N; ++n) W[la(n)] = y[n];
+    }
+}
 
 // ---- staging -------------------------------------------------------------------
 
@@ -185,23 +284,21 @@ __device__ __forceinline__ void sweep(const typename Eng::V* in, typename Eng::V
     constexpr int NI = DIR == 0 ? X : (DIR == 1 ? Y : Z);
     constexpr int LB = DIR == 2 ? Y : Z;
     constexpr int L = (X * Y * Z) / NI;
-    constexpr int SD = DIR == 0 ? WB::PS : (DIR == 1 ? WB::ZP : 1);
     for (int w = tid; w < ne * L; w += nt) {
         const int e = w / L;
         const int l = w - e * L;
         const int a = l / LB;
         const int b = l - a * LB;
-        int base = (DIR == 0) ? a * WB::ZP + b : (DIR == 1 ? a * WB::PS + b : a * WB::PS + b * WB::ZP);
-        base += e * WB::size;
+        const BoxLine<WB, DIR> la(e, a, b);
         V x[NI];
 #pragma unroll
-        for (int n = 0; n < NI; ++n) x[n] = in[base + n * SD];
+        for (int n = 0; n < NI; ++n) x[n] = in[la(n)];
 #pragma unroll
         for (int o = 0; o < NO; ++o) {
             A acc = Eng::first(mat(o, 0), x[0]);
 #pragma unroll
             for (int n = 1; n < NI; ++n) Eng::madd(acc, mat(o, n), x[n]);
-            out[base + o * SD] = Eng::result(acc);
+            out[la(o)] = Eng::result(acc);
         }
     }
 }
@@ -293,6 +390,7 @@ __device__ __forceinline__ void sweep_eo(const typename Eng::V* in, typename Eng
     constexpr int LB = Q;
     constexpr int L = Q * Q;
     constexpr int SD = DIR == 0 ? WB::PS : (DIR == 1 ? WB::ZP : 1);
+    static_assert(WB::X == 0, "unswizzled boxes");
     for (int w = tid; w < ne * L; w += nt) {
         const int e = w / L;
         const int l = w - e * L;
@@ -320,6 +418,7 @@ __device__ __forceinline__ void sweep_eo_dyn(const typename Eng::V* in, typename
     using A = typename Eng::A;
     constexpr int H = Q / 2;
     constexpr int L = Q * Q;
+    static_assert(WB::X == 0, "unswizzled boxes");
     const int SD = dir == 0 ? WB::PS : (dir == 1 ? WB::ZP : 1);
     const int SA = dir == 0 ? WB::ZP : WB::PS;   // stride of the line's first index
     const int SB = dir == 2 ? WB::ZP : 1;        // stride of its second index
@@ -457,20 +556,26 @@ __device__ __forceinline__ void sweep_eor(const typename Eng::V* in, typename En
     constexpr int NI = DIR == 0 ? X : (DIR == 1 ? Y : Z);
     constexpr int LB = DIR == 2 ? Y : Z;
     constexpr int L = (X * Y * Z) / NI;
-    constexpr int SD = DIR == 0 ? WB::PS : (DIR == 1 ? WB::ZP : 1);
     for (int w = tid; w < ne * L; w += nt) {
         const int e = w / L;
         const int l = w - e * L;
         const int a = l / LB;
         const int b = l - a * LB;
-        int base = (DIR == 0) ? a * WB::ZP + b : (DIR == 1 ? a * WB::PS + b : a * WB::PS + b * WB::ZP);
-        base += e * WB::size;
+        const BoxLine<WB, DIR> la(e, a, b);
         V x[NI], y[NO];
+        if constexpr (DIR == 2) {
+            line_load<WB, NI>(in, la, x);
+        } else {
 #pragma unroll
-        for (int n = 0; n < NI; ++n) x[n] = in[base + n * SD];
+            for (int n = 0; n < NI; ++n) x[n] = in[la(n)];
+        }
         eor_line<Eng, NI, NO, SIGN>(x, y, m);
+        if constexpr (DIR == 2) {
+            line_store<WB, NO>(out, la, y);
+        } else {
 #pragma unroll
-        for (int o = 0; o < NO; ++o) out[base + o * SD] = y[o];
+            for (int o = 0; o < NO; ++o) out[la(o)] = y[o];
+        }
     }
 }
 
@@ -496,9 +601,9 @@ __device__ __forceinline__ void interp0_from_dense(const typename Eng::S* us, ty
 #pragma unroll
         for (int n = 0; n < P; ++n) x[n] = Eng::load(src[n * P * P]);
         eor_line<Eng, P, Q, +1>(x, y, m);
-        const int base = e * WB::size + j * WB::ZP + kk;
+        const BoxLine<WB, 0> la(e, j, kk);
 #pragma unroll
-        for (int o = 0; o < Q; ++o) out[base + o * WB::PS] = y[o];
+        for (int o = 0; o < Q; ++o) out[la(o)] = y[o];
     }
 }
 
@@ -517,10 +622,10 @@ __device__ __forceinline__ void interp0_to_dense(const typename Eng::V* in, type
         const int l = w - e * L;
         const int j = l / P;
         const int kk = l - j * P;
-        const int base = e * WB::size + j * WB::ZP + kk;
+        const BoxLine<WB, 0> la(e, j, kk);
         V x[Q], y[P];
 #pragma unroll
-        for (int n = 0; n < Q; ++n) x[n] = in[base + n * WB::PS];
+        for (int n = 0; n < Q; ++n) x[n] = in[la(n)];
         eor_line<Eng, Q, P, +1>(x, y, m);
         typename Eng::S* dst = v + e * (P * P * P) + j * P + kk;
 #pragma unroll
@@ -530,7 +635,8 @@ __device__ __forceinline__ void interp0_to_dense(const typename Eng::V* in, type
 
 // One pass over the lines along k (thread per (i, j) line of every element)
 // of a padded box holding (Q, Q, P): the line's P values are read once and
-// `f(e, i, j, x, base)` computes and writes from registers.  The fused
+// `f(e, i, j, x, la)` computes and writes from registers (la: the line's
+// addresses, for the other boxes' values on the same line).  The fused
 // k-direction steps of BK1 and BK3 use it.
 template <class Eng, class WB, int Q, int P, class F>
 __device__ __forceinline__ void kline_pass(const typename Eng::V* in, int ne, int tid, int nt, F f)
@@ -542,11 +648,10 @@ __device__ __forceinline__ void kline_pass(const typename Eng::V* in, int ne, in
         const int l = w - e * L;
         const int i = l / Q;
         const int j = l - i * Q;
-        const int base = e * WB::size + WB::at(i, j, 0);
+        const BoxLine<WB, 2> la(e, i, j);
         V x[P];
-#pragma unroll
-        for (int n = 0; n < P; ++n) x[n] = in[base + n];
-        f(e, i, j, x, base);
+        line_load<WB, P>(in, la, x);
+        f(e, i, j, x, la);
     }
 }
 
@@ -816,10 +921,10 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
             const int l = w - e * L;
             const int i = l / Q;
             const int j = l - i * Q;
-            const int base = e * WB::size + WB::at(i, j, 0);
+            const BoxLine<WB, 2> la(e, i, j);
             V x[Q];
 #pragma unroll
-            for (int n = 0; n < Q; ++n) x[n] = W2[base + n];
+            for (int n = 0; n < Q; ++n) x[n] = W2[la(n)];
 #pragma unroll
             for (int o = 0; o < Q; ++o) {
                 A acc = Eng::first(Dt(o, 0), x[0]);
@@ -827,13 +932,13 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
                 for (int n = 1; n < Q; ++n) Eng::madd(acc, Dt(o, n), x[n]);
                 V res;
                 if constexpr (HasSum3<Eng>::value) {
-                    res = Eng::sum3(Eng::result(acc), W0[base + o], W1[base + o]);
+                    res = Eng::sum3(Eng::result(acc), W0[la(o)], W1[la(o)]);
                 } else {
-                    Eng::add(acc, W0[base + o]);
-                    Eng::add(acc, W1[base + o]);
+                    Eng::add(acc, W0[la(o)]);
+                    Eng::add(acc, W1[la(o)]);
                     res = Eng::loose(acc);
                 }
-                W2[base + o] = res;
+                W2[la(o)] = res;
             }
         }
         __syncthreads();
@@ -875,7 +980,7 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
     //    third flux in registers (no write and re-read of the box), the sum,
     //    the mass term, each thread storing its line's Q values
     auto kline_last = [&](auto with_mass) {
-        kline_pass<Eng, WB, Q, Q>(QT, ne, tid, nt, [&](int e, int i, int j, const V (&x)[Q], int base) {
+        kline_pass<Eng, WB, Q, Q>(QT, ne, tid, nt, [&](int e, int i, int j, const V (&x)[Q], const BoxLine<WB, 2>& la) {
             V t[Q];
             eo_line<Eng, Q>(x, t, eot);
             const int w0 = e * Q3 + (i * Q + j) * Q;
@@ -883,11 +988,11 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
             for (int o = 0; o < Q; ++o) {
                 V res;
                 if constexpr (HasSum3<Eng>::value) {
-                    res = Eng::sum3(t[o], W0[base + o], W1[base + o]);
+                    res = Eng::sum3(t[o], W0[la(o)], W1[la(o)]);
                 } else {
                     A acc = Eng::from(t[o]);
-                    Eng::add(acc, W0[base + o]);
-                    Eng::add(acc, W1[base + o]);
+                    Eng::add(acc, W0[la(o)]);
+                    Eng::add(acc, W1[la(o)]);
                     res = Eng::loose(acc);   // store() renormalises
                 }
                 S out = Eng::store(res);
@@ -1078,7 +1183,7 @@ __global__ void __launch_bounds__(BK1Cfg<Eng, Q, EB>::NT)
             __syncthreads();
             // along k in registers: interpolate to the points, times JxW,
             // back to the nodes, (Q,Q,P) in place
-            kline_pass<Eng, WB, Q, P>(W0, ne, tid, nt, [&](int e, int i, int j, const V (&x)[P], int base) {
+            kline_pass<Eng, WB, Q, P>(W0, ne, tid, nt, [&](int e, int i, int j, const V (&x)[P], const BoxLine<WB, 2>& la) {
                 V y[Q], z[P];
                 eor_line<Eng, P, Q, +1>(x, y, prm.bi);
                 const S* jl = js + e * Q3 + (i * Q + j) * Q;
@@ -1086,7 +1191,7 @@ __global__ void __launch_bounds__(BK1Cfg<Eng, Q, EB>::NT)
                 for (int o = 0; o < Q; ++o) y[o] = Eng::mul(y[o], Eng::load(jl[o]));
                 eor_line<Eng, Q, P, +1>(y, z, prm.bb);
 #pragma unroll
-                for (int o = 0; o < P; ++o) W0[base + o] = z[o];
+                for (int o = 0; o < P; ++o) W0[la(o)] = z[o];
             });
             __syncthreads();
             if (bt + gridDim.x < nbatch) issue(bt + gridDim.x);   // the stage is free
@@ -1140,7 +1245,7 @@ template <class Eng, int Q, int EB, int DPAR = 0>
 struct BK3Cfg {
     using S = typename Eng::S;
     using V = typename Eng::V;
-    using WB = WBox3<Q, V>;
+    using WB = WBox3<Q, V, true>;   // swizzled rows at 4-byte Q = 8 (bk3_swz)
     static constexpr int P = Q - 1;
     static constexpr int Q3 = Q * Q * Q;
     static constexpr int P3 = P * P * P;
@@ -1246,15 +1351,32 @@ __global__ void __launch_bounds__(BK3Cfg<Eng, Q, EB, DPAR>::NT)
         };
         // the transposed k-direction derivative of the third flux plus the
         // other two terms, at one (i, j) line: s = D^T x + W0 + W1
-        auto sum_line = [&](const V (&t)[Q], V (&sv)[Q], int base) {
+        auto sum_line = [&](const V (&t)[Q], V (&sv)[Q], const BoxLine<WB, 2>& la) {
+            if constexpr (WB::VEC) {
+                V w0[Q], w1[Q];
+                line_load<WB, Q>(W0, la, w0);
+                line_load<WB, Q>(W1, la, w1);
+#pragma unroll
+                for (int o = 0; o < Q; ++o) {
+                    if constexpr (HasSum3<Eng>::value) {
+                        sv[o] = Eng::sum3(t[o], w0[o], w1[o]);
+                    } else {
+                        A acc = Eng::from(t[o]);
+                        Eng::add(acc, w0[o]);
+                        Eng::add(acc, w1[o]);
+                        sv[o] = Eng::result(acc);
+                    }
+                }
+                return;
+            }
 #pragma unroll
             for (int o = 0; o < Q; ++o) {
                 if constexpr (HasSum3<Eng>::value) {
-                    sv[o] = Eng::sum3(t[o], W0[base + o], W1[base + o]);
+                    sv[o] = Eng::sum3(t[o], W0[la(o)], W1[la(o)]);
                 } else {
                     A acc = Eng::from(t[o]);
-                    Eng::add(acc, W0[base + o]);
-                    Eng::add(acc, W1[base + o]);
+                    Eng::add(acc, W0[la(o)]);
+                    Eng::add(acc, W1[la(o)]);
                     sv[o] = Eng::result(acc);
                 }
             }
@@ -1283,15 +1405,12 @@ __global__ void __launch_bounds__(BK3Cfg<Eng, Q, EB, DPAR>::NT)
             } else {
                 // along k in registers: u at the points (W2) and its
                 // k-derivative qt (W3)
-                kline_pass<Eng, WB, Q, P>(W0, ne, tid, nt, [&](int, int, int, const V (&x)[P], int base) {
+                kline_pass<Eng, WB, Q, P>(W0, ne, tid, nt, [&](int, int, int, const V (&x)[P], const BoxLine<WB, 2>& la) {
                     V y[Q], t[Q];
                     eor_line<Eng, P, Q, +1>(x, y, prm.bi);
                     eor_line<Eng, Q, Q, -1>(y, t, prm.dg);
-#pragma unroll
-                    for (int o = 0; o < Q; ++o) {
-                        W2[base + o] = y[o];
-                        W3[base + o] = t[o];
-                    }
+                    line_store<WB, Q>(W2, la, y);
+                    line_store<WB, Q>(W3, la, t);
                 });
                 __syncthreads();
                 sweep_eor<Eng, WB, 0, Q, Q, Q, Q, -1>(W2, W0, ne, prm.dg, tid, nt);   // qr
@@ -1312,11 +1431,10 @@ __global__ void __launch_bounds__(BK3Cfg<Eng, Q, EB, DPAR>::NT)
                 }
                 __syncthreads();
                 // the three terms summed into W2, then back along k
-                kline_pass<Eng, WB, Q, Q>(W3, ne, tid, nt, [&](int, int, int, const V (&x)[Q], int base) {
+                kline_pass<Eng, WB, Q, Q>(W3, ne, tid, nt, [&](int, int, int, const V (&x)[Q], const BoxLine<WB, 2>& la) {
                     V sv[Q];
-                    sum_line(x, sv, base);
-#pragma unroll
-                    for (int o = 0; o < Q; ++o) W2[base + o] = sv[o];
+                    sum_line(x, sv, la);
+                    line_store<WB, Q>(W2, la, sv);
                 });
                 __syncthreads();
                 sweep_eor<Eng, WB, 2, Q, Q, Q, P, +1>(W2, W0, ne, prm.bb, tid, nt);   // (Q,Q,P)
@@ -1327,13 +1445,12 @@ __global__ void __launch_bounds__(BK3Cfg<Eng, Q, EB, DPAR>::NT)
                 // along k in registers: the transposed derivative of the
                 // third flux, plus the other two terms, back to the nodes;
                 // (Q,Q,P) into W0 (each line reads its own W0 values first)
-                kline_pass<Eng, WB, Q, Q>(W3, ne, tid, nt, [&](int, int, int, const V (&x)[Q], int base) {
+                kline_pass<Eng, WB, Q, Q>(W3, ne, tid, nt, [&](int, int, int, const V (&x)[Q], const BoxLine<WB, 2>& la) {
                     V t[Q], sv[Q], z[P];
                     eor_line<Eng, Q, Q, -1>(x, t, prm.dtr);
-                    sum_line(t, sv, base);
+                    sum_line(t, sv, la);
                     eor_line<Eng, Q, P, +1>(sv, z, prm.bb);
-#pragma unroll
-                    for (int o = 0; o < P; ++o) W0[base + o] = z[o];
+                    line_store<WB, P>(W0, la, z);
                 });
             }
             __syncthreads();
@@ -1370,7 +1487,7 @@ __global__ void __launch_bounds__(BK3Cfg<Eng, Q, EB, DPAR>::NT)
             sweep<Eng, WB, 1, Q, Q, Q, Q>(W1, W1, ne, Dtr, tid, nt);
             __syncthreads();
             // along r on W3 plus the two other terms -> W2
-            kline_pass<Eng, WB, Q, Q>(W3, ne, tid, nt, [&](int, int, int, const V (&x)[Q], int base) {
+            kline_pass<Eng, WB, Q, Q>(W3, ne, tid, nt, [&](int, int, int, const V (&x)[Q], const BoxLine<WB, 2>& la) {
                 V t[Q], sv[Q];
 #pragma unroll
                 for (int o = 0; o < Q; ++o) {
@@ -1379,9 +1496,8 @@ __global__ void __launch_bounds__(BK3Cfg<Eng, Q, EB, DPAR>::NT)
                     for (int n = 1; n < Q; ++n) Eng::madd(acc, Dtr(o, n), x[n]);
                     t[o] = Eng::result(acc);
                 }
-                sum_line(t, sv, base);
-#pragma unroll
-                for (int o = 0; o < Q; ++o) W2[base + o] = sv[o];
+                sum_line(t, sv, la);
+                line_store<WB, Q>(W2, la, sv);
             });
             __syncthreads();
             sweep<Eng, WB, 2, Q, Q, Q, P>(W2, W0, ne, Bb, tid, nt);   // (Q,Q,P)

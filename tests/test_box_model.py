@@ -40,3 +40,18 @@ def test_wavefront_counts():
     assert box_model.wavefronts([5] * 32, 4) == 1
     # 8-byte values: two half-warp passes when conflict-free
     assert box_model.wavefronts(list(range(32)), 8) == 2
+
+
+def test_swizzled_q8_box():
+    # op 32's scalar, unswizzled form is op 31 itself; the swizzled box with
+    # 128-bit k lines (WBox3<8, float, true>) has fewer wavefronts and fewer
+    # shared-memory instructions
+    s0, wf0, ideal0, ins0 = box_model.score32(8, 71, 568, 0, 2, vec=False)
+    assert abs(s0 - box_model.score(31, 8, 1, 4, 8, 71, 568)) < 1e-12
+    s, wf, ideal, ins = box_model.score32()
+    assert (wf, ins) == (474, 344) and (wf0, ins0) == (612, 424)
+    # the swizzle permutes each row: every (i, j, k) of an element has its
+    # own slot inside the element's 576 values
+    at = box_model.swizzled_at(8, 72, 576, 4, 2)
+    slots = {at(0, i, j, k) for i in range(8) for j in range(8) for k in range(8)}
+    assert len(slots) == 512 and min(slots) >= 0 and max(slots) < 576
