@@ -373,6 +373,13 @@ int BK_CAT3(bk5_col, BK_SFX, BK_LAYOUT_TU)(int p, int F, int eb, const double* D
 #endif
 
 #if BK_OP_TU == 1
+// Elements per BK1 block: the default (about 128 lines) except the
+// FP32-storage forms at q = 5 (BK1 p=3), whose EB = 5 (125 lines in 128
+// threads) measured fastest of EB = 1..10 on GB300: FP32 88.8 against 85.0
+// GDoF/s at E = 4096, 181.0 against 171.8 at E = 131072; the float-float
+// engine keeps EB = 6 (35.8 against 35.1, 52.1 against 50.4).
+constexpr int bk1_eb(int q) { return (q == 5 && !eng_is_ff() && !eng_is_dfma()) ? 5 : default_eb(q); }
+
 int BK_CAT(launch_bk1, BK_SFX)(int p, long long E, const double* B, const void* jxw, const void* u, void* v,
                                 int eb, cudaStream_t s)
 {
@@ -380,7 +387,7 @@ int BK_CAT(launch_bk1, BK_SFX)(int p, long long E, const double* B, const void* 
     switch (p + 2) {
         case 3: return bk1_q<3, default_eb(3)>(B, E, jxw, u, v, s);
         case 4: return bk1_q<4, default_eb(4)>(B, E, jxw, u, v, s);
-        case 5: return bk1_q<5, default_eb(5)>(B, E, jxw, u, v, s);
+        case 5: return bk1_q<5, bk1_eb(5)>(B, E, jxw, u, v, s);
         case 6: return bk1_q<6, default_eb(6)>(B, E, jxw, u, v, s);
         case 7: return bk1_q<7, default_eb(7)>(B, E, jxw, u, v, s);
         case 8: return bk1_q<8, default_eb(8)>(B, E, jxw, u, v, s);
