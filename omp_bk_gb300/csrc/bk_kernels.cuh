@@ -24,7 +24,9 @@
 //   5. the result is written to HBM with coalesced stores (from the box, or
 //      from the last interpolation's registers).
 // Work boxes are padded (row stride ZP, plane stride PS, element stride) per
-// Q from a model of the warps' shared-memory wavefronts (bk5_box, bk3_box).
+// Q from a model of the warps' shared-memory wavefronts (bk5_box, bk3_box);
+// BK3's FP32-storage box at Q = 8 also swizzles its rows and moves k lines
+// as 128-bit accesses (WBox3, BoxLine, line_load / line_store).
 #pragma once
 
 #include <cstdint>

@@ -55,3 +55,12 @@ def test_swizzled_q8_box():
     at = box_model.swizzled_at(8, 72, 576, 4, 2)
     slots = {at(0, i, j, k) for i in range(8) for j in range(8) for k in range(8)}
     assert len(slots) == 512 and min(slots) >= 0 and max(slots) < 576
+
+
+def test_swizzled_box_constants_match_the_model():
+    # the kernel header's swizzled BK3 box is the one op 32 scores
+    text = open(SRC).read()
+    assert re.search(r"constexpr int bk3_swz\(int q, int vbytes\) \{ return \(q == 8 && vbytes == 4\) \? 4 : 0; \}", text)
+    assert "static constexpr int SB = 2;" in text
+    for name, val in (("ZP", 8), ("PS", 72), ("size", 576)):
+        assert re.search(r"static constexpr int " + name + r" = X \? " + str(val) + r" :", text), name
