@@ -64,3 +64,36 @@ def test_swizzled_box_constants_match_the_model():
     assert "static constexpr int SB = 2;" in text
     for name, val in (("ZP", 8), ("PS", 72), ("size", 576)):
         assert re.search(r"static constexpr int " + name + r" = X \? " + str(val) + r" :", text), name
+
+
+def test_two_base_line_addressing():
+    # BoxLine's per-line bases (two per line, picked by the compile-time
+    # index) give the swizzled address of every value of every line, and a
+    # k line's two 16-byte halves start at la(0) and la(4)
+    zp, ps, es, x, sb = 8, 72, 576, 4, 2
+    at = box_model.swizzled_at(zp, ps, es, x, sb)
+    swz = lambda j: x if (j >> sb) & 1 else 0
+
+    def line(d, e, a, b):
+        eb = e * es
+        if d == 0:
+            b0 = eb + a * zp + (b ^ swz(a))
+            return lambda n: b0 + n * ps
+        if d == 1:
+            b0, b1 = eb + a * ps + b, eb + a * ps + (b ^ x)
+            return lambda n: (b1 if (n >> sb) & 1 else b0) + n * zp
+        m = swz(b)
+        b0, b1 = eb + a * ps + b * zp + m, eb + a * ps + b * zp - m
+        return lambda n: (b1 if n & x else b0) + n
+
+    for e in range(2):
+        for i in range(8):
+            for j in range(8):
+                for k in range(8):
+                    want = at(e, i, j, k)
+                    assert line(0, e, j, k)(i) == want
+                    assert line(1, e, i, k)(j) == want
+                    assert line(2, e, i, j)(k) == want
+                la = line(2, e, i, j)
+                for c in (0, 4):
+                    assert la(c) % 4 == 0 and [la(c) + q for q in range(4)] == [at(e, i, j, c + q) for q in range(4)]
