@@ -21,9 +21,21 @@ form uses the float-float engine (FP64 storage, FP64-accurate arithmetic on
 the FP32 pipes: the GB300's FP64 pipe runs at 1/64 rate); the native-DFMA
 engine and the FP32-storage mixed form are timed beside it ("forms").
 
+The headline's own result is checked against the FP64 oracle (the first and
+the last 1024 elements of u and G copied to the host, oracle.bk5): `parity`.
+The default run also measures the other four configurations and puts them
+under `configs` (BK1 p=3, BK3 p=6 FP64 and mixed with both inputs, the BK3
+adjoint p=4, the mixed-order Helmholtz launch and CG), each with its error
+against the oracle and its own CPU baseline; `--workload X` prints one of
+them alone.
+
 `--impl reference` times the reference's algorithm on the host cores: the
 oracle's C restatement of bk::SumFactorization<double, 8> (openmp/BK5.cpp:
-19-103) with OpenMP over all cores, on a bounded sample of the same workload.
+19-103), pinned to the reference's own kernels, with OpenMP over all cores,
+on the whole workload (E = 262144) built on the host by the oracle's
+restatement of the same seeded generators, G in BK5.cpp's interleaved layout.
+It imports nothing of the GPU package.  Both arms report the mean time per
+step over K steps after W warm-up steps.
 Multi-GPU (torchrun): replicas only (the apply has no exchange step); every
 rank applies the operator to its own elements, value = all DoFs / max time.
 """
@@ -69,6 +81,7 @@ def parse():
     ap.add_argument("--no-forms", action="store_true", help="skip the side-by-side forms")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-configs", action="store_true", help="skip the other four configurations")
     ap.add_argument("--workload", default="bk5", choices=["bk5", "bk1", "bk3", "adjoint", "helmholtz"],
                     help="bk5: the headline; the others: the remaining configurations, one JSON line each")
     return ap.parse_args()
@@ -201,34 +214,52 @@ def time_loop(fn, steps, warmup, world, stream, torch):
     return t0.elapsed_time(t1) / 1e3 / steps   # seconds per step
 
 
-def cpu_baseline_run(sample_E, steps, warmup=1, best=True):
-    """The oracle's restatement of the reference's BK5 kernel in double, OpenMP
-    over the host cores, on `sample_E` elements of the workload: `warmup`
-    untimed applies, then `steps` timed ones; the rate from the best
-    (bk::time_min, include/bk_common.h:182-192) or the mean time."""
-    import numpy as np
+def headline_config(E):
+    """The workload both arms report (the same dict in both lines)."""
+    return {"workload": f"BK5 collocated Laplacian p={P_ORDER} (P=Q=8 GLL) FP64 apply, E={E} "
+                        f"({E * (P_ORDER + 1) ** 3} DoFs), jittered trilinear mesh (h=1/{NX}, jitter {JITTER}h), "
+                        f"u ~ U[-1,1]", "p": P_ORDER, "elements": E}
 
+
+def host_inputs(E):
+    """The headline's inputs built on the host by the oracle (no GPU code):
+    D (8 x 8 GLL derivative), u ~ U[-1,1] (seed SEED_U), G (seed SEED_G) in
+    BK5.cpp's interleaved layout G(e, i, j, f, k)."""
     import oracle
     Q = P_ORDER + 1
-    rng = np.random.default_rng(0)
-    D = np.asarray(__import__("omp_bk_gb300").bk5_matrices(P_ORDER)[0])
-    u = rng.uniform(-1, 1, sample_E * Q ** 3)
-    G = rng.uniform(0.5, 1.5, sample_E * 6 * Q ** 3)
+    D, x, w = oracle.bk5_matrices(P_ORDER)
+    u = oracle.uniform(E * Q ** 3, SEED_U, -1.0, 1.0, fast=True)
+    G, _, _ = oracle.geom_trilinear(Q, 0, E, NX, NX, x, w, SEED_G, H, JITTER, layout=1, fast=True)
+    return D, u, G
+
+
+def cpu_bk5_run(E, steps, warmup):
+    """The oracle's restatement of the reference's BK5 kernel
+    (bk::SumFactorization<double, 8>, openmp/BK5.cpp:19-103) in double, OpenMP
+    over all host cores, on the whole workload: `warmup` untimed applies, then
+    `steps` timed ones; the rate from the mean time per apply (the GPU arm's
+    statistic)."""
+    import oracle
+    Q = P_ORDER + 1
+    t = time.perf_counter()
+    D, u, G = host_inputs(E)
+    gen_s = time.perf_counter() - t
     oracle.lib(fast=True)
+    out = None
     for _ in range(warmup):
-        oracle.bk5(Q, sample_E, D, G, u, fast=True)
-    times = []
+        out = oracle.bk5(Q, E, D, G, u, fast=True)
+    t = time.perf_counter()
     for _ in range(steps):
-        t = time.perf_counter()
-        oracle.bk5(Q, sample_E, D, G, u, fast=True)
-        times.append(time.perf_counter() - t)
-    sec = min(times) if best else sum(times) / len(times)
+        out = oracle.bk5(Q, E, D, G, u, fast=True)
+    sec = (time.perf_counter() - t) / steps
     cores = os.cpu_count()
-    how = f"min of {steps} applies" if best else f"mean of {steps} applies after {warmup} warm-up"
-    return {"value": sample_E * Q ** 3 / sec / 1e9, "unit": UNIT, "cores": cores, "kind": "port",
-            "ms_per_step": sec * 1e3,
-            "sample": f"BK5 p=7 FP64, {sample_E} of the {E_FULL} elements (random u, G), {how}, "
-                      f"OMP over {cores} host threads (oracle/bk_oracle.c, -O3)"}
+    return {"value": E * Q ** 3 / sec / 1e9, "unit": UNIT, "cores": cores, "kind": "port",
+            "ms_per_step": sec * 1e3, "input_build_s": gen_s,
+            "output_norm": float(__import__("numpy").linalg.norm(out)),
+            "sample": f"the whole workload (E={E}), mean of {steps} applies after {warmup} warm-up, OpenMP over "
+                      f"{cores} host threads: oracle/bk_oracle.c (-O3), the restatement of bk::SumFactorization"
+                      f"<double, 8> pinned to the reference's own kernels; inputs from oracle/bk_geom_oracle.c "
+                      f"(the same seeded generators as the GPU's)"}
 
 
 def traffic_from_profiles():
@@ -253,19 +284,18 @@ def measured_peak():
 def run_reference(args):
     """The reference arm: the reference's BK5 p=7 FP64 kernel restated in C
     (the oracle port; the reference's own build is CMake-only and does not
-    travel to the Arm machine) on the host cores, each step one apply of a
-    32768-element sample of the workload, `--warmup` untimed steps first."""
+    travel to the Arm machine) on the host cores, each step one apply of the
+    whole workload, `--warmup` untimed steps first.  Rank 0 alone runs it."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
     steps, warmup = max(1, args.steps), max(0, args.warmup)
-    cb = cpu_baseline_run(32768, steps, warmup, best=False)
+    E = args.elements or E_FULL
+    cb = cpu_bk5_run(E, steps, warmup)
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
             "steps": steps, "warmup": warmup, "ms_per_step": cb["ms_per_step"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "BK5 p=7 FP64 apply, E=262144 (134M DoFs), CPU sample of 32768 elements",
-                       "p": P_ORDER, "elements": E_FULL},
-            "cpu_baseline": cb,
+            "config": headline_config(E), "cpu_baseline": cb,
             "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -316,12 +346,35 @@ def _line(args, workload, value, ms, dtype, extra):
     print(json.dumps(out), flush=True)
 
 
+def _hostrel(a, ref):
+    """max |a - ref| / max |ref| of two host arrays (the harness's rel-max,
+    include/bk_harness.h:74-83)."""
+    import numpy as np
+    a, ref = np.asarray(a, dtype=np.float64).ravel(), np.asarray(ref, dtype=np.float64).ravel()
+    return float(np.abs(a - ref).max() / np.abs(ref).max())
+
+
+def _cpu_time(fn, steps=3):
+    """Mean seconds of `steps` calls of a host function after one warm-up."""
+    fn()
+    t = time.perf_counter()
+    for _ in range(steps):
+        fn()
+    return (time.perf_counter() - t) / steps
+
+
+def _cpu_line(units, sec, what):
+    return {"value": units / sec / 1e9, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+            "ms_per_step": sec * 1e3, "sample": what}
+
+
 def run_bk1(args):
     """BK1 mass apply p = 3 (P = 4 GLL nodes, Q = 5 Gauss points), E = 4096,
     affine elements (h = 1/16, U[-0.2, 0.2] perturbation), u ~ U[-1, 1]."""
     import torch
 
     import omp_bk_gb300 as bk
+    import oracle
     p, E = 3, args.elements or 4096
     P, Q = p + 1, p + 2
     B, _, xq, wq, _ = bk.bk1_bk3_matrices(p)
@@ -331,7 +384,7 @@ def run_bk1(args):
     v = torch.empty_like(u)
     dofs = E * P ** 3
     steps, warm = max(args.steps, 20), max(args.warmup, 3)
-    # one apply is ~15 us: the applies are timed as one CUDA graph of `steps`
+    # one apply is ~10 us: the applies are timed as one CUDA graph of `steps`
     # launches (device time; a host-timed loop measured the ctypes call)
     ms = _events_ms(lambda: bk.bk1_apply(p, E, B, qd, u, v), steps, warm, torch, graph=True)
     forms = {}
@@ -343,18 +396,19 @@ def run_bk1(args):
     v32 = torch.empty_like(u32)
     for name, pr in (("fp32", bk.PREC_FP32), ("mixed", bk.PREC_MIXED)):
         m32 = _events_ms(lambda: bk.bk1_apply(p, E, B, q32, u32, v32, prec=pr), steps, warm, torch, graph=True)
-        forms[name] = {"gdofs": dofs / m32 / 1e6, "rel_max_err": _rel(v32, ref)[0]}
-    import oracle
-    t = time.perf_counter()
-    host = oracle.bk1(Q, E, B, qd.cpu().numpy(), u.cpu().numpy(), fast=True)
-    cpu_s = time.perf_counter() - t
-    err = float(abs(torch.from_numpy(host) - ref.cpu()).max() / ref.abs().max())
-    _line(args, f"BK1 mass apply p={p} (P=4 GLL, Q=5 Gauss), E={E}, FP64 float-float, L2-resident (8.3 MB), "
-                f"timed as one CUDA graph of {steps} applies",
-          dofs / ms / 1e6, ms, "f64",
-          {"forms": forms, "rel_max_err_vs_oracle": err,
-           "cpu_baseline": {"value": dofs / cpu_s / 1e9, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-                            "sample": f"full workload, one apply (oracle/bk_oracle.c, OpenMP)"}})
+        forms[name] = {"gdofs": dofs / m32 / 1e6, "rel_max_err": _rel(v32, ref)[0],
+                       "hbm_frac_if_from_hbm": 4 * (2 * dofs + E * Q ** 3) / m32 / 1e6 / measured_peak()[0]}
+    qh, uh = qd.cpu().numpy(), u.cpu().numpy()
+    err = _hostrel(ref.cpu().numpy(), oracle.bk1(Q, E, B, qh, uh))
+    sec = _cpu_time(lambda: oracle.bk1(Q, E, B, qh, uh, fast=True))
+    return {"workload": f"BK1 mass apply p={p} (P=4 GLL, Q=5 Gauss), E={E}, affine mesh, FP64 float-float, "
+                        f"L2-resident (8.3 MB), timed as one CUDA graph of {steps} applies",
+            "gdofs": dofs / ms / 1e6, "ms_per_apply": ms, "dtype": "f64",
+            "bytes_per_apply": 8 * (2 * dofs + E * Q ** 3),
+            "l2_frac_note": "8.3 MB per apply stays in the 129 MB L2: no HBM roofline applies",
+            "rel_max_err_vs_oracle": err, "oracle_elements": E, "forms": forms,
+            "cpu_baseline": _cpu_line(dofs, sec, f"the whole workload, mean of 3 applies, oracle/bk_oracle.c "
+                                                 f"(-O3, OpenMP)")}
 
 
 def run_bk3(args):
@@ -364,6 +418,7 @@ def run_bk3(args):
     import torch
 
     import omp_bk_gb300 as bk
+    import oracle
     p, E = 6, args.elements or 131072
     P, Q = p + 1, p + 2
     B, D, xq, wq, xn = bk.bk1_bk3_matrices(p)
@@ -374,10 +429,15 @@ def run_bk3(args):
     bk.coords_affine(P, E, 64, 64, xn, 31, 1.0 / 64, 0.2, X)
     X = X.view(-1, 3)
     u_smooth = (torch.sin(math.pi * X[:, 0]) * torch.sin(math.pi * X[:, 1]) * torch.sin(math.pi * X[:, 2])).contiguous()
+    del X
     dofs = E * P ** 3
     steps, warm = max(args.steps // 4, 10), max(args.warmup, 3)
     v = torch.empty_like(u_rand)
     ms = _events_ms(lambda: bk.bk3_apply(p, E, B, D, G, u_rand, v), steps, warm, torch)
+    # the FP64 result against the oracle on its first elements
+    ns = min(E, 512)
+    Gh, uh = G[: ns * 6 * Q ** 3].cpu().numpy(), u_rand[: ns * P ** 3].cpu().numpy()
+    err64 = _hostrel(v[: ns * P ** 3].cpu().numpy(), oracle.bk3(Q, ns, B, D, Gh, uh))
     G32 = G.float()
     v32 = torch.empty(E * P ** 3, dtype=torch.float32, device="cuda")
     errs = {}
@@ -395,8 +455,13 @@ def run_bk3(args):
         bk.bk3_apply(p, E, B, D, G32d, u32.double(), vr)
         mx_in, rms_in = _rel(vr, v)
         mx_ar, rms_ar = _rel(v32, vr)
-        errs[name] = {"rel_max": mx, "rel_rms": rms, "input_rounding_rel_max": mx_in,
-                      "input_rounding_rel_rms": rms_in, "arithmetic_rel_max": mx_ar, "arithmetic_rel_rms": rms_ar}
+        errs[name] = {"rel_max": mx, "rel_rms": rms, "meets_1e-6": mx <= 1e-6,
+                      "input_rounding_rel_max": mx_in, "input_rounding_rel_rms": rms_in,
+                      "arithmetic_rel_max": mx_ar, "arithmetic_rel_rms": rms_ar}
+    del G32d, vr
+    errs["note"] = ("smooth u: storing u and G in FP32 alone gives input_rounding_rel_max (the operator's image of "
+                    "a smooth field cancels), so no FP32-storage form can meet 1e-6 there; the FP64 forms and the "
+                    "CG with FP64 refinement (Helmholtz, 1e-10) do")
     mm = _events_ms(lambda: bk.bk3_apply(p, E, B, D, G32, u32, v32, prec=bk.PREC_MIXED), steps, warm, torch)
     vd = torch.empty_like(v)
     md = _events_ms(lambda: bk.bk3_apply(p, E, B, D, G, u_smooth, vd, engine=bk.ENGINE_DFMA), max(3, steps // 4),
@@ -407,23 +472,34 @@ def run_bk3(args):
     bk.bk3_apply(p, E, B, D, G, u_rand, v)
     split_diff = float((vd - v).abs().max())
     del Gff
+    peak = measured_peak()[0]
     bytes64 = 8 * (2 * dofs + 6 * E * Q ** 3)
-    _line(args, f"BK3 Poisson p={p} (P=7 GLL, Q=8 Gauss), E={E}, FP64 float-float vs mixed (FP32 storage)",
-          dofs / ms / 1e6, ms, "f64",
-          {"forms": {"fp64_ff": {"gdofs": dofs / ms / 1e6, "hbm_frac": bytes64 / ms / 1e6 / measured_peak()[0]},
-                     "fp64_dfma": {"gdofs": dofs / md / 1e6},
-                     "fp64_ff_split_g": {"gdofs": dofs / mg / 1e6, "max_abs_diff_vs_fp64_ff": split_diff,
-                                         "hbm_frac": bytes64 / mg / 1e6 / measured_peak()[0]},
-                     "mixed": {"gdofs": dofs / mm / 1e6, "speedup_vs_fp64": ms / mm,
-                               "hbm_frac": bytes64 / 2 / mm / 1e6 / measured_peak()[0], "errors": errs}}})
+    nc = min(E, 8192)
+    Gc, uc = G[: nc * 6 * Q ** 3].cpu().numpy(), u_rand[: nc * P ** 3].cpu().numpy()
+    sec = _cpu_time(lambda: oracle.bk3(Q, nc, B, D, Gc, uc, fast=True))
+    return {"workload": f"BK3 Poisson p={p} (P=7 GLL, Q=8 Gauss), E={E}, affine mesh, FP64 float-float vs mixed "
+                        f"(FP32 storage)",
+            "gdofs": dofs / ms / 1e6, "ms_per_apply": ms, "dtype": "f64", "hbm_frac": bytes64 / ms / 1e6 / peak,
+            "rel_max_err_vs_oracle": err64, "oracle_elements": ns,
+            "forms": {"fp64_ff": {"gdofs": dofs / ms / 1e6, "hbm_frac": bytes64 / ms / 1e6 / peak},
+                      "fp64_dfma": {"gdofs": dofs / md / 1e6},
+                      "fp64_ff_split_g": {"gdofs": dofs / mg / 1e6, "max_abs_diff_vs_fp64_ff": split_diff,
+                                          "hbm_frac": bytes64 / mg / 1e6 / peak},
+                      "mixed": {"gdofs": dofs / mm / 1e6, "speedup_vs_fp64": ms / mm,
+                                "hbm_frac": bytes64 / 2 / mm / 1e6 / peak, "errors": errs}},
+            "cpu_baseline": _cpu_line(nc * P ** 3, sec, f"{nc} of the {E} elements, mean of 3 applies, "
+                                                        f"oracle/bk_oracle.c (-O3, OpenMP)")}
 
 
 def run_adjoint(args):
     """BK3 adjoint p = 4 (P = 5, Q = 6), E = 65536, log k ~ N(0, 0.5^2):
-    forward + backward timing and the central-difference check (h = 1e-6)."""
+    forward + backward timing, the FP64 host gradient of the oracle on the
+    first elements and the central-difference check (h = 1e-6, 64
+    directions)."""
     import torch
 
     import omp_bk_gb300 as bk
+    import oracle
     p, E = 4, args.elements or 65536
     P, Q = p + 1, p + 2
     B, D, xq, wq, _ = bk.bk1_bk3_matrices(p)
@@ -451,6 +527,12 @@ def run_adjoint(args):
     bk.bk3_adjoint(p, E, B, D, G, k, u, r, dk, dG)
     split_same = bool(torch.equal(dk, dk2) and torch.equal(dG, dG2))
     del Gff, dk2, dG2
+    # the FP64 host gradient on the first elements
+    ns = min(E, 256)
+    hs = lambda t, n: t[:n].cpu().numpy()   # noqa: E731
+    args_h = (hs(G, ns * 6 * Q ** 3), hs(k, ns * Q ** 3), hs(u, ns * P ** 3), hs(r, ns * P ** 3))
+    rdk, rdG = oracle.bk3_adjoint(Q, ns, B, D, *args_h)
+    host_err = max(_hostrel(hs(dk, ns * Q ** 3), rdk), _hostrel(hs(dG, ns * 6 * Q ** 3), rdG))
     ws = bk.dot_workspace(6 * E * Q ** 3)
     out = torch.zeros(1, dtype=torch.float64, device="cuda")
     fwd(k, G, r, bk.ENGINE_DFMA)
@@ -473,13 +555,20 @@ def run_adjoint(args):
         an += out.item()
         worst = max(worst, abs(fd - an) / abs(an))
     qdofs = E * Q ** 3
-    _line(args, f"BK3 adjoint p={p} (P=5, Q=6), E={E}, FP64: dL/dk, dL/dG of 1/2|A(k)u - f|^2",
-          qdofs / mb / 1e6, mb, "f64",
-          {"adjoint": {"backward_ms": mb, "forward_ms": mf, "backward_gpoints_s": qdofs / mb / 1e6,
-                       "backward_hbm_gbs": 8 * (2 * E * P ** 3 + 14 * qdofs) / mb / 1e6,
-                       "backward_split_g_gpoints_s": qdofs / mbg / 1e6, "split_g_bitwise": split_same,
-                       "fd_directions": 64, "fd_step": h, "fd_max_rel_err": worst},
-           "unit_note": "value = quadrature points per second of the backward kernel (G points/s)"})
+    nc = min(E, 4096)
+    args_c = (hs(G, nc * 6 * Q ** 3), hs(k, nc * Q ** 3), hs(u, nc * P ** 3), hs(r, nc * P ** 3))
+    sec = _cpu_time(lambda: oracle.bk3_adjoint(Q, nc, B, D, *args_c))
+    peak = measured_peak()[0]
+    bwd_bytes = 8 * (2 * E * P ** 3 + 14 * qdofs)
+    return {"workload": f"BK3 adjoint p={p} (P=5, Q=6), E={E}, FP64: dL/dk, dL/dG of 1/2|A(k)u - f|^2",
+            "gpoints_s": qdofs / mb / 1e6, "unit_note": "G points/s: quadrature points per second of the backward",
+            "backward_ms": mb, "forward_ms": mf, "dtype": "f64",
+            "backward_hbm_gbs": bwd_bytes / mb / 1e6, "hbm_frac": bwd_bytes / mb / 1e6 / peak,
+            "backward_split_g_gpoints_s": qdofs / mbg / 1e6, "split_g_bitwise": split_same,
+            "rel_max_err_vs_oracle_gradient": host_err, "oracle_elements": ns,
+            "fd_directions": 64, "fd_step": h, "fd_max_rel_err": worst,
+            "cpu_baseline": _cpu_line(nc * Q ** 3, sec, f"G points/s of the oracle's host gradient on {nc} of the "
+                                                        f"{E} elements, mean of 3 (oracle/bk_oracle.c, OpenMP)")}
 
 
 def run_helmholtz(args):
@@ -490,6 +579,7 @@ def run_helmholtz(args):
     import torch
 
     import omp_bk_gb300 as bk
+    import oracle
     from omp_bk_gb300 import helmholtz as hz
     from omp_bk_gb300 import tune
     orders = hz.config_orders()
@@ -502,6 +592,18 @@ def run_helmholtz(args):
     ustar = bk.fill_uniform(torch.empty(plan.n, dtype=torch.float64, device="cuda"), 5)
     f = torch.empty_like(ustar)
     plan.apply(G, M, 1.0, ustar, f, prec=bk.PREC_FP64)
+    # the FP64 persistent apply against the oracle (BK5 + mass), first elements of every order
+    errs = {}
+    Gh_s, Mh_s, uh_s = {}, {}, {}
+    for kk, p in enumerate(plan.p):
+        q, ns = p + 1, min(plan.E[kk], 64)
+        g = G[plan.goff[kk]: plan.goff[kk] + ns * 6 * q ** 3].cpu().numpy().reshape(ns, 6, q, q, q)
+        g = g.transpose(0, 3, 4, 1, 2).copy().ravel()   # column (f,k,i,j) -> BK5.cpp's (i,j,f,k)
+        m = M[plan.uoff[kk]: plan.uoff[kk] + ns * q ** 3].cpu().numpy()
+        uu = ustar[plan.uoff[kk]: plan.uoff[kk] + ns * q ** 3].cpu().numpy()
+        ref = oracle.bk5(q, ns, oracle.bk5_matrices(p)[0], g, uu, mass=m, lam=1.0)
+        errs[p] = _hostrel(f[plan.uoff[kk]: plan.uoff[kk] + ns * q ** 3].cpu().numpy(), ref)
+        Gh_s[p], Mh_s[p], uh_s[p] = g, m, uu
     u32, v32, v64 = ustar.float(), torch.empty(plan.n, dtype=torch.float32, device="cuda"), torch.empty_like(ustar)
     steps, warm = max(args.steps // 4, 10), max(args.warmup, 3)
     # every apply below is timed as one CUDA graph of its launches (device
@@ -543,15 +645,65 @@ def run_helmholtz(args):
     torch.cuda.synchronize()
     solve_s = time.perf_counter() - t
     err = float(torch.linalg.norm(x - ustar) / torch.linalg.norm(ustar))
-    _line(args, f"mixed-order Helmholtz p=2..8, E_p=2^(8-p)*{orders[-1][1]} ({plan.n} DoFs), one persistent launch",
-          plan.n / m_multi / 1e6, m_multi, "f32",
-          {"helmholtz": {"dofs": plan.n, "tiles": plan.ntiles, "tile_elems": best,
-                         "kernel": {bk.KERNEL_SWEEP: "sweep (even-odd)", bk.KERNEL_COLUMN: "column"}[plan.kernel],
-                         "multi_mixed_gdofs": plan.n / m_multi / 1e6, "multi_fp64_gdofs": plan.n / m_multi64 / 1e6,
-                         "multi_mixed_column_gdofs": plan.n / m_col / 1e6, "tile_elems_column": best_col,
-                         "per_order_mixed_gdofs": (plan.n / m_per32 / 1e6) if m_per32 else None,
-                         "per_order_fp64_gdofs": (plan.n / m_per64 / 1e6) if m_per64 else None,
-                         "cg": st, "cg_seconds": solve_s, "solution_rel_err": err}})
+    # CPU baseline: the oracle's BK5 + mass on the sampled elements of every order
+    units = sum((p + 1) ** 3 * Gh_s[p].size // (6 * (p + 1) ** 3) for p in plan.p)
+    sec = _cpu_time(lambda: [oracle.bk5(p + 1, Gh_s[p].size // (6 * (p + 1) ** 3), oracle.bk5_matrices(p)[0],
+                                        Gh_s[p], uh_s[p], mass=Mh_s[p], lam=1.0, fast=True) for p in plan.p])
+    return {"workload": f"mixed-order Helmholtz p=2..8, E_p=2^(8-p)*{orders[-1][1]} ({plan.n} DoFs), "
+                        f"one persistent launch, CG to 1e-10 (FP32 inner, FP64 refinement)",
+            "gdofs": plan.n / m_multi / 1e6, "ms_per_apply": m_multi, "dtype": "f32",
+            "hbm_frac": 36 * plan.n / m_multi / 1e6 / measured_peak()[0],
+            "rel_max_err_vs_oracle_fp64_apply": errs, "oracle_elements_per_order": 64,
+            "dofs": plan.n, "tiles": plan.ntiles, "tile_elems": best,
+            "kernel": {bk.KERNEL_SWEEP: "sweep (even-odd)", bk.KERNEL_COLUMN: "column"}[plan.kernel],
+            "multi_mixed_gdofs": plan.n / m_multi / 1e6, "multi_fp64_gdofs": plan.n / m_multi64 / 1e6,
+            "multi_mixed_column_gdofs": plan.n / m_col / 1e6, "tile_elems_column": best_col,
+            "per_order_mixed_gdofs": (plan.n / m_per32 / 1e6) if m_per32 else None,
+            "per_order_fp64_gdofs": (plan.n / m_per64 / 1e6) if m_per64 else None,
+            "cg": st, "cg_seconds": solve_s, "solution_rel_err": err,
+            "cpu_baseline": _cpu_line(units, sec, "BK5 + mass FP64 on the first 64 elements of every order, mean of "
+                                                  "3 (oracle/bk_oracle.c, -O3, OpenMP)")}
+
+
+def headline_parity(D, u, G, v, E, layout, prec, n=1024):
+    """max |v - oracle| / max |oracle| over the first and the last n elements
+    of the headline apply, the oracle (oracle.bk5, the checker build) run on
+    those elements' own u and G."""
+    import numpy as np
+
+    import oracle
+    Q = P_ORDER + 1
+    Q3 = Q ** 3
+    n = min(n, E)
+    worst, parts = 0.0, {}
+    for name, e0 in (("first", 0), ("last", E - n)):
+        uh = u[e0 * Q3: (e0 + n) * Q3].double().cpu().numpy()
+        g = G[e0 * 6 * Q3: (e0 + n) * 6 * Q3].double().cpu().numpy().reshape(n, 6, Q, Q, Q)
+        if layout == 0:      # (f,i,j,k) -> (i,j,f,k)
+            g = g.transpose(0, 2, 3, 1, 4)
+        elif layout == 2:    # (f,k,i,j) -> (i,j,f,k)
+            g = g.transpose(0, 3, 4, 1, 2)
+        else:
+            g = g.reshape(n, Q, Q, 6, Q)
+        ref = oracle.bk5(Q, n, np.asarray(D), np.ascontiguousarray(g).ravel(), uh)
+        err = _hostrel(v[e0 * Q3: (e0 + n) * Q3].double().cpu().numpy(), ref)
+        parts[name] = err
+        worst = max(worst, err)
+    return {"rel_max_err_vs_oracle": worst, "elements_checked": {"first": n, "last": n}, "by_range": parts,
+            "bound": 1e-12 if prec == 0 else 1e-5,
+            "oracle": "oracle/bk_oracle.c: bk::SumFactorization<double, 8> (openmp/BK5.cpp:19-103) restated, "
+                      "pinned to the reference's own kernels"}
+
+
+CONFIG_RUNS = {"bk1": run_bk1, "bk3": run_bk3, "adjoint": run_adjoint, "helmholtz": run_helmholtz}
+
+
+def run_config_line(args):
+    """--workload X: one configuration as its own JSON line."""
+    r = CONFIG_RUNS[args.workload](args)
+    value = r.get("gdofs", r.get("gpoints_s"))
+    ms = r.get("ms_per_apply", r.get("backward_ms"))
+    _line(args, r["workload"], value, ms, r.get("dtype", "f64"), {"result": r})
 
 
 def main():
@@ -559,7 +711,7 @@ def main():
     if args.impl == "reference":
         return run_reference(args)
     if args.workload != "bk5":
-        {"bk1": run_bk1, "bk3": run_bk3, "adjoint": run_adjoint, "helmholtz": run_helmholtz}[args.workload](args)
+        run_config_line(args)
         return 0
     import torch
 
@@ -596,11 +748,10 @@ def main():
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps, "warmup": warmup,
            "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "f64" if prec == bk.PREC_FP64 else "f32", "data": "synthetic",
-           "config": {"workload": f"BK5 collocated Laplacian p={P_ORDER} (P=Q=8 GLL) FP64 apply, E={E} "
-                                  f"({dofs} DoFs), jittered trilinear mesh, G6 layout {args.layout}",
-                      "p": P_ORDER, "elements": E, "engine": args.engine, "prec": args.prec, "kernel": args.kernel,
-                      "layout": args.layout, "l2": "inputs 8.6 GB >> 129 MB L2, no flush",
-                      "parallelism": f"replicas x{world}"},
+           "config": headline_config(E),
+           "options": {"engine": args.engine, "prec": args.prec, "kernel": args.kernel,
+                       "layout": f"G6 layout {args.layout} (2: column G(e,f,k,i,j))",
+                       "l2": "inputs 8.6 GB >> 129 MB L2, no flush", "parallelism": f"replicas x{world}"},
            "gpu_launches": steps,
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                         "frac": achieved / peak, "traffic": traffic,
@@ -621,18 +772,14 @@ def main():
         def step_e2e():
             hp.apply(uh, vh, G=G, D=D, engine=engine, layout=args.layout, kernel=kernel, stream=stream)
 
-        # three timed rounds, the best kept (the reference's time_min); the
-        # host link is shared with the machine's other work, so the rounds
-        # are reported too
-        rounds = [max_over_ranks(time_loop(step_e2e, max(3, steps // 10), 2, world, stream, torch), world)
-                  for _ in range(3)]
-        te = min(rounds)
+        # K timed calls after the warm-up, the mean per call (the statistic of
+        # `value` and of the reference arm)
+        te = max_over_ranks(time_loop(step_e2e, steps, warmup, world, stream, torch), world)
         torch.cuda.synchronize()
         e2e_err = float((vh.to(v.device) - v).abs().max())
         hp.close()
         out["e2e"] = {"value": world * dofs / te / 1e9, "unit": UNIT, "h2d_bytes_per_step": u.element_size() * dofs,
                       "d2h_bytes_per_step": u.element_size() * dofs, "ms_per_step": te * 1e3,
-                      "rounds_ms_per_step": [r * 1e3 for r in rounds],
                       "max_abs_diff_vs_device_apply": e2e_err,
                       "note": "bk5_apply_host: G (6.4 GB) resident on the device; u in, v out every step "
                               "from/to pinned host memory in 16 element chunks, copies overlapping the applies"}
@@ -641,7 +788,7 @@ def main():
     if not args.no_forms and rank == 0 and prec == bk.PREC_FP64:
         forms = {}
         ref = v.clone()
-        forms["fp64_ff"] = {"gdofs": value / world, "rel_err_vs_fp64": 0.0}
+        forms["fp64_ff"] = {"gdofs": value / world}
         vd = torch.empty_like(v)
         td = time_loop(lambda: bk.bk5_apply(P_ORDER, E, D, G, u, vd, engine=bk.ENGINE_DFMA, layout=args.layout,
                                             stream=stream),
@@ -662,18 +809,39 @@ def main():
         del vd
         u32, G32 = u.float(), G.float()
         v32 = torch.empty_like(u32)
-        for name, prec in (("mixed_fp32_storage", bk.PREC_MIXED), ("fp32", bk.PREC_FP32)):
-            tm = time_loop(lambda: bk.bk5_apply(P_ORDER, E, D, G32, u32, v32, prec=prec, layout=args.layout,
+        for name, pr in (("mixed_fp32_storage", bk.PREC_MIXED), ("fp32", bk.PREC_FP32)):
+            tm = time_loop(lambda: bk.bk5_apply(P_ORDER, E, D, G32, u32, v32, prec=pr, layout=args.layout,
                                                 stream=stream),
                            max(3, steps // 4), 3, 1, stream, torch)
             err = float((v32.double() - ref).abs().max() / ref.abs().max())
-            forms[name] = {"gdofs": dofs / tm / 1e9, "rel_err_vs_fp64": err,
+            # against the FP64 oracle on the FP64 inputs (storage rounding included)
+            orc = headline_parity(D, u, G, v32, E, args.layout, bk.PREC_FP64)["rel_max_err_vs_oracle"]
+            forms[name] = {"gdofs": dofs / tm / 1e9, "rel_err_vs_fp64": err, "rel_err_vs_oracle": orc,
+                           "speedup_vs_fp64": (dofs / tm / 1e9) / (value / world),
                            "hbm_frac": 4 * 8 * dofs / tm / 1e9 / peak}
         out["forms"] = forms
         del u32, G32, v32
 
+    # the headline's own result against the FP64 oracle: the first and the
+    # last elements of u and G copied to the host (G relaid to BK5.cpp's
+    # interleaved layout), oracle.bk5 on them
+    if rank == 0:
+        out["parity"] = headline_parity(D, u, G, v, E, args.layout, prec)
+        if "forms" in out:
+            out["forms"]["fp64_ff"]["rel_err_vs_oracle"] = out["parity"]["rel_max_err_vs_oracle"]
+
+    if rank == 0 and world == 1 and not args.no_configs and E == E_FULL:
+        out["configs"] = {}
+        for name, fn in CONFIG_RUNS.items():
+            try:
+                out["configs"][name] = fn(args)
+            except Exception as exc:   # recorded, so that the headline line still prints
+                out["configs"][name] = {"error": f"{type(exc).__name__}: {exc}"}
+            torch.cuda.synchronize()
+            torch.cuda.empty_cache()
+
     if rank == 0 and world == 1 and not args.no_cpu:
-        out["cpu_baseline"] = cpu_baseline_run(32768, 3)
+        out["cpu_baseline"] = cpu_bk5_run(E, 3, 1)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:

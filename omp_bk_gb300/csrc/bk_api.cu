@@ -1,5 +1,6 @@
 // bk_api.cu -- the C ABI of include/bk_gpu.h: argument checks on the host,
 // order/precision/engine dispatch, the device status word.
+#include <atomic>
 #include <cstdint>
 #include <cstring>
 
@@ -19,9 +20,14 @@ __device__ int g_status_word;
 
 namespace {
 constexpr long long kDefaultWaitLimit = 4000000000LL;   // SM cycles, ~2 s
-long long g_wait_limit[kMaxDevices];
-int* g_status_ptr[kMaxDevices];
-int g_sm_count[kMaxDevices];
+// Per-device values filled in on first use.  Host threads may make their
+// first calls on a device at the same time: each slot is an atomic, and two
+// threads that both look a value up store the same value.  The status word's
+// address is that of this module's copy in the device's primary context; the
+// library is not meant to outlive a reset of that context (cudaDeviceReset).
+std::atomic<long long> g_wait_limit[kMaxDevices];
+std::atomic<int*> g_status_ptr[kMaxDevices];
+std::atomic<int> g_sm_count[kMaxDevices];
 }  // namespace
 
 int current_device()
@@ -35,24 +41,27 @@ int sm_count()
 {
     const int d = current_device();
     if (d < 0 || d >= kMaxDevices) return 1;
-    if (g_sm_count[d] == 0) {
-        int n = 0;
+    int n = g_sm_count[d].load(std::memory_order_acquire);
+    if (n == 0) {
         cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, d);
-        g_sm_count[d] = n > 0 ? n : 1;
+        n = n > 0 ? n : 1;
+        g_sm_count[d].store(n, std::memory_order_release);
     }
-    return g_sm_count[d];
+    return n;
 }
 
 static int* status_ptr()
 {
     const int d = current_device();
     if (d < 0 || d >= kMaxDevices) return nullptr;
-    if (g_status_ptr[d] == nullptr) {
+    int* ptr = g_status_ptr[d].load(std::memory_order_acquire);
+    if (ptr == nullptr) {
         void* p = nullptr;
         if (cudaGetSymbolAddress(&p, g_status_word) != cudaSuccess) return nullptr;
-        g_status_ptr[d] = static_cast<int*>(p);
+        ptr = static_cast<int*>(p);
+        g_status_ptr[d].store(ptr, std::memory_order_release);
     }
-    return g_status_ptr[d];
+    return ptr;
 }
 
 DevCtx dev_ctx()
@@ -60,7 +69,8 @@ DevCtx dev_ctx()
     const int d = current_device();
     DevCtx c;
     c.status = status_ptr();
-    c.wait_limit = (d >= 0 && d < kMaxDevices && g_wait_limit[d] > 0) ? g_wait_limit[d] : kDefaultWaitLimit;
+    const long long lim = (d >= 0 && d < kMaxDevices) ? g_wait_limit[d].load(std::memory_order_relaxed) : 0;
+    c.wait_limit = lim > 0 ? lim : kDefaultWaitLimit;
     return c;
 }
 
@@ -294,7 +304,7 @@ int bk_set_wait_limit(long long cycles)
     const int d = current_device();
     if (d < 0 || d >= kMaxDevices) return BK_ERR_CUDA;
     if (cycles < 0) return BK_ERR_ARG;
-    g_wait_limit[d] = cycles;
+    g_wait_limit[d].store(cycles, std::memory_order_relaxed);
     return BK_OK;
 }
 

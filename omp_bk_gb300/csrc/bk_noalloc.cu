@@ -16,11 +16,15 @@
 // Host code cannot use the array's name as a device address (in host code it
 // names a host-side stand-in): the device address is looked up once per
 // device with cudaGetSymbolAddress, with that device current, on the first
-// call made on it -- so make a first call before capturing a stream.  Every
+// call made on it -- so make a first call before capturing a stream.  The
+// address cached per device is an atomic, so host threads that make their
+// first calls at the same time are safe; it belongs to the device's primary
+// context, so the library must not be used across a cudaDeviceReset.  Every
 // call shares the array and leaves its last partial sums in it; a call reads
 // back only the partials it has just written, so nothing has to start at
 // zero.  Calls whose kernels overlap on the GPU (different streams, no
 // ordering between them) race on the array.
+#include <atomic>
 #include <cstdint>
 
 #include <cuda_runtime.h>
@@ -38,7 +42,7 @@ constexpr int kThreads = 256;
 
 static __device__ __align__(256) double g_noalloc_scratch[kNoAllocPartials];
 
-double* g_scratch_ptr[bkg::kMaxDevices];
+std::atomic<double*> g_scratch_ptr[bkg::kMaxDevices];
 
 template <class T>
 __global__ void __launch_bounds__(kThreads) chunk_dot_kernel(const T* __restrict__ x, const T* __restrict__ y,
@@ -79,15 +83,16 @@ double* scratch_on_current_device()
 {
     const int dev = bkg::current_device();
     if (dev < 0 || dev >= bkg::kMaxDevices) return nullptr;
-    if (g_scratch_ptr[dev] == nullptr) {
-        double* p = nullptr;
+    double* p = g_scratch_ptr[dev].load(std::memory_order_acquire);
+    if (p == nullptr) {
         if (cudaGetSymbolAddress(reinterpret_cast<void**>(&p), g_noalloc_scratch) != cudaSuccess) {
             cudaGetLastError();
             return nullptr;
         }
-        g_scratch_ptr[dev] = p;
+        // two threads that race here store the same address
+        g_scratch_ptr[dev].store(p, std::memory_order_release);
     }
-    return g_scratch_ptr[dev];
+    return p;
 }
 
 }  // namespace

@@ -69,6 +69,22 @@ def lib(fast: bool = False):
     _declare(L, "bko_rel_maxdiff", C.c_double, [_dp, _dp, _sz])
     _declare(L, "bko_bk3_adjoint", None, [C.c_int, _sz, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp])
     _declare(L, "bko_max_nq", C.c_int, [])
+    # inputs of the benchmark configurations (bk_geom_oracle.c)
+    u64 = C.c_uint64
+    _declare(L, "bko_splitmix64", u64, [u64])
+    _declare(L, "bko_uniform01", C.c_double, [u64, u64])
+    _declare(L, "bko_fill_uniform", None, [_dp, _sz, u64, C.c_double, C.c_double])
+    _declare(L, "bko_fill_lognormal", None, [_dp, _sz, u64, C.c_double])
+    _declare(L, "bko_gauss", C.c_int, [C.c_int, _dp, _dp])
+    _declare(L, "bko_gll", C.c_int, [C.c_int, _dp, _dp])
+    _declare(L, "bko_lagrange_interp", C.c_int, [C.c_int, _dp, C.c_int, _dp, _dp])
+    _declare(L, "bko_lagrange_deriv", C.c_int, [C.c_int, _dp, _dp])
+    _declare(L, "bko_geom_affine", None, [C.c_int, _sz, _sz, _dp, _dp, u64, C.c_double, C.c_double,
+                                          C.c_void_p, C.c_void_p, C.c_int])
+    _declare(L, "bko_coords_affine", None, [C.c_int, _sz, _sz, C.c_int, C.c_int, _dp, u64, C.c_double,
+                                            C.c_double, _dp])
+    _declare(L, "bko_geom_trilinear", None, [C.c_int, _sz, _sz, C.c_int, C.c_int, _dp, _dp, u64, C.c_double,
+                                             C.c_double, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p])
     _libs[key] = L
     return L
 
@@ -188,3 +204,98 @@ def reference_bk5(nq, E, D, G6i, u):
     f = np.float32
     lib().bko_reference_bk5(nq, E, _c(D, f), _c(G6i, f), _c(u, f), out)
     return out
+
+
+# ---- inputs of the benchmark configurations (bk_geom_oracle.c) ----------------
+
+def _opt(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def uniform(n, seed, lo=-1.0, hi=1.0, fast=False):
+    """lo + (hi - lo) U(seed, i), i = 0..n-1 (splitmix64 streams)."""
+    out = np.empty(int(n))
+    lib(fast).bko_fill_uniform(out, out.size, seed, lo, hi)
+    return out
+
+
+def lognormal(n, seed, sigma, fast=False):
+    out = np.empty(int(n))
+    lib(fast).bko_fill_lognormal(out, out.size, seed, sigma)
+    return out
+
+
+def gauss(n):
+    x, w = np.empty(n), np.empty(n)
+    assert lib().bko_gauss(n, x, w) == 0
+    return x, w
+
+
+def gll(n):
+    x, w = np.empty(n), np.empty(n)
+    assert lib().bko_gll(n, x, w) == 0
+    return x, w
+
+
+def lagrange_interp(nodes, pts):
+    nodes, pts = _c(nodes, np.float64), _c(pts, np.float64)
+    B = np.empty(nodes.size * pts.size)
+    assert lib().bko_lagrange_interp(nodes.size, nodes, pts.size, pts, B) == 0
+    return B
+
+
+def lagrange_deriv(x):
+    x = _c(x, np.float64)
+    D = np.empty(x.size * x.size)
+    assert lib().bko_lagrange_deriv(x.size, x, D) == 0
+    return D
+
+
+def bk5_matrices(p):
+    """(D, x, w) of BK5 at order p: Q = p + 1 GLL points, D(i, n) = l_n'(x_i)
+    (openmp/BK5.cpp's dbasis[i*nq + n])."""
+    x, w = gll(p + 1)
+    return lagrange_deriv(x), x, w
+
+
+def bk1_bk3_matrices(p):
+    """(B, D, gauss x, gauss w, gll x) of BK1/BK3 at order p: B(i, q) =
+    l_i(xq_q) from P = p + 1 GLL nodes to Q = p + 2 Gauss points, and BK3's
+    D(n, q) = l_n'(xq_q) on the Gauss points (openmp/bk3_sumfact.h's
+    dbasis[n*nq + q])."""
+    xn, _ = gll(p + 1)
+    xq, wq = gauss(p + 2)
+    B = lagrange_interp(xn, xq)
+    Q = p + 2
+    D = lagrange_deriv(xq).reshape(Q, Q).T.copy().ravel()
+    return B, D, xq, wq, xn
+
+
+def geom_affine(Q, e0, ne, x, w, seed, h, pert, qdata=True, G=True, layout=0, fast=False):
+    """(qdata, G) of elements e0..e0+ne-1 of the affine mesh (None where not
+    asked for)."""
+    Q3 = Q ** 3
+    q = np.empty(ne * Q3) if qdata else None
+    g = np.empty(ne * 6 * Q3) if G else None
+    lib(fast).bko_geom_affine(Q, e0, ne, _c(x, np.float64), _c(w, np.float64), seed, h, pert, _opt(q), _opt(g),
+                              layout)
+    return q, g
+
+
+def coords_affine(Q, e0, ne, nx, ny, x, seed, h, pert):
+    out = np.empty(ne * Q ** 3 * 3)
+    lib().bko_coords_affine(Q, e0, ne, nx, ny, _c(x, np.float64), seed, h, pert, out)
+    return out
+
+
+def geom_trilinear(Q, e0, ne, nx, ny, x, w, seed, h, jit, G=True, layout=1, mass=False, coords=False,
+                   fast=False):
+    """(G, mass, coords) of elements e0..e0+ne-1 of the jittered trilinear
+    mesh on an nx x ny x .. grid (None where not asked for)."""
+    Q3 = Q ** 3
+    g = np.empty(ne * 6 * Q3) if G else None
+    m = np.empty(ne * Q3) if mass else None
+    c = np.empty(ne * Q3 * 3) if coords else None
+    lib(fast).bko_geom_trilinear(Q, e0, ne, nx, ny, _c(x, np.float64), _c(w, np.float64), seed, h, jit, _opt(g),
+                                 layout, _opt(m), _opt(c))
+    return g, m, c

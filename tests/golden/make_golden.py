@@ -1,7 +1,8 @@
 """Generate tests/golden/golden.npz from the reference's OWN host kernels.
 
-Run in a container that holds the reference's sources (default
-/root/reference): ``make -C oracle ref`` compiles them by include path into
+Run where the reference's sources are present (the tree named by
+$BK_REF_DIR or --ref; by default the one oracle/Makefile names):
+``make -C oracle ref`` compiles them by include path into
 oracle/_ref/, and this script calls them through ctypes.  The fixtures pin the
 oracle (tests/test_oracle.py) and the CUDA kernels (tests/test_golden_gpu.py)
 to the reference's results on the reference's own test data:
@@ -16,7 +17,7 @@ to the reference's results on the reference's own test data:
   * make_bk5_G in every (F, layout) and transpose_jxw on one element;
   * the first LCG draws and a test basis.
 
-Usage:  python tests/golden/make_golden.py [--ref /root/reference]
+Usage:  python tests/golden/make_golden.py [--ref <reference tree>]
 """
 import argparse
 import ctypes as C
@@ -38,7 +39,8 @@ fp = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
 
 
 def load(ref):
-    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={ref}"], check=True)
+    cmd = ["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"] + ([f"REF={ref}"] if ref else [])
+    subprocess.run(cmd, check=True)
     d = os.path.join(ROOT, "oracle", "_ref")
     L = {k: C.CDLL(os.path.join(d, f"libbkref_{k}.so")) for k in ("bk1", "bk3", "bk5", "harness")}
     for sfx, p in (("f64", dp), ("f32", fp)):
@@ -73,7 +75,8 @@ def rand(H, nin, nj):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("BK_REF_DIR"),
+                    help="the reference's source tree (default: $BK_REF_DIR, else the oracle Makefile's)")
     args = ap.parse_args()
     L = load(args.ref)
     H = L["harness"]

@@ -148,3 +148,100 @@ def test_adjoint_oracle_fd(oracle_lib):
         dg = rng.standard_normal(G.size)
         fd = (loss(k, G + h * dg) - loss(k, G - h * dg)) / (2 * h)
         assert abs(fd - dG @ dg) <= 1e-7 * max(1.0, abs(fd))
+
+
+# ---- inputs of the benchmark configurations (oracle/bk_geom_oracle.c) --------
+
+def test_splitmix64_known_values(oracle_lib):
+    """splitmix64 (Steele, Lea, Flood 2014) from state 0: the generator's
+    published first outputs."""
+    L = oracle_lib.lib()
+    assert L.bko_splitmix64(0) == 0xE220A8397B1DCDAF
+    assert L.bko_splitmix64(0x9E3779B97F4A7C15) == 0x6E789E6AA1B965F4
+    # U(s, i): the top 53 bits over 2^53
+    s = L.bko_splitmix64(5)
+    assert L.bko_uniform01(5, 3) == (L.bko_splitmix64((s + 3) % 2 ** 64) >> 11) / 2.0 ** 53
+    u = oracle_lib.uniform(100000, 9)
+    assert -1.0 <= u.min() and u.max() < 1.0 and abs(u.mean()) < 0.01
+
+
+@pytest.mark.parametrize("n", range(2, 11))
+def test_rules(oracle_lib, n):
+    o = oracle_lib
+    xg, wg = o.gauss(n)
+    xr, wr = np.polynomial.legendre.leggauss(n)
+    assert np.abs(xg - xr).max() < 1e-14 and np.abs(wg - wr).max() < 1e-14
+    x, w = o.gll(n)
+    inner = np.sort(np.polynomial.legendre.Legendre.basis(n - 1).deriv().roots().real)
+    assert x[0] == -1.0 and x[-1] == 1.0 and (n == 2 or np.abs(x[1:-1] - inner).max() < 1e-13)
+    # GLL is exact for degree 2n - 3
+    for k in range(2 * n - 2):
+        exact = 0.0 if k % 2 else 2.0 / (k + 1)
+        assert abs(w @ x ** k - exact) < 1e-14
+    D = o.lagrange_deriv(x).reshape(n, n)
+    assert np.abs(D @ np.ones(n)).max() < 1e-12 and np.abs(D @ x - 1).max() < 1e-12
+    B = o.lagrange_interp(x, xg).reshape(n, n)   # B(i, q) = l_i(xg_q)
+    assert np.abs(B.sum(axis=0) - 1).max() < 1e-14 and np.abs(x @ B - xg).max() < 1e-14
+
+
+def test_affine_geometry_analytic(oracle_lib):
+    """Undistorted affine elements (pert = 0): J = (h/2) I, so qdata = w h^3/8
+    (summing to h^3 per element) and G = w (h/2) I."""
+    o = oracle_lib
+    Q, h, E = 5, 1.0 / 16, 3
+    x, w = o.gauss(Q)
+    q, G = o.geom_affine(Q, 0, E, x, w, 21, h, 0.0)
+    W = np.einsum("i,j,k->ijk", w, w, w).ravel()
+    assert np.abs(q.reshape(E, -1).sum(axis=1) - h ** 3).max() < 1e-15
+    G = G.reshape(E, 6, -1)
+    for f, diag in enumerate((1, 0, 0, 1, 0, 1)):
+        assert np.abs(G[:, f] - diag * W * h / 2).max() <= 1e-16
+
+
+def test_affine_geometry_against_numpy(oracle_lib):
+    """G = w det J J^-1 J^-T with J from the stated seeded perturbation,
+    formed here by numpy's inverse (a third formula)."""
+    o = oracle_lib
+    Q, h, pert, seed, E = 4, 1.0 / 16, 0.2, 41, 5
+    x, w = o.gauss(Q)
+    q, G = o.geom_affine(Q, 0, E, x, w, seed, h, pert, layout=1)
+    L = o.lib()
+    G = G.reshape(E, Q, Q, 6, Q)
+    for e in range(E):
+        P = np.array([[2 * L.bko_uniform01(seed, 9 * e + 3 * a + b) - 1 for b in range(3)] for a in range(3)])
+        J = 0.5 * h * (np.eye(3) + pert * P)
+        K = np.linalg.inv(J)
+        M = np.linalg.det(J) * K @ K.T
+        for i, j, k in ((0, 0, 0), (1, 2, 3), (3, 3, 1)):
+            wp = w[i] * w[j] * w[k]
+            ref = wp * np.array([M[0, 0], M[0, 1], M[0, 2], M[1, 1], M[1, 2], M[2, 2]])
+            assert np.abs(G[e, i, j, :, k] - ref).max() <= 1e-14 * np.abs(ref).max()
+            assert abs(q[(e * Q + i) * Q * Q + j * Q + k] - wp * np.linalg.det(J)) <= 1e-14 * wp * h ** 3
+
+
+def test_trilinear_geometry(oracle_lib):
+    """Without jitter the trilinear map of a grid cell is the affine map
+    x = c + (h/2) xi: G = w (h/2) I and the coordinates follow; with jitter
+    the three layouts hold the same factors and the mass is w det J."""
+    o = oracle_lib
+    Q, h, nx = 4, 0.25, 3
+    x, w = o.gll(Q)
+    G, m, c = o.geom_trilinear(Q, 0, 30, nx, nx, x, w, 5, h, 0.0, layout=0, mass=True, coords=True)
+    W = np.einsum("i,j,k->ijk", w, w, w).ravel()
+    G = G.reshape(30, 6, -1)
+    for f, diag in enumerate((1, 0, 0, 1, 0, 1)):
+        assert np.abs(G[:, f] - diag * W * h / 2).max() <= 1e-15
+    assert np.abs(m.reshape(30, -1) - W * h ** 3 / 8).max() <= 1e-16
+    c = c.reshape(30, Q, Q, Q, 3)
+    e = 23   # cell (2, 1, 2)
+    assert abs(c[e, 1, 2, 3, 0] - (2.5 + 0.5 * x[1]) * h) < 1e-15
+    assert abs(c[e, 1, 2, 3, 1] - (1.5 + 0.5 * x[2]) * h) < 1e-15
+    assert abs(c[e, 1, 2, 3, 2] - (2.5 + 0.5 * x[3]) * h) < 1e-15
+    # jittered: the three layouts are permutations of one another
+    g = [o.geom_trilinear(Q, 7, 4, nx, nx, x, w, 5, h, 0.15, layout=L)[0].reshape(4, -1) for L in (0, 1, 2)]
+    g0 = g[0].reshape(4, 6, Q, Q, Q)
+    assert np.array_equal(np.ascontiguousarray(g0.transpose(0, 2, 3, 1, 4)).reshape(4, -1), g[1])
+    assert np.array_equal(np.ascontiguousarray(g0.transpose(0, 1, 4, 2, 3)).reshape(4, -1), g[2])
+    # an element range gives the same elements as the full array
+    full = o.geom_trilinear(Q, 0, 11, nx, nx, x, w, 5, h, 0.15, layout=1)[0].reshape(11, -1)
+    assert np.array_equal(full[7:11], g[1])
