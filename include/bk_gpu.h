@@ -101,7 +101,16 @@ typedef struct bk_options {
                             GB300 and ignore it */
     int kernel;    /* bk_kernel_shape (BK5); BK1/BK3 have the sweep kernel only */
     int gform;     /* bk_gform (BK5, BK3, the adjoint): how G is stored */
+    int jxw_layout; /* bk_jxw_layout (BK1): the order of qdata's points */
 } bk_options;
+
+/* BK1 qdata ("JxW") layouts. */
+enum bk_jxw_layout {
+    BK_JXW_PQR = 0,  /* JxW(e, p, q, r), r fastest: bk1_sumfact.h's layout (:53) */
+    BK_JXW_RQP = 1   /* JxW_t(e, r, q, p), p fastest: the layout transpose_jxw
+                        makes (include/bk_harness.h:89-102) and the SYCL BK1
+                        variants read (sycl/bk1_sycl.cpp:74-98) */
+};
 
 /* Geometric-factor storage forms (BK5, BK3). */
 enum bk_gform {
@@ -134,7 +143,7 @@ enum bk_kernel_shape {
 
 /* bk_options with the defaults: prec FP64, engine AUTO, BK5 layout
  * INTERLEAVED with 6 factors, elems_per_block 0, kernel AUTO, gform
- * STORAGE. */
+ * STORAGE, jxw_layout PQR. */
 bk_options bk_default_options(void);
 
 /* ---- operator apply ------------------------------------------------------- */
@@ -142,7 +151,9 @@ bk_options bk_default_options(void);
 /* BK1 mass operator v = B^T diag(qdata) B u per element
  * (replaces bk::SumFactorization<T, nq>, openmp/bk1_sumfact.h:16-159).
  *   B      host, P x Q doubles, B(i,p) = B[i*Q+p]
- *   qdata  device, E x Q^3 (quadrature weight x detJ, "JxW" in the reference)
+ *   qdata  device, E x Q^3 (quadrature weight x detJ, "JxW" in the reference),
+ *          JxW(e,p,q,r); bk1_apply_opt with jxw_layout BK_JXW_RQP reads
+ *          JxW_t(e,r,q,p) instead
  *   u, v   device, E x P^3 */
 int bk1_apply(int p, int64_t E, const double* B, const void* qdata, const void* u, void* v,
               int prec, bk_stream_t stream);
@@ -207,6 +218,13 @@ int bk3_adjoint(int p, int64_t E, const double* B, const double* D, const void* 
  * otherwise), device, 16-byte aligned, distinct.  Asynchronous on stream. */
 int bk5_make_g(int p, int64_t E, const void* G6i, void* G, int nfactors, int layout, int prec,
                bk_stream_t stream);
+
+/* transpose_jxw on the device (replaces include/bk_harness.h:89-102):
+ * JxW(e, p, q, r) -> JxW_t(e, r, q, p) for BK1 with Q = p + 2 points per
+ * direction, in the storage type of prec; device, 16-byte aligned, distinct.
+ * BK1 reads the result with jxw_layout = BK_JXW_RQP.  Asynchronous on
+ * stream. */
+int bk1_transpose_jxw(int p, int64_t E, const void* jxw, void* jxw_t, int prec, bk_stream_t stream);
 
 /* Splits n doubles G (device) into float-float pairs Gff (device, n x 8
  * bytes; may be G itself: the conversion is in place value by value): hi =

@@ -35,6 +35,7 @@ ENGINE_AUTO, ENGINE_DFMA, ENGINE_FF = 0, 1, 2
 LAYOUT_FACTOR, LAYOUT_INTERLEAVED, LAYOUT_COLUMN = 0, 1, 2
 KERNEL_AUTO, KERNEL_SWEEP, KERNEL_COLUMN = 0, 1, 2
 G_STORAGE, G_FF = 0, 1
+JXW_PQR, JXW_RQP = 0, 1
 
 # every symbol the C headers declare (checked by the CPU tests)
 EXPORTS = [
@@ -47,7 +48,7 @@ EXPORTS = [
     "bk_hplan_create", "bk_hplan_destroy", "bk_hplan_size", "bk_hplan_set_kernel", "bk_hplan_apply", "bk_hplan_cg",
     "bk_dot_noalloc",
     "bk_host_plan_create", "bk_host_plan_destroy", "bk1_apply_host", "bk3_apply_host", "bk5_apply_host",
-    "bk_g_to_ff", "bk5_make_g",
+    "bk_g_to_ff", "bk5_make_g", "bk1_transpose_jxw",
 ]
 
 
@@ -61,7 +62,7 @@ class BKError(RuntimeError):
 
 class Options(C.Structure):
     _fields_ = [("prec", C.c_int), ("engine", C.c_int), ("layout", C.c_int), ("nfactors", C.c_int),
-                ("elems_per_block", C.c_int), ("kernel", C.c_int), ("gform", C.c_int)]
+                ("elems_per_block", C.c_int), ("kernel", C.c_int), ("gform", C.c_int), ("jxw_layout", C.c_int)]
 
 
 _lib = None
@@ -110,6 +111,7 @@ def lib():
         "bk_axpby": [C.c_longlong, C.c_double, _vp, C.c_double, _vp, C.c_int, _vp],
         "bk_g_to_ff": [_vp, _vp, _i64, _vp],
         "bk5_make_g": [C.c_int, _i64, _vp, _vp, C.c_int, C.c_int, C.c_int, _vp],
+        "bk1_transpose_jxw": [C.c_int, _i64, _vp, _vp, C.c_int, _vp],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -173,19 +175,22 @@ class ApplyOptions:
     elems_per_block: int = 0
     kernel: int = KERNEL_AUTO
     gform: int = G_STORAGE
+    jxw_layout: int = JXW_PQR
 
     def c(self) -> Options:
         return Options(self.prec, self.engine, self.layout, self.nfactors, self.elems_per_block, self.kernel,
-                       self.gform)
+                       self.gform, self.jxw_layout)
 
 
 # ---- operator apply (device tensors) -------------------------------------------
 
-def bk1_apply(p, E, B, qdata, u, v, prec=PREC_FP64, engine=ENGINE_AUTO, stream=None):
-    """v = B^T diag(qdata) B u per element (openmp/bk1_sumfact.h:16-159)."""
+def bk1_apply(p, E, B, qdata, u, v, prec=PREC_FP64, engine=ENGINE_AUTO, jxw_layout=JXW_PQR, stream=None):
+    """v = B^T diag(qdata) B u per element (openmp/bk1_sumfact.h:16-159);
+    jxw_layout=JXW_RQP: qdata is JxW_t(e, r, q, p), as bk1_transpose_jxw
+    (transpose_jxw, include/bk_harness.h:89-102) makes it."""
     _order(p, "bk1_apply")
     Bh, Bp = _host(B)
-    o = ApplyOptions(prec=prec, engine=engine).c()
+    o = ApplyOptions(prec=prec, engine=engine, jxw_layout=jxw_layout).c()
     check(lib().bk1_apply_opt(p, E, Bp, _ptr(qdata), _ptr(u), _ptr(v), C.byref(o), _stream(stream)), "bk1_apply")
 
 
@@ -223,6 +228,17 @@ def bk5_make_g(p, E, G6i, nfactors=6, layout=LAYOUT_COLUMN, out=None, stream=Non
         out = torch.empty(E * nfactors * q ** 3, dtype=G6i.dtype, device=G6i.device)
     prec = PREC_FP64 if G6i.dtype == torch.float64 else PREC_FP32
     check(lib().bk5_make_g(p, E, _ptr(G6i), _ptr(out), nfactors, layout, prec, _stream(stream)), "bk5_make_g")
+    return out
+
+
+def bk1_transpose_jxw(p, E, jxw, out=None, stream=None):
+    """transpose_jxw (include/bk_harness.h:89-102) on the device: JxW(e, p,
+    q, r) -> JxW_t(e, r, q, p), Q = p + 2; float64 or float32 tensors."""
+    import torch
+    if out is None:
+        out = torch.empty_like(jxw)
+    prec = PREC_FP64 if jxw.dtype == torch.float64 else PREC_FP32
+    check(lib().bk1_transpose_jxw(p, E, _ptr(jxw), _ptr(out), prec, _stream(stream)), "bk1_transpose_jxw")
     return out
 
 
@@ -438,10 +454,11 @@ class HostPlan:
     __del__ = close
 
     def apply(self, u_host, v_host, G=None, B=None, D=None, k=None, engine=ENGINE_AUTO,
-              layout=LAYOUT_INTERLEAVED, nfactors=6, kernel=KERNEL_AUTO, stream=None):
+              layout=LAYOUT_INTERLEAVED, nfactors=6, kernel=KERNEL_AUTO, jxw_layout=JXW_PQR, stream=None):
         """v_host = A u_host (torch CPU tensors or numpy arrays); G: qdata
         (BK1) or the geometric factors (BK3, BK5) on the device."""
-        o = ApplyOptions(prec=self.prec, engine=engine, layout=layout, nfactors=nfactors, kernel=kernel).c()
+        o = ApplyOptions(prec=self.prec, engine=engine, layout=layout, nfactors=nfactors, kernel=kernel,
+                         jxw_layout=jxw_layout).c()
         uptr = u_host.data_ptr() if hasattr(u_host, "data_ptr") else u_host.ctypes.data
         vptr = v_host.data_ptr() if hasattr(v_host, "data_ptr") else v_host.ctypes.data
         L = lib()

@@ -143,6 +143,7 @@ bk_options bk_default_options(void)
     o.elems_per_block = 0;
     o.kernel = BK_KERNEL_AUTO;
     o.gform = BK_G_STORAGE;
+    o.jxw_layout = BK_JXW_PQR;
     return o;
 }
 
@@ -207,14 +208,16 @@ int bk1_apply_opt(int p, int64_t E, const double* B, const void* qdata, const vo
     if ((rc = check_ptrs(E, {qdata, u, v}))) return rc;
     const int eng = engine_of(o);
     if (eng < 0 || o.gform != BK_G_STORAGE) return BK_ERR_PREC;
+    if (o.jxw_layout != BK_JXW_PQR && o.jxw_layout != BK_JXW_RQP) return BK_ERR_ARG;
     if (E == 0) return BK_OK;
     if ((rc = status_or_null())) return rc;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const int jt = o.jxw_layout == BK_JXW_RQP;
     switch (eng) {
-        case 0: return launch_bk1_dfma(p, E, B, qdata, u, v, o.elems_per_block, s);
-        case 1: return launch_bk1_ff(p, E, B, qdata, u, v, o.elems_per_block, s);
-        case 2: return launch_bk1_f32(p, E, B, qdata, u, v, o.elems_per_block, s);
-        default: return launch_bk1_mixed(p, E, B, qdata, u, v, o.elems_per_block, s);
+        case 0: return launch_bk1_dfma(p, E, B, qdata, u, v, o.elems_per_block, jt, s);
+        case 1: return launch_bk1_ff(p, E, B, qdata, u, v, o.elems_per_block, jt, s);
+        case 2: return launch_bk1_f32(p, E, B, qdata, u, v, o.elems_per_block, jt, s);
+        default: return launch_bk1_mixed(p, E, B, qdata, u, v, o.elems_per_block, jt, s);
     }
 }
 

@@ -20,7 +20,7 @@ DevCtx dev_ctx();              // status word and wait limit of the current devi
     int launch_bk5_##sfx(int p, long long E, const double* D, const void* G, const void* u, const void* mass,    \
                          double lambda, void* v, int F, int layout, int eb, int kernel, int gform, cudaStream_t s); \
     int launch_bk1_##sfx(int p, long long E, const double* B, const void* jxw, const void* u, void* v, int eb,   \
-                         cudaStream_t s);                                                                        \
+                         int jxw_t, cudaStream_t s);                                                             \
     int launch_bk3_##sfx(int p, long long E, const double* B, const double* D, const void* G, const void* k,     \
                          const void* u, void* v, int eb, int gform, cudaStream_t s);                                        \
     int bk5_sweep_##sfx##_L0(int p, int F, const double* D, long long E, const void* u, const void* G,  \

@@ -1121,7 +1121,7 @@ struct BK1Cfg {
 template <class Eng, int Q, int EB, bool EO = false>
 __global__ void __launch_bounds__(BK1Cfg<Eng, Q, EB>::NT)
     bk1_kernel(const __grid_constant__ P13<typename Eng::C, Q> prm, const long long E,
-               const typename Eng::S* __restrict__ u, const typename Eng::S* __restrict__ jxw,
+               const typename Eng::S* __restrict__ u, const typename Eng::S* __restrict__ jxw, const int jxw_t,
                typename Eng::S* __restrict__ v, const DevCtx ctx)
 {
     using Cfg = BK1Cfg<Eng, Q, EB>;
@@ -1188,9 +1188,16 @@ __global__ void __launch_bounds__(BK1Cfg<Eng, Q, EB>::NT)
             kline_pass<Eng, WB, Q, P>(W0, ne, tid, nt, [&](int e, int i, int j, const V (&x)[P], const BoxLine<WB, 2>& la) {
                 V y[Q], z[P];
                 eor_line<Eng, P, Q, +1>(x, y, prm.bi);
-                const S* jl = js + e * Q3 + (i * Q + j) * Q;
+                // point (i, j, o) of JxW(e,p,q,r), or of JxW_t(e,r,q,p)
+                if (jxw_t) {
+                    const S* jl = js + e * Q3 + j * Q + i;
 #pragma unroll
-                for (int o = 0; o < Q; ++o) y[o] = Eng::mul(y[o], Eng::load(jl[o]));
+                    for (int o = 0; o < Q; ++o) y[o] = Eng::mul(y[o], Eng::load(jl[o * Q * Q]));
+                } else {
+                    const S* jl = js + e * Q3 + (i * Q + j) * Q;
+#pragma unroll
+                    for (int o = 0; o < Q; ++o) y[o] = Eng::mul(y[o], Eng::load(jl[o]));
+                }
                 eor_line<Eng, Q, P, +1>(y, z, prm.bb);
 #pragma unroll
                 for (int o = 0; o < P; ++o) W0[la(o)] = z[o];
@@ -1221,7 +1228,8 @@ __global__ void __launch_bounds__(BK1Cfg<Eng, Q, EB>::NT)
                 const int x = w - e * Q3;
                 const int i = x / (Q * Q), j = (x / Q) % Q, k = x % Q;
                 const int wi = e * WB::size + WB::at(i, j, k);
-                W1[wi] = Eng::mul(W1[wi], Eng::load(js[e * Q3 + x]));
+                const int jx = jxw_t ? (k * Q + j) * Q + i : x;
+                W1[wi] = Eng::mul(W1[wi], Eng::load(js[e * Q3 + jx]));
             }
             __syncthreads();
             if (bt + gridDim.x < nbatch) issue(bt + gridDim.x);   // the stage is free

@@ -211,7 +211,7 @@ int bk5col_f(int F, int eb, const double* D, long long E, const void* u, const v
 
 #if BK_OP_TU == 1
 template <int Q, int EB>
-int bk1_q(const double* B, long long E, const void* jxw, const void* u, void* v, cudaStream_t s)
+int bk1_q(const double* B, long long E, const void* jxw, const void* u, void* v, int jxw_t, cudaStream_t s)
 {
     using Cfg = BK1Cfg<Eng, Q, EB>;
     using S = typename Eng::S;
@@ -227,7 +227,7 @@ int bk1_q(const double* B, long long E, const void* jxw, const void* u, void* v,
     const int occ = eo ? prepare<EoTag<Cfg, true>>(kern, Cfg::SMEM, Cfg::NT) : prepare<Cfg>(kern, Cfg::SMEM, Cfg::NT);
     if (occ <= 0) return BK_ERR_CUDA;
     const int grid = grid_for((E + EB - 1) / EB, occ);
-    kern<<<grid, Cfg::NT, Cfg::SMEM, s>>>(prm, E, static_cast<const S*>(u), static_cast<const S*>(jxw),
+    kern<<<grid, Cfg::NT, Cfg::SMEM, s>>>(prm, E, static_cast<const S*>(u), static_cast<const S*>(jxw), jxw_t,
                                           static_cast<S*>(v), dev_ctx());
     return cudaGetLastError() == cudaSuccess ? BK_OK : BK_ERR_CUDA;
 }
@@ -381,18 +381,18 @@ int BK_CAT3(bk5_col, BK_SFX, BK_LAYOUT_TU)(int p, int F, int eb, const double* D
 constexpr int bk1_eb(int q) { return (q == 5 && !eng_is_ff() && !eng_is_dfma()) ? 5 : default_eb(q); }
 
 int BK_CAT(launch_bk1, BK_SFX)(int p, long long E, const double* B, const void* jxw, const void* u, void* v,
-                                int eb, cudaStream_t s)
+                                int eb, int jxw_t, cudaStream_t s)
 {
     (void)eb;
     switch (p + 2) {
-        case 3: return bk1_q<3, default_eb(3)>(B, E, jxw, u, v, s);
-        case 4: return bk1_q<4, default_eb(4)>(B, E, jxw, u, v, s);
-        case 5: return bk1_q<5, bk1_eb(5)>(B, E, jxw, u, v, s);
-        case 6: return bk1_q<6, default_eb(6)>(B, E, jxw, u, v, s);
-        case 7: return bk1_q<7, default_eb(7)>(B, E, jxw, u, v, s);
-        case 8: return bk1_q<8, default_eb(8)>(B, E, jxw, u, v, s);
-        case 9: return bk1_q<9, default_eb(9)>(B, E, jxw, u, v, s);
-        case 10: return bk1_q<10, default_eb(10)>(B, E, jxw, u, v, s);
+        case 3: return bk1_q<3, default_eb(3)>(B, E, jxw, u, v, jxw_t, s);
+        case 4: return bk1_q<4, default_eb(4)>(B, E, jxw, u, v, jxw_t, s);
+        case 5: return bk1_q<5, bk1_eb(5)>(B, E, jxw, u, v, jxw_t, s);
+        case 6: return bk1_q<6, default_eb(6)>(B, E, jxw, u, v, jxw_t, s);
+        case 7: return bk1_q<7, default_eb(7)>(B, E, jxw, u, v, jxw_t, s);
+        case 8: return bk1_q<8, default_eb(8)>(B, E, jxw, u, v, jxw_t, s);
+        case 9: return bk1_q<9, default_eb(9)>(B, E, jxw, u, v, jxw_t, s);
+        case 10: return bk1_q<10, default_eb(10)>(B, E, jxw, u, v, jxw_t, s);
         default: return BK_ERR_ORDER;
     }
 }

@@ -121,6 +121,28 @@ __global__ void g_to_ff_kernel(const double* G, bkg::ff2* out, long long n)
     }
 }
 
+// transpose_jxw on the device: one block per element (grid-stride), the
+// element's JxW(p, q, r) staged in shared memory with coalesced loads,
+// JxW_t(r, q, p) written with coalesced stores.
+template <class T>
+__global__ void transpose_jxw_kernel(const T* __restrict__ jxw, T* __restrict__ jt, long long E, int q)
+{
+    extern __shared__ __align__(16) unsigned char sm[];
+    T* s = reinterpret_cast<T*>(sm);
+    const int q2 = q * q, q3 = q2 * q;
+    for (long long e = blockIdx.x; e < E; e += gridDim.x) {
+        const T* src = jxw + e * q3;
+        for (int x = threadIdx.x; x < q3; x += blockDim.x) s[x] = src[x];
+        __syncthreads();
+        T* dst = jt + e * q3;
+        for (int y = threadIdx.x; y < q3; y += blockDim.x) {
+            const int r = y / q2, qq = (y / q) % q, pp = y % q;   // y = (r, q, p)
+            dst[y] = s[(pp * q + qq) * q + r];
+        }
+        __syncthreads();
+    }
+}
+
 // make_bk5_G on the device: one block per element (grid-stride), the
 // element's six interleaved factors G6i(i, j, s, k) staged in shared memory
 // with coalesced loads, the F factors of the target layout written with
@@ -267,6 +289,31 @@ int bk5_make_g(int p, int64_t E, const void* G6i, void* G, int nfactors, int lay
     else
         make_g_kernel<float><<<grid, 256, 6 * q * q * q * sizeof(float), s>>>(
             static_cast<const float*>(G6i), static_cast<float*>(G), E, q, nfactors, layout);
+    return ok();
+}
+
+int bk1_transpose_jxw(int p, int64_t E, const void* jxw, void* jxw_t, int prec, bk_stream_t stream)
+{
+    if (p < 1 || p > 8) return BK_ERR_ORDER;
+    if (E < 0) return BK_ERR_SIZE;
+    if (prec != BK_PREC_FP64 && prec != BK_PREC_FP32 && prec != BK_PREC_MIXED) return BK_ERR_PREC;
+    if (E == 0) return BK_OK;
+    if (!jxw || !jxw_t) return BK_ERR_NULL;
+    if ((reinterpret_cast<uintptr_t>(jxw) | reinterpret_cast<uintptr_t>(jxw_t)) & 15) return BK_ERR_ALIGN;
+    if (jxw == jxw_t) return BK_ERR_ARG;
+    const int q = p + 2;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long cap = 8LL * sms;
+    const int grid = int(E < cap ? E : cap);
+    if (prec == BK_PREC_FP64)
+        transpose_jxw_kernel<double><<<grid, 256, q * q * q * sizeof(double), s>>>(
+            static_cast<const double*>(jxw), static_cast<double*>(jxw_t), E, q);
+    else
+        transpose_jxw_kernel<float><<<grid, 256, q * q * q * sizeof(float), s>>>(
+            static_cast<const float*>(jxw), static_cast<float*>(jxw_t), E, q);
     return ok();
 }
 

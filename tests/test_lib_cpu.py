@@ -82,6 +82,15 @@ def test_host_argument_errors(bklib):
     assert L.bk5_make_g(3, 4, None, a16, 6, 2, 0, None) == bklib.BK_ERR_NULL
     assert L.bk5_make_g(3, 4, a16, a8, 9, 0, 0, None) == bklib.BK_ERR_ALIGN
     assert L.bk5_make_g(3, 0, None, None, 6, 2, 0, None) == bklib.BK_OK
+    # BK1 qdata layouts: PQR or RQP; the device transpose_jxw
+    o = bklib.ApplyOptions(jxw_layout=2).c()
+    assert L.bk1_apply_opt(3, 4, dp, a16, a16, a16, C.byref(o), None) == bklib.BK_ERR_ARG
+    assert L.bk1_transpose_jxw(9, 4, a16, a16, 0, None) == bklib.BK_ERR_ORDER
+    assert L.bk1_transpose_jxw(3, -1, a16, a16, 0, None) == bklib.BK_ERR_SIZE
+    assert L.bk1_transpose_jxw(3, 4, a16, a16, 9, None) == bklib.BK_ERR_PREC
+    assert L.bk1_transpose_jxw(3, 4, None, a16, 0, None) == bklib.BK_ERR_NULL
+    assert L.bk1_transpose_jxw(3, 4, a16, a8, 0, None) == bklib.BK_ERR_ALIGN
+    assert L.bk1_transpose_jxw(3, 0, None, None, 0, None) == bklib.BK_OK
     # E = 0 is a no-op, even with null device pointers
     assert L.bk5_apply(3, 0, dp, None, None, None, 0, None) == bklib.BK_OK
     assert L.bk1_apply(8, 0, dp, None, None, None, 0, None) == bklib.BK_OK

@@ -403,3 +403,48 @@ def test_bk5_make_g_feeds_the_apply(bklib):
             bklib.bk5_apply(p, E, D, G, dev(u, "f64"), v, layout=layout, nfactors=nf)
             torch.cuda.synchronize()
             assert oracle.rel_maxdiff(host(v), ref) < TOL64, (nf, layout)
+
+
+@pytest.mark.parametrize("p", [1, 2, 3, 5, 8])
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_bk1_transpose_jxw_matches_oracle(bklib, p, prec):
+    """The device transpose_jxw is bitwise the oracle's restatement of
+    include/bk_harness.h:89-102 (JxW(e,p,q,r) -> JxW_t(e,r,q,p))."""
+    E = 7
+    q = p + 2
+    jxw = np.random.default_rng(700 + p).uniform(0.5, 1.5, E * q ** 3)
+    if prec == "f32":
+        jxw = jxw.astype(np.float32).astype(np.float64)
+    out = bklib.bk1_transpose_jxw(p, E, dev(jxw, prec))
+    torch.cuda.synchronize()
+    assert np.array_equal(host(out), oracle.transpose_jxw(jxw, E, q))
+
+
+@pytest.mark.parametrize("p", [1, 3, 4, 6, 8])
+@pytest.mark.parametrize("prec", [0, 1, 2])
+@pytest.mark.parametrize("basis", ["gll", "test"])
+def test_bk1_transposed_jxw_apply(bklib, p, prec, basis):
+    """BK1 on JxW_t(e,r,q,p) (jxw_layout RQP, the layout of the SYCL BK1
+    variants, sycl/bk1_sycl.cpp:74-98) gives bitwise the apply on JxW(e,p,q,r)
+    for every engine, on the even-odd (GLL/Gauss) and the plain (test basis)
+    paths, and agrees with the oracle."""
+    E = 37
+    q, P = p + 2, p + 1
+    if basis == "gll":
+        B = bklib.bk1_bk3_matrices(p)[0]
+    else:
+        B = oracle.test_basis(P, q)
+    rng = np.random.default_rng(40 + p)
+    u = rng.uniform(-1, 1, E * P ** 3)
+    jxw = rng.uniform(0.5, 1.5, E * q ** 3)
+    dt = "f64" if prec == bklib.PREC_FP64 else "f32"
+    du, dj = dev(u, dt), dev(jxw, dt)
+    djt = bklib.bk1_transpose_jxw(p, E, dj)
+    v0 = torch.full_like(du, float("nan"))
+    v1 = torch.full_like(du, float("nan"))
+    bklib.bk1_apply(p, E, B, dj, du, v0, prec=prec)
+    bklib.bk1_apply(p, E, B, djt, du, v1, prec=prec, jxw_layout=bklib.JXW_RQP)
+    torch.cuda.synchronize()
+    assert torch.equal(v0, v1)
+    tol = TOL64 if prec == bklib.PREC_FP64 else 1e-5
+    assert oracle.rel_maxdiff(host(v1), oracle.bk1(q, E, B, jxw, u)) < tol
