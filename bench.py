@@ -585,8 +585,8 @@ def run_helmholtz(args):
     orders = hz.config_orders()
     if args.elements:
         orders = [(p, max(1, (2 ** (8 - p)) * args.elements // 64)) for p, _ in orders]
-    best = tune.tune(orders)
-    plan = hz.HelmholtzPlan([(p, E, best[p]) for p, E in orders])
+    tuned = tune.tune(orders)
+    plan = tune.make_plan(orders, tuned)
     G, M = plan.geometry(seed=11)
     G32, M32 = G.float(), M.float()
     ustar = bk.fill_uniform(torch.empty(plan.n, dtype=torch.float64, device="cuda"), 5)
@@ -630,9 +630,8 @@ def run_helmholtz(args):
     m_per32 = _events_ms(lambda: per_order(bk.PREC_MIXED, G32, M32, u32, v32), steps, warm, torch, graph=True) \
         if aligned32 else None
     # the column body of the same launch (tiles tuned for it)
-    best_col = tune.tune(orders, kernel=bk.KERNEL_COLUMN)
-    plan_col = hz.HelmholtzPlan([(p, E, best_col[p]) for p, E in orders])
-    plan_col.set_kernel(bk.KERNEL_COLUMN)
+    tuned_col = tune.tune(orders, kernel=bk.KERNEL_COLUMN)
+    plan_col = tune.make_plan(orders, tuned_col, kernel=bk.KERNEL_COLUMN)
     m_col = _events_ms(lambda: plan_col.apply(G32, M32, 1.0, u32, v32, prec=bk.PREC_MIXED), steps, warm, torch,
                        graph=True)
     plan_col.close()
@@ -654,10 +653,11 @@ def run_helmholtz(args):
             "gdofs": plan.n / m_multi / 1e6, "ms_per_apply": m_multi, "dtype": "f32",
             "hbm_frac": 36 * plan.n / m_multi / 1e6 / measured_peak()[0],
             "rel_max_err_vs_oracle_fp64_apply": errs, "oracle_elements_per_order": 64,
-            "dofs": plan.n, "tiles": plan.ntiles, "tile_elems": best,
+            "dofs": plan.n, "tiles": plan.ntiles,
+            "tuned": {k: tuned.get(k) for k in ("block", "gstage", "tiles", "evaluated", "starts_ms")},
             "kernel": {bk.KERNEL_SWEEP: "sweep (even-odd)", bk.KERNEL_COLUMN: "column"}[plan.kernel],
             "multi_mixed_gdofs": plan.n / m_multi / 1e6, "multi_fp64_gdofs": plan.n / m_multi64 / 1e6,
-            "multi_mixed_column_gdofs": plan.n / m_col / 1e6, "tile_elems_column": best_col,
+            "multi_mixed_column_gdofs": plan.n / m_col / 1e6, "tile_elems_column": tuned_col["tiles"],
             "per_order_mixed_gdofs": (plan.n / m_per32 / 1e6) if m_per32 else None,
             "per_order_fp64_gdofs": (plan.n / m_per64 / 1e6) if m_per64 else None,
             "cg": st, "cg_seconds": solve_s, "solution_rel_err": err,

@@ -23,7 +23,8 @@ typedef struct bk_order_range {
     int p;               /* polynomial order, 2..8 (q = p + 1 points) */
     int64_t E;           /* elements of this order */
     int elems_per_tile;  /* elements per tile of the persistent launch, with
-                            elems_per_tile * q^2 <= 256; 0: about 128 / q^2 */
+                            elems_per_tile * q^2 <= 1024 (the column body:
+                            <= 256, one thread per column); 0: about 128 / q^2 */
 } bk_order_range;
 
 typedef struct bk_hplan* bk_hplan_t;
@@ -36,7 +37,10 @@ int bk_hplan_create(bk_hplan_t* plan, int norders, const bk_order_range* orders,
                     bk_stream_t stream);
 int bk_hplan_destroy(bk_hplan_t plan);
 /* what = 0: values of a vector (sum E_p q^3); 1: values of G; 2: tiles;
- * 3: the kernel shape of the applies (BK_KERNEL_SWEEP or BK_KERNEL_COLUMN). */
+ * 3: the kernel shape of the applies (BK_KERNEL_SWEEP or BK_KERNEL_COLUMN);
+ * 4, 5: shared memory per block of the sweep body's launch for FP64 / FP32
+ * storage (a launch needs at most 232448 bytes); 6, 7: the threads and G
+ * staging set by bk_hplan_set_shape. */
 long long bk_hplan_size(bk_hplan_t plan, int what);
 
 /* The body of the persistent launch: BK_KERNEL_SWEEP (line sweeps in the
@@ -45,6 +49,17 @@ long long bk_hplan_size(bk_hplan_t plan, int what);
  * thread per k-column, any D) or BK_KERNEL_AUTO (SWEEP when possible: the
  * default of a new plan). */
 int bk_hplan_set_kernel(bk_hplan_t plan, int kernel);
+
+/* The shape of the even-odd sweep body's persistent launch.  threads: per
+ * block, a multiple of 32 in 64..256, or 0 (the default) for the largest
+ * tile's lines (elements x q^2, at most 256); tiles with more lines than
+ * threads loop over their lines, so tile sizes per order and the block are
+ * chosen apart.  The FP64 launch runs three thread groups of that size (one
+ * per direction).  gstage (FP32 storage): 1 stages each tile's G into shared
+ * memory by TMA, 0 (the default) reads it in the pointwise stage straight
+ * from global memory, prefetched into L2 one tile ahead.  omp_bk_gb300.tune
+ * chooses both by measurement.  BK_ERR_ARG for other values. */
+int bk_hplan_set_shape(bk_hplan_t plan, int threads, int gstage);
 
 /* v = A u for all orders in ONE persistent launch.  prec BK_PREC_FP64 (engine
  * AUTO/FF: float-float, DFMA: native), BK_PREC_MIXED or BK_PREC_FP32 (float

@@ -209,6 +209,8 @@ struct PMultiEO {
     EOSet<C> eo;
     MultiSeg seg[kMultiNQ];
     int nseg;
+    int block;      // threads per block (0: the largest tile's lines)
+    int gstage;     // FP32 storage: G staged by TMA (1) or read from global memory (0)
     long long n;    // values of u, v and mass over all segments
     long long ng;   // values of G over all segments
 };
@@ -239,11 +241,22 @@ inline int multi_wbox_bytes(int q, int eb, int vbytes)
     return eb * bk5_box(q, vbytes, 2) * vbytes;   // the element stride of WBox5
 }
 
-// Shared memory of the even-odd launch: u stage (followed by the mass stage,
-// of the same size), G stage (FP64 forms only), three work boxes (each the
-// largest tile's), one mbarrier.
+// Stage buffers of u and the mass of the even-odd launch: two for FP32
+// storage (the next tile's copies go into one while the current tile reads
+// the other), one for FP64 storage (whose G stage takes the room).
 template <class Eng>
-inline void multi_eo_smem(const MultiSeg* seg, int nseg, int& u_bytes, int& g_bytes, int& w_bytes, int& total)
+constexpr int multi_eo_nbuf()
+{
+    return sizeof(typename Eng::S) == 4 ? 2 : 1;
+}
+
+// Shared memory of the even-odd launch: per stage buffer a u stage followed
+// by the mass stage (of the same size), the G stage (FP64, and FP32 with G
+// staged), three work boxes (four with direction-parallel groups; each the
+// largest tile's), one mbarrier per stage buffer.
+template <class Eng>
+inline void multi_eo_smem(const MultiSeg* seg, int nseg, int& u_bytes, int& g_bytes, int& w_bytes, int& total,
+                          int dpar = 0, bool gst = false)
 {
     using S = typename Eng::S;
     using V = typename Eng::V;
@@ -252,19 +265,37 @@ inline void multi_eo_smem(const MultiSeg* seg, int nseg, int& u_bytes, int& g_by
     w_bytes = 16;
     for (int s = 0; s < nseg; ++s) {
         const int q = seg[s].q, eb = seg[s].eb, q3 = q * q * q;
-        // FP32 storage: G is read straight from HBM (no G stage)
-        const int ub = stage_bytes<S>(eb * q3), gb = (sizeof(S) == 4) ? 16 : stage_bytes<S>(eb * 6 * q3);
+        // FP32 storage: G read straight from global memory unless staged
+        const int ub = stage_bytes<S>(eb * q3), gb = (sizeof(S) == 4 && !gst) ? 16 : stage_bytes<S>(eb * 6 * q3);
         const int wb = (multi_wbox_bytes(q, eb, int(sizeof(V))) + 15) / 16 * 16;
         u_bytes = ub > u_bytes ? ub : u_bytes;
         g_bytes = gb > g_bytes ? gb : g_bytes;
         w_bytes = wb > w_bytes ? wb : w_bytes;
     }
-    total = 2 * u_bytes + g_bytes + 3 * w_bytes + 16;
+    total = multi_eo_nbuf<Eng>() * 2 * u_bytes + g_bytes + (dpar ? 4 : 3) * w_bytes + 16;
 }
 
 // DOT: also sum u . v over the launch, one partial per block in dot_part
-// (the CG's p . A p), from compensated per-thread sums.
-template <class Eng, int NT, int MINB, bool DOT = false>
+// (the CG's p . A p), from compensated per-thread sums.  DPAR = 2: the block
+// is three thread groups that run the three gradient sweeps, and then the
+// three transposed ones, at the same time (one shared code body, a fourth
+// work box), as the single-order float-float kernels do.  GST (FP32
+// storage): G staged by TMA instead of read straight from global memory; the
+// tuner picks the faster for a plan.
+//
+// Staging, by mode:
+//   FP32, G direct:  u and mass double-buffered; at the top of tile t the
+//                    next tile's u and mass go into the other buffer (its
+//                    barrier gets the bytes and the arrival) and its G is
+//                    prefetched into L2 (one bulk prefetch), so the pointwise
+//                    stage's loads wait on L2 rather than HBM.
+//   FP32, G staged:  the same, but the arrival on the other buffer's barrier
+//                    comes with the next tile's G, issued into the single G
+//                    stage after tile t's pointwise stage.
+//   FP64:            one buffer; the next tile's G after the pointwise stage
+//                    (bytes only), its u and mass after the last pass (the
+//                    arrival), as the single-order kernels do.
+template <class Eng, int NT, int MINB, bool DOT = false, int DPAR = 0, bool GST = false>
 __global__ void __launch_bounds__(NT, MINB)
     bk5_multi_eo_kernel(const __grid_constant__ PMultiEO<typename Eng::C> prm, const MultiTile* __restrict__ tiles,
                         const int ntiles, const typename Eng::S* __restrict__ u, const typename Eng::S* __restrict__ G,
@@ -274,80 +305,128 @@ __global__ void __launch_bounds__(NT, MINB)
 {
     using S = typename Eng::S;
     using V = typename Eng::V;
-    // FP32 storage: the pointwise stage reads G straight from HBM (coalesced:
-    // G's column layout walks with the points), which leaves the largest
-    // stage out of shared memory and more blocks per SM; the FP64 forms stage it
-    constexpr bool GD = sizeof(S) == 4;
+    constexpr int NB = multi_eo_nbuf<Eng>();
+    constexpr bool GD = NB == 2 && !GST;   // FP32, G read straight from global memory
+    constexpr bool GS2 = NB == 2 && GST;   // FP32, G staged
+    static_assert(NB == 2 || !GST, "FP64 storage always stages G");
     extern __shared__ __align__(16) unsigned char smem[];
-    unsigned char* ustage = smem;
-    unsigned char* mstage = smem + u_bytes;
-    unsigned char* gstage = mstage + u_bytes;
+    // [u 0][mass 0]([u 1][mass 1]) [G] [W0][W1][W2]([W3]) [barrier per buffer]
+    unsigned char* gstage = smem + NB * 2 * u_bytes;
     V* W0 = reinterpret_cast<V*>(gstage + g_bytes);
     V* W1 = reinterpret_cast<V*>(reinterpret_cast<unsigned char*>(W0) + w_bytes);
     V* W2 = reinterpret_cast<V*>(reinterpret_cast<unsigned char*>(W1) + w_bytes);
-    uint64_t* bar = reinterpret_cast<uint64_t*>(reinterpret_cast<unsigned char*>(W2) + w_bytes);
+    V* W3 = DPAR ? reinterpret_cast<V*>(reinterpret_cast<unsigned char*>(W2) + w_bytes) : nullptr;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(reinterpret_cast<unsigned char*>(W2) + (DPAR ? 2 : 1) * w_bytes);
     const int tid = threadIdx.x;
-    const int nt = blockDim.x;   // the largest tile's lines, at most NT
+    const int nt = blockDim.x;   // the plan's block: tiles with more lines loop
     if (tid == 0) {
-        mbar_init(bar, 1);
+        for (int b = 0; b < NB; ++b) mbar_init(&bars[b], 1);
         fence_mbar_init();
     }
     __syncthreads();
     ffacc dacc = acc_zero();   // u . A u over the thread's points (DOT)
-    // where the staged tile's u, G and mass landed
-    const S* us = nullptr;
-    const S* gs = nullptr;
-    const S* ms = nullptr;
-    // G of tile t (thread 0 adds its bytes to the phase without arriving),
-    // then u and the mass diagonal (thread 0 arrives): the next tile's G is
-    // copied while the current tile finishes its transposed sweeps, u and the
-    // mass (read by the last pass) right after
-    auto issue_g = [&](int t) {
-        if constexpr (GD) return;
-        const MultiTile tl = tiles[t];
+    // The stages of a tile are found from its descriptor (stage_at), so no
+    // stage pointers stay live across tiles.
+    auto g_src = [&](const MultiTile& tl) {
         const MultiSeg& sg = prm.seg[tl.seg];
-        const int q3 = sg.q * sg.q * sg.q;
-        uint32_t tx = 0;
-        if (tid == 0) fence_proxy_async();
-        gs = stage_issue<S>(gstage, G + sg.goff + tl.e_first * 6 * q3, tl.ne * 6 * q3, G + prm.ng, bar, tx, tid, nt);
-        if (tid == 0) mbar_expect_tx(bar, tx);
+        return G + sg.goff + tl.e_first * 6 * sg.q * sg.q * sg.q;
     };
-    auto issue_um = [&](int t) {
+    auto prefetch_g = [&](int t) {
+        if (tid != 0) return;
+        const MultiTile tl = tiles[t];
+        const int q = prm.seg[tl.seg].q;
+        prefetch_l2(g_src(tl), size_t(tl.ne) * 6 * q * q * q * sizeof(S), G + prm.ng);
+    };
+    // G of tile t into the G stage, counted on bars[b], with the arrival
+    // (FP32 staged) or bytes only (FP64: the arrival follows with u)
+    auto issue_g = [&](int t, int b, bool arrive) {
+        const MultiTile tl = tiles[t];
+        const int q = prm.seg[tl.seg].q;
+        uint32_t tx = 0;
+        if (tid == 0) fence_proxy_async();
+        stage_issue<S>(gstage, g_src(tl), tl.ne * 6 * q * q * q, G + prm.ng, &bars[b], tx, tid, nt);
+        if (tid == 0) {
+            if (arrive)
+                mbar_arrive_expect_tx(&bars[b], tx);
+            else
+                mbar_expect_tx(&bars[b], tx);
+        }
+    };
+    // u and the mass diagonal of tile t into stage buffer b
+    auto issue_um = [&](int t, int b, bool arrive) {
         const MultiTile tl = tiles[t];
         const MultiSeg& sg = prm.seg[tl.seg];
         const int q3 = sg.q * sg.q * sg.q;
+        unsigned char* ust = smem + b * 2 * u_bytes;
         uint32_t tx = 0;
         if (tid == 0) fence_proxy_async();
-        us = stage_issue<S>(ustage, u + sg.uoff + tl.e_first * q3, tl.ne * q3, u + prm.n, bar, tx, tid, nt);
-        ms = (mass != nullptr)
-                 ? stage_issue<S>(mstage, mass + sg.uoff + tl.e_first * q3, tl.ne * q3, mass + prm.n, bar, tx, tid, nt)
-                 : nullptr;
-        if (tid == 0) mbar_arrive_expect_tx(bar, tx);
+        stage_issue<S>(ust, u + sg.uoff + tl.e_first * q3, tl.ne * q3, u + prm.n, &bars[b], tx, tid, nt);
+        if (mass != nullptr)
+            stage_issue<S>(ust + u_bytes, mass + sg.uoff + tl.e_first * q3, tl.ne * q3, mass + prm.n, &bars[b], tx,
+                           tid, nt);
+        if (tid == 0) {
+            if (arrive)
+                mbar_arrive_expect_tx(&bars[b], tx);
+            else
+                mbar_expect_tx(&bars[b], tx);
+        }
     };
     if (blockIdx.x < ntiles) {
-        issue_g(blockIdx.x);
-        issue_um(blockIdx.x);
+        if constexpr (GD) {
+            prefetch_g(blockIdx.x);
+            issue_um(blockIdx.x, 0, true);
+        } else if constexpr (GS2) {
+            issue_um(blockIdx.x, 0, false);
+            issue_g(blockIdx.x, 0, true);
+        } else {
+            issue_g(blockIdx.x, 0, false);
+            issue_um(blockIdx.x, 0, true);
+        }
     }
-    uint32_t phase = 0;
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, phase ^= 1u) {
-        if (batch_wait_failed(bar, phase, ctx, tid)) return;
+    int it = 0;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++it) {
+        const int b = (NB == 2) ? (it & 1) : 0;
+        const uint32_t parity = (NB == 2) ? uint32_t((it >> 1) & 1) : uint32_t(it & 1);
+        const int tn = t + gridDim.x;
+        if constexpr (NB == 2) {
+            // the other buffer was last read by the previous tile, which
+            // ended with a block barrier: the next tile's u and mass go there
+            // now, so that they land while this tile computes
+            if (tn < ntiles) {
+                if constexpr (GD) prefetch_g(tn);
+                issue_um(tn, b ^ 1, GD);
+            }
+        }
+        if (batch_wait_failed(&bars[b], parity, ctx, tid)) {
+            if (NB == 2 && tn < ntiles) {
+                // the next tile's copies into the other buffer may be in
+                // flight: complete its phase's arrival (G staged: still owed)
+                // and wait for them before the block leaves
+                if (GS2 && tid == 0) mbar_arrive(&bars[b ^ 1]);
+                mbar_wait_bounded(&bars[b ^ 1], uint32_t(((it + 1) >> 1) & 1), ctx.wait_limit);
+            }
+            return;
+        }
         const MultiTile tl = tiles[t];
         const MultiSeg& sg = prm.seg[tl.seg];
         const int q = sg.q;
         const int q3 = q * q * q;
-        const int tn = t + gridDim.x;
         S* vb = v + sg.uoff + tl.e_first * q3;
-        const S* ub = us;
-        const S* gb = GD ? G + sg.goff + tl.e_first * 6 * q3 : gs;
-        const S* mb = ms;
+        const unsigned char* ust = smem + b * 2 * u_bytes;
+        const S* ub = stage_at<S>(ust, u + sg.uoff + tl.e_first * q3);
+        const S* gb = GD ? g_src(tl) : stage_at<S>(gstage, g_src(tl));
+        const S* mb = (mass != nullptr) ? stage_at<S>(ust + u_bytes, mass + sg.uoff + tl.e_first * q3) : nullptr;
+        // after the pointwise stage the G stage is free for the next tile's G
         auto early = [&]() {
-            if (tn < ntiles) issue_g(tn);
+            if constexpr (!GD) {
+                if (tn < ntiles) issue_g(tn, NB == 2 ? (b ^ 1) : 0, NB == 2);
+            }
         };
         switch (q) {
 #define BK_MULTI_EO_CASE(QQ)                                                                                    \
     case QQ:                                                                                                    \
-        bk5_sweep_batch<Eng, QQ, 6, 2, true, 0, decltype(early), DOT>(                                         \
-            nullptr, prm.eo.template at<QQ>().eo, prm.eo.template at<QQ>().eot, ub, gb, W0, W1, W2, nullptr,    \
+        bk5_sweep_batch<Eng, QQ, 6, 2, true, DPAR, decltype(early), DOT>(                                      \
+            nullptr, prm.eo.template at<QQ>().eo, prm.eo.template at<QQ>().eot, ub, gb, W0, W1, W2, W3,         \
             tl.ne, tid, nt, vb, mb, lambda, &dacc, early);                                                      \
         break;
             BK_MULTI_EO_CASE(3)
@@ -361,7 +440,8 @@ __global__ void __launch_bounds__(NT, MINB)
             default:
                 break;
         }
-        if (tn < ntiles) issue_um(tn);
+        // FP64: the single buffer is free after the tile's last pass
+        if (NB == 1 && tn < ntiles) issue_um(tn, 0, true);
     }
     if constexpr (DOT) {
         // block sum of the threads' partial dot products, one value per block

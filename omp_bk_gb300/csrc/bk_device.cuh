@@ -130,4 +130,24 @@ __device__ __forceinline__ void tma_store_wait_all()
 
 __device__ __forceinline__ bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
+// One arrival on the barrier (no transaction bytes).
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// A hint: brings [p, p + bytes) into L2 by one bulk prefetch (no shared
+// memory, no completion to wait for).  The range is widened to 16-byte
+// boundaries but never past `end` rounded down, so it stays inside the array
+// p points into (whose start is 16-byte aligned).
+__device__ __forceinline__ void prefetch_l2(const void* p, size_t bytes, const void* end)
+{
+    const uintptr_t a = reinterpret_cast<uintptr_t>(p) & ~uintptr_t(15);
+    uintptr_t b = (reinterpret_cast<uintptr_t>(p) + bytes + 15) & ~uintptr_t(15);
+    const uintptr_t cap = reinterpret_cast<uintptr_t>(end) & ~uintptr_t(15);
+    if (b > cap) b = cap;
+    if (b > a)
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "r"(uint32_t(b - a)) : "memory");
+}
+
 }  // namespace bkg

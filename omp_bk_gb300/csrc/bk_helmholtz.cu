@@ -33,7 +33,8 @@
 namespace bkg {
 namespace {
 
-constexpr int kNT = 256;   // threads per block of the persistent kernel
+constexpr int kNT = 256;   // threads per block of the persistent kernel (per thread group), at most
+constexpr int kMaxTileLines = 1024;   // lines (elements x q^2) of a tile, at most
 constexpr int kRedBlocks = 1216;   // 8 blocks of 256 threads per SM
 constexpr int kMaxDotParts = 4864;  // blocks of the persistent launch at most (32 per SM)
 constexpr int kRedThreads = 256;
@@ -98,28 +99,32 @@ struct MultiLaunch {
 };
 
 // The even-odd sweep launch: blockDim = the largest tile's lines (eb q^2),
-// rounded up to whole warps; MAXT threads at most, MINB blocks per SM asked
-// of the register allocator.
-template <class Eng, int MAXT, int MINB, bool DOT = false>
+// rounded up to whole warps, or the plan's block size when that is smaller
+// (the sweeps of a tile with more lines than threads loop over them); three
+// times that with direction-parallel groups (DPAR); MAXT threads at most,
+// MINB blocks per SM asked of the register allocator.  GST: FP32 G staged.
+template <class Eng, int MAXT, int MINB, bool DOT = false, int DPAR = 0, bool GST = false>
 struct MultiEOLaunch {
-    static int threads(const MultiSeg* seg, int nseg)
+    static int threads(const MultiSeg* seg, int nseg, int block)
     {
         int nt = 64;
         for (int s = 0; s < nseg; ++s) {
             const int l = (seg[s].eb * seg[s].q * seg[s].q + 31) / 32 * 32;
             nt = l > nt ? l : nt;
         }
-        return nt;
+        if (block > 0 && nt > block) nt = block;
+        if (DPAR) nt *= 3;
+        return nt > MAXT ? MAXT : nt;
     }
     static int smem(const PMultiEO<typename Eng::C>& prm, int& ub, int& gb, int& wb)
     {
         int total = 0;
-        multi_eo_smem<Eng>(prm.seg, prm.nseg, ub, gb, wb, total);
+        multi_eo_smem<Eng>(prm.seg, prm.nseg, ub, gb, wb, total, DPAR, GST);
         return total;
     }
     static int prepare(int total, int nt)
     {
-        auto kern = bk5_multi_eo_kernel<Eng, MAXT, MINB, DOT>;
+        auto kern = bk5_multi_eo_kernel<Eng, MAXT, MINB, DOT, DPAR, GST>;
         static int set[kMaxDevices] = {0};
         static int occ_of[kMaxDevices][3] = {{0, 0, 0}};
         const int dev = current_device();
@@ -148,7 +153,7 @@ struct MultiEOLaunch {
         int ub = 0, gb = 0, wb = 0;
         const int total = smem(prm, ub, gb, wb);
         if (total > 232448) return 0;
-        return prepare(total, threads(prm.seg, prm.nseg));
+        return prepare(total, threads(prm.seg, prm.nseg, prm.block));
     }
     // dot_part (optional): one partial sum of u . v per block, their count in
     // *nparts
@@ -159,10 +164,10 @@ struct MultiEOLaunch {
         using S = typename Eng::S;
         int ub = 0, gb = 0, wb = 0;
         const int total = smem(prm, ub, gb, wb);
-        const int nt = threads(prm.seg, prm.nseg);
-        if (total > 232448 || nt > MAXT) return BK_ERR_ARG;
+        const int nt = threads(prm.seg, prm.nseg, prm.block);
+        if (total > 232448) return BK_ERR_ARG;
         if (DOT != (dot_part != nullptr)) return BK_ERR_ARG;
-        auto kern = bk5_multi_eo_kernel<Eng, MAXT, MINB, DOT>;
+        auto kern = bk5_multi_eo_kernel<Eng, MAXT, MINB, DOT, DPAR, GST>;
         const int occ = prepare(total, nt);
         if (occ < 1) return BK_ERR_CUDA;
         int grid = occ * sm_count();
@@ -176,6 +181,38 @@ struct MultiEOLaunch {
         return cudaGetLastError() == cudaSuccess ? BK_OK : BK_ERR_CUDA;
     }
 };
+
+// The float-float (FP64) launch: direction-parallel groups, three per block
+// of up to 3 x 256 threads (the groups' shared body needs few registers).
+using MultiFF = MultiEOLaunch<EngFF, 768, 1, false, 2>;
+
+// The FP32-storage launches with G read from global memory or staged (the
+// plan's gstage), with and without the fused dot product.
+template <class Eng, bool DOT = false>
+int run_f32(const PMultiEO<float>& prm, const MultiTile* tiles, int ntiles, const void* u, const void* G,
+            const void* mass, double lambda, void* v, cudaStream_t s, double* dot_part = nullptr, int* nparts = nullptr)
+{
+    if (prm.gstage)
+        return MultiEOLaunch<Eng, 256, 4, DOT, 0, true>::run(prm, tiles, ntiles, u, G, mass, lambda, v, s, dot_part,
+                                                             nparts);
+    return MultiEOLaunch<Eng, 256, 4, DOT, 0, false>::run(prm, tiles, ntiles, u, G, mass, lambda, v, s, dot_part,
+                                                          nparts);
+}
+
+template <class Eng, bool DOT = false>
+int prepare_f32(const PMultiEO<float>& prm)
+{
+    return prm.gstage ? MultiEOLaunch<Eng, 256, 4, DOT, 0, true>::prepare(prm)
+                      : MultiEOLaunch<Eng, 256, 4, DOT, 0, false>::prepare(prm);
+}
+
+template <class Eng>
+int smem_f32(const PMultiEO<float>& prm)
+{
+    int ub = 0, gb = 0, wb = 0;
+    return prm.gstage ? MultiEOLaunch<Eng, 256, 4, false, 0, true>::smem(prm, ub, gb, wb)
+                      : MultiEOLaunch<Eng, 256, 4, false, 0, false>::smem(prm, ub, gb, wb);
+}
 
 // ---- CG kernels --------------------------------------------------------------
 
@@ -488,10 +525,10 @@ int apply_plan(bk_hplan* h, int eng, const void* G, const void* mass, double lam
     if (h->kernel == BK_KERNEL_SWEEP) {
         switch (eng) {
             case 0: return MultiEOLaunch<EngDfma, 256, 2>::run(h->e_dfma, h->tiles, h->ntiles, u, G, mass, lambda, v, s);
-            case 1: return MultiEOLaunch<EngFF, 256, 2>::run(h->e_ff, h->tiles, h->ntiles, u, G, mass, lambda, v, s);
-            case 2: return MultiEOLaunch<EngF32, 256, 4>::run(h->e_f32, h->tiles, h->ntiles, u, G, mass, lambda, v, s);
+            case 1: return MultiFF::run(h->e_ff, h->tiles, h->ntiles, u, G, mass, lambda, v, s);
+            case 2: return run_f32<EngF32>(h->e_f32, h->tiles, h->ntiles, u, G, mass, lambda, v, s);
             default:
-                return MultiEOLaunch<EngMixed, 256, 4>::run(h->e_f32, h->tiles, h->ntiles, u, G, mass, lambda, v, s);
+                return run_f32<EngMixed>(h->e_f32, h->tiles, h->ntiles, u, G, mass, lambda, v, s);
         }
     }
     switch (eng) {
@@ -503,6 +540,15 @@ int apply_plan(bk_hplan* h, int eng, const void* G, const void* mass, double lam
 }
 
 int ck(cudaError_t e) { return e == cudaSuccess ? BK_OK : BK_ERR_CUDA; }
+
+// The column body has one thread per k-column of a tile: every tile's
+// columns (elements x q^2) must fit one block.
+bool column_fits(const bk_hplan& h)
+{
+    for (int s = 0; s < h.nseg; ++s)
+        if (h.seg[s].eb * h.seg[s].q * h.seg[s].q > kNT) return false;
+    return true;
+}
 
 void free_graph(bk_hplan* h)
 {
@@ -521,7 +567,7 @@ int build_inner_graph(bk_hplan* h, const void* G32, const void* mass32, double l
         // kernel attributes and occupancy outside the capture
         int st = 0, cb = 0;
         if (h->kernel == BK_KERNEL_SWEEP) {
-            if (MultiEOLaunch<EngMixed, 256, 4, true>::prepare(h->e_f32) < 1) return BK_ERR_CUDA;
+            if (prepare_f32<EngMixed, true>(h->e_f32) < 1) return BK_ERR_CUDA;
         } else if (MultiLaunch<EngMixed, 2>::prepare(MultiLaunch<EngMixed, 2>::smem(h->p_f32, st, cb)) < 1) {
             return BK_ERR_CUDA;
         }
@@ -593,8 +639,8 @@ int build_inner_graph(bk_hplan* h, const void* G32, const void* mass32, double l
                 if (h->kernel == BK_KERNEL_SWEEP) {
                     // p . Ap summed by the apply itself (one partial per block)
                     int nparts = 0;
-                    arc = MultiEOLaunch<EngMixed, 256, 4, true>::run(h->e_f32, h->tiles, h->ntiles, h->p32, G32, mass32,
-                                                                lambda, h->Ap32, s, h->part, &nparts);
+                    arc = run_f32<EngMixed, true>(h->e_f32, h->tiles, h->ntiles, h->p32, G32, mass32, lambda, h->Ap32,
+                                                  s, h->part, &nparts);
                     cg_pap_kernel<<<1, kRedThreads, 0, s>>>(h->part, nparts, h->sc);
                 } else {
                     arc = apply_plan(h, 3, G32, mass32, lambda, h->p32, h->Ap32, s);
@@ -648,7 +694,7 @@ int bk_hplan_create(bk_hplan_t* out, int norders, const bk_order_range* orders, 
         const int q = p + 1;
         int eb = orders[s].elems_per_tile;
         if (eb <= 0) eb = (q * q >= 100) ? 1 : ((q * q >= 64) ? 2 : (128 + q * q - 1) / (q * q));
-        if (eb * q * q > kNT || orders[s].E < 0 || !D[s]) {
+        if (eb * q * q > kMaxTileLines || orders[s].E < 0 || !D[s]) {
             delete h;
             return orders[s].E < 0 ? BK_ERR_SIZE : BK_ERR_ARG;
         }
@@ -684,6 +730,10 @@ int bk_hplan_create(bk_hplan_t* out, int norders, const bk_order_range* orders, 
     h->eo_ok = fill_eo_params(h->e_dfma, *h, D, conv_d) && fill_eo_params(h->e_ff, *h, D, conv_ff) &&
                fill_eo_params(h->e_f32, *h, D, conv_f);
     h->kernel = h->eo_ok ? BK_KERNEL_SWEEP : BK_KERNEL_COLUMN;
+    if (!h->eo_ok && !column_fits(*h)) {
+        delete h;
+        return BK_ERR_ARG;
+    }
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     int rc = BK_OK;
     const size_t nb = size_t(h->n);
@@ -731,7 +781,27 @@ long long bk_hplan_size(bk_hplan_t h, int what)
     if (what == 1) return h->ng;
     if (what == 2) return h->ntiles;
     if (what == 3) return h->kernel;
+    if (what == 4) {
+        int ub = 0, gb = 0, wb = 0;
+        return MultiFF::smem(h->e_ff, ub, gb, wb);
+    }
+    if (what == 5) return smem_f32<EngMixed>(h->e_f32);
+    if (what == 6) return h->e_f32.block;
+    if (what == 7) return h->e_f32.gstage;
     return -1;
+}
+
+int bk_hplan_set_shape(bk_hplan_t h, int threads, int gstage)
+{
+    if (!h) return BK_ERR_NULL;
+    if (threads != 0 && (threads < 64 || threads > kNT || threads % 32 != 0)) return BK_ERR_ARG;
+    if (gstage != 0 && gstage != 1) return BK_ERR_ARG;
+    if (threads != h->e_f32.block || gstage != h->e_f32.gstage) {
+        free_graph(h);
+        h->e_dfma.block = h->e_ff.block = h->e_f32.block = threads;
+        h->e_dfma.gstage = h->e_ff.gstage = h->e_f32.gstage = gstage;
+    }
+    return BK_OK;
 }
 
 int bk_hplan_set_kernel(bk_hplan_t h, int kernel)
@@ -742,6 +812,7 @@ int bk_hplan_set_kernel(bk_hplan_t h, int kernel)
     else if (kernel == BK_KERNEL_COLUMN) k = BK_KERNEL_COLUMN;
     else if (kernel == BK_KERNEL_SWEEP && h->eo_ok) k = BK_KERNEL_SWEEP;
     else return BK_ERR_ARG;
+    if (k == BK_KERNEL_COLUMN && !column_fits(*h)) return BK_ERR_ARG;
     if (k != h->kernel) {
         free_graph(h);
         h->kernel = k;

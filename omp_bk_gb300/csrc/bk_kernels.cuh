@@ -243,6 +243,18 @@ constexpr int stage_bytes(int n)
 // part; every thread adds its bytes to *tx.
 template <class S>
 __device__ __forceinline__ S* stage_issue(void* buf, const S* src, int n, const S* lim, uint64_t* bar, uint32_t& tx,
+                                          int tid, int nt);
+
+// Where stage_issue(buf, src, ...) puts src[0]: the copy starts at src
+// rounded down to 16 bytes, which lands on buf itself.
+template <class S>
+__device__ __forceinline__ const S* stage_at(const void* buf, const S* src)
+{
+    return reinterpret_cast<const S*>(static_cast<const char*>(buf) + (reinterpret_cast<uintptr_t>(src) & 15));
+}
+
+template <class S>
+__device__ __forceinline__ S* stage_issue(void* buf, const S* src, int n, const S* lim, uint64_t* bar, uint32_t& tx,
                                           int tid, int nt)
 {
     const uintptr_t a = reinterpret_cast<uintptr_t>(src);

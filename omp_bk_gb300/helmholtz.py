@@ -46,7 +46,9 @@ def _declare():
     L.bk_hplan_cg.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_void_p,
                               C.c_void_p, C.POINTER(CGOptions), C.POINTER(CGStats), C.c_void_p]
     L.bk_hplan_set_kernel.argtypes = [C.c_void_p, C.c_int]
-    for f in ("bk_hplan_create", "bk_hplan_destroy", "bk_hplan_apply", "bk_hplan_cg", "bk_hplan_set_kernel"):
+    L.bk_hplan_set_shape.argtypes = [C.c_void_p, C.c_int, C.c_int]
+    for f in ("bk_hplan_create", "bk_hplan_destroy", "bk_hplan_apply", "bk_hplan_cg", "bk_hplan_set_kernel",
+              "bk_hplan_set_shape"):
         getattr(L, f).restype = C.c_int
     L._hplan_declared = True
     return L
@@ -62,7 +64,7 @@ def default_tiles(p: int) -> int:
 class HelmholtzPlan:
     """orders: list of (p, E) or (p, E, elems_per_tile)."""
 
-    def __init__(self, orders, stream=None):
+    def __init__(self, orders, stream=None, block=0, gstage=0):
         L = _declare()
         self.orders = [tuple(o) + (0,) * (3 - len(o)) for o in orders]
         self.p = [o[0] for o in self.orders]
@@ -73,6 +75,8 @@ class HelmholtzPlan:
         h = C.c_void_p()
         check(L.bk_hplan_create(C.byref(h), len(self.orders), arr, dptr, _stream(stream)), "bk_hplan_create")
         self.h = h
+        if block or gstage:
+            self.set_shape(block, gstage)
         self.n = L.bk_hplan_size(h, 0)
         self.ng = L.bk_hplan_size(h, 1)
         self.ntiles = L.bk_hplan_size(h, 2)
@@ -90,6 +94,25 @@ class HelmholtzPlan:
         """The body of the persistent launch: KERNEL_SWEEP (even-odd line
         sweeps) or KERNEL_COLUMN."""
         return int(_declare().bk_hplan_size(self.h, 3))
+
+    def set_shape(self, block: int = 0, gstage: int = 0):
+        """Threads per block of the sweep body's launch (0: the largest
+        tile's lines; tiles with more lines loop over them) and, for FP32
+        storage, whether G is staged in shared memory (bk_hplan_set_shape)."""
+        check(_declare().bk_hplan_set_shape(self.h, int(block), int(gstage)), "bk_hplan_set_shape")
+
+    @property
+    def block(self) -> int:
+        return int(_declare().bk_hplan_size(self.h, 6))
+
+    @property
+    def gstage(self) -> int:
+        return int(_declare().bk_hplan_size(self.h, 7))
+
+    def smem_bytes(self, fp64: bool = False) -> int:
+        """Shared memory per block of the sweep body's launch for FP64
+        (fp64) or FP32 storage."""
+        return int(_declare().bk_hplan_size(self.h, 4 if fp64 else 5))
 
     def set_kernel(self, kernel: int):
         check(_declare().bk_hplan_set_kernel(self.h, int(kernel)), "bk_hplan_set_kernel")

@@ -1,34 +1,65 @@
 """Autotuner of the mixed-order persistent launch.
 
-The launch runs every tile with the same block, whose threads are the
-largest tile's lines (elements x (p+1)^2): tiles of the other orders should
-have about as many lines, or threads idle in their sweeps.  So the tuner
-picks one line budget T for the whole plan and gives order p
-max(1, T // (p+1)^2) elements per tile; every candidate T is timed with CUDA
-events on the plan itself (element counts capped), the fastest kept.
-Results are cached per GPU name, precision, kernel body and order set in a
-JSON file (~/.cache/omp_bk_gb300/tune.json, or $BK_TUNE_CACHE)."""
+The persistent launch walks tiles of every order with one block shape.  The
+choices that shape it are timed here with CUDA events on the plan itself
+(element counts capped), the fastest kept:
+
+* the block size B (threads per block of the even-odd sweep body), from
+  BLOCKS;
+* for FP32 storage, whether each tile's G is staged in shared memory by TMA
+  or read in the pointwise stage straight from global memory (prefetched
+  into L2 one tile ahead): staging costs shared memory and so blocks per SM,
+  reading costs load latency;
+* the elements per tile eb_p of every order p: a tile of eb_p elements has
+  eb_p (p+1)^2 lines, which the block's B threads sweep (a tile with more
+  lines than threads loops over them), and the largest tile's stages and
+  work boxes set the launch's shared memory and so its blocks per SM.
+
+Search: every (B, staging) starts from the tiles whose lines fill B best (at
+most B lines); the best start is then improved one order at a time over the
+counts whose lines fill 1..4 sweeps of B threads (coordinate descent, two
+passes).  Shapes whose FP64 or FP32 launch would not fit a block's shared
+memory are skipped (the solver's FP64 residual runs on the same tiles).  The
+column body (one thread per column, tiles of at most 256 columns) keeps one
+line budget T for the plan, eb_p = max(1, T // (p+1)^2).
+
+Results are cached per GPU name, precision, body and order set in a JSON file
+(~/.cache/omp_bk_gb300/tune.json, or $BK_TUNE_CACHE)."""
 from __future__ import annotations
 
 import json
 import os
 
-from . import PREC_MIXED
+from . import KERNEL_COLUMN, PREC_MIXED
 from .helmholtz import HelmholtzPlan
 
 CACHE = os.environ.get("BK_TUNE_CACHE", os.path.join(os.path.expanduser("~"), ".cache", "omp_bk_gb300", "tune.json"))
 
-LINE_BUDGETS = (64, 96, 128, 160, 192, 256)
+BLOCKS = (128, 192, 256)      # threads per block of the sweep body
+GSTAGE = (0, 1)               # FP32 G read from global memory / staged
+LINE_BUDGETS = (64, 96, 128, 160, 192, 256)   # column body
+MAX_TILE_LINES = 1024         # bk_order_range: elems_per_tile * q^2 <= 1024
+MAX_SMEM = 232448             # shared memory of one block, bytes
 
 
 def tiles_for(p: int, lines: int) -> int:
-    """Elements per tile of order p under a budget of `lines` threads."""
+    """Elements per tile of order p under a budget of `lines` lines."""
     return max(1, lines // (p + 1) ** 2)
 
 
-def candidates(p: int):
-    """The elements per tile the tuner can give order p."""
-    return sorted({tiles_for(p, t) for t in LINE_BUDGETS})
+def candidates(p: int, block: int = 0):
+    """Elements per tile the tuner tries for order p: with a block of
+    `block` threads, the counts whose lines fill 1..4 sweeps of the block
+    best; without, the column body's line budgets."""
+    if not block:
+        return sorted({tiles_for(p, t) for t in LINE_BUDGETS})
+    q2 = (p + 1) ** 2
+    out = set()
+    for k in range(1, 5):
+        eb = max(1, (k * block) // q2)
+        if eb * q2 <= MAX_TILE_LINES:
+            out.add(eb)
+    return sorted(out)
 
 
 def _time(plan, G, M, u, v, prec, reps, torch):
@@ -44,12 +75,93 @@ def _time(plan, G, M, u, v, prec, reps, torch):
     return t0.elapsed_time(t1) / reps
 
 
+class _Bench:
+    """Times plans over the capped orders on one set of operator data."""
+
+    def __init__(self, capped, prec, kernel, reps, torch):
+        self.capped, self.prec, self.kernel, self.reps, self.torch = capped, prec, kernel, reps, torch
+        self.dt = torch.float64 if prec == 0 else torch.float32
+        self.data = None
+        self.seen = {}
+
+    def __call__(self, block, gstage, tiles):
+        key = (block, gstage, tuple(sorted(tiles.items())))
+        if key in self.seen:
+            return self.seen[key]
+        plan = HelmholtzPlan([(p, E, tiles[p]) for p, E in self.capped])
+        try:
+            plan.set_kernel(self.kernel)
+            plan.set_shape(block, gstage)
+            # the FP64 apply (the solver's residual) runs on the same tiles:
+            # both forms' stages must fit a block's shared memory
+            if max(plan.smem_bytes(fp64=True), plan.smem_bytes(fp64=False)) > MAX_SMEM:
+                ms = float("inf")
+            else:
+                if self.data is None:
+                    G, M = plan.geometry()
+                    u = self.torch.ones(plan.n, dtype=self.dt, device="cuda")
+                    self.data = (G.to(self.dt), M.to(self.dt), u, self.torch.empty_like(u))
+                G, M, u, v = self.data
+                ms = _time(plan, G, M, u, v, self.prec, self.reps, self.torch)
+        finally:
+            plan.close()
+        self.seen[key] = ms
+        return ms
+
+
+def _search_sweep(bench, orders, prec, verbose):
+    ps = [p for p, _ in orders]
+    stages = GSTAGE if prec != 0 else (0,)
+    # the best-filling tiles (at most B lines) for every block size and staging
+    starts = {}
+    for B in BLOCKS:
+        for gs in stages:
+            tiles = {p: tiles_for(p, B) for p in ps}
+            starts[(B, gs)] = (bench(B, gs, tiles), tiles)
+    B, gs = min(starts, key=lambda k: starts[k][0])
+    best_ms, best = starts[(B, gs)]
+    best = dict(best)
+    for _ in range(2):
+        changed = False
+        for p in ps:
+            for eb in candidates(p, B):
+                if eb == best[p]:
+                    continue
+                trial = dict(best)
+                trial[p] = eb
+                ms = bench(B, gs, trial)
+                if ms < best_ms:
+                    best_ms, best, changed = ms, trial, True
+        if not changed:
+            break
+    if verbose:
+        print("tune (sweep body): starts " + ", ".join(f"B={b} g={g}:{starts[(b, g)][0]:.3f}ms" for b, g in starts) +
+              f" -> B={B} gstage={gs} tiles {best} {best_ms:.3f}ms")
+    return {"block": B, "gstage": gs, "tiles": best, "ms": best_ms,
+            "starts_ms": {f"B{b}_g{g}": v[0] for (b, g), v in starts.items()}}
+
+
+def _search_column(bench, orders, verbose):
+    times = {}
+    for lines in LINE_BUDGETS:
+        times[lines] = bench(0, 0, {p: tiles_for(p, lines) for p, _ in orders})
+    best_lines = min(times, key=times.get)
+    if verbose:
+        print("tune (column body): " + ", ".join(f"{t}:{ms:.3f}ms" for t, ms in sorted(times.items())) +
+              f" -> {best_lines} lines")
+    return {"block": 0, "gstage": 0, "tiles": {p: tiles_for(p, best_lines) for p, _ in orders},
+            "ms": times[best_lines]}
+
+
 def tune(orders, prec=PREC_MIXED, max_elements=65536, reps=5, use_cache=True, verbose=False, kernel=0):
-    """{p: elements per tile} for the (p, E) orders, for the plan body
-    `kernel` (KERNEL_AUTO: the plan's default)."""
+    """The plan shape for the (p, E) orders and the plan body `kernel`
+    (KERNEL_AUTO: the plan's default, the even-odd sweep body for GLL):
+    {"block": threads per block (0: the largest tile's lines), "gstage": FP32
+    G staged (1) or read from global memory (0), "tiles": {p: elements per
+    tile}, "ms": the tuned plan's time on the capped orders}."""
     import torch
     ps = sorted(p for p, _ in orders)
-    key = f"{torch.cuda.get_device_name()}|prec{prec}|kernel{kernel}|p{','.join(map(str, ps))}"
+    key = f"{torch.cuda.get_device_name()}|prec{prec}|kernel{kernel}|p{','.join(map(str, ps))}|v2"
     cache = {}
     if use_cache and os.path.exists(CACHE):
         try:
@@ -57,30 +169,31 @@ def tune(orders, prec=PREC_MIXED, max_elements=65536, reps=5, use_cache=True, ve
         except (OSError, ValueError):
             cache = {}
     if key in cache:
-        return {int(p): int(e) for p, e in cache[key].items()}
+        c = cache[key]
+        return {"block": int(c["block"]), "gstage": int(c["gstage"]),
+                "tiles": {int(p): int(e) for p, e in c["tiles"].items()}, "ms": c.get("ms")}
     capped = [(p, max(1, min(int(E), max_elements))) for p, E in orders]
-    dt = torch.float64 if prec == 0 else torch.float32
-    times = {}
-    G = M = None
-    for lines in LINE_BUDGETS:
-        plan = HelmholtzPlan([(p, E, tiles_for(p, lines)) for p, E in capped])
-        plan.set_kernel(kernel)
-        if G is None:
-            G, M = plan.geometry()
-            G, M = G.to(dt), M.to(dt)
-            u = torch.ones(plan.n, dtype=dt, device="cuda")
-            v = torch.empty_like(u)
-        times[lines] = _time(plan, G, M, u, v, prec, reps, torch)
-        plan.close()
-    best_lines = min(times, key=times.get)
-    best = {p: tiles_for(p, best_lines) for p, _ in orders}
-    if verbose:
-        print("tune: " + ", ".join(f"{t}:{ms:.3f}ms" for t, ms in sorted(times.items())) + f" -> {best_lines} lines")
+    bench = _Bench(capped, prec, kernel, reps, torch)
+    if kernel == KERNEL_COLUMN:
+        res = _search_column(bench, capped, verbose)
+    else:
+        res = _search_sweep(bench, capped, prec, verbose)
+    res["evaluated"] = len(bench.seen)
     if use_cache:
-        cache[key] = {str(p): e for p, e in best.items()}
+        cache[key] = {"block": res["block"], "gstage": res["gstage"],
+                      "tiles": {str(p): e for p, e in res["tiles"].items()}, "ms": res["ms"]}
         try:
             os.makedirs(os.path.dirname(CACHE), exist_ok=True)
             json.dump(cache, open(CACHE, "w"), indent=1)
         except OSError:
             pass
-    return best
+    return res
+
+
+def make_plan(orders, tuned, kernel=0):
+    """A HelmholtzPlan over the (p, E) orders in the tuned shape."""
+    plan = HelmholtzPlan([(p, E, tuned["tiles"][p]) for p, E in orders])
+    if kernel:
+        plan.set_kernel(kernel)
+    plan.set_shape(tuned.get("block", 0), tuned.get("gstage", 0))
+    return plan

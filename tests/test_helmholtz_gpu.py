@@ -135,10 +135,117 @@ def test_cg_graph_reused_and_restarted(bklib, small_plan):
 
 
 def test_tuner(bklib):
+    """The tuner's plan shape: a block size and a G staging from its lists,
+    per-order tiles from their candidates (lines within the plan limit); the
+    plan it describes applies the operator."""
     from omp_bk_gb300 import tune
-    best = tune.tune([(2, 512), (5, 256), (8, 64)], max_elements=512, reps=2, use_cache=False)
+    orders = [(2, 512), (5, 256), (8, 64)]
+    best = tune.tune(orders, max_elements=512, reps=2, use_cache=False)
+    assert best["block"] in tune.BLOCKS and best["gstage"] in tune.GSTAGE and best["ms"] > 0
+    assert best["evaluated"] >= len(tune.BLOCKS) * len(tune.GSTAGE)
     for p in (2, 5, 8):
-        assert best[p] in tune.candidates(p)
+        eb = best["tiles"][p]
+        assert eb in tune.candidates(p, best["block"]) and eb * (p + 1) ** 2 <= tune.MAX_TILE_LINES
+    col = tune.tune(orders, max_elements=512, reps=2, use_cache=False, kernel=bklib.KERNEL_COLUMN)
+    assert col["block"] == 0
+    for p in (2, 5, 8):
+        assert col["tiles"][p] in tune.candidates(p) and col["tiles"][p] * (p + 1) ** 2 <= 256
+    plan = tune.make_plan(orders, best)
+    try:
+        assert plan.block == best["block"] and plan.gstage == best["gstage"]
+        G, M = plan.geometry(seed=8)
+        u = bklib.fill_uniform(torch.empty(plan.n, dtype=torch.float64, device="cuda"), 9)
+        _check_per_order(bklib, plan, G, M, u, "ff")
+        _check_per_order(bklib, plan, G, M, u, "mixed")
+    finally:
+        plan.close()
+
+
+def _check_per_order(bk, plan, G, M, u, prec, lam=1.0):
+    """The plan's persistent apply against the per-order BK5 applies with
+    the mass term and, on each order's first elements, the oracle."""
+    if prec in ("ff", "dfma"):
+        pr, eng, dt, tol = bk.PREC_FP64, (bk.ENGINE_FF if prec == "ff" else bk.ENGINE_DFMA), torch.float64, 1e-12
+    else:
+        pr, eng, dt, tol = (bk.PREC_MIXED if prec == "mixed" else bk.PREC_FP32), 0, torch.float32, 1e-5
+    Gd, Md, ud = G.to(dt), M.to(dt), u.to(dt)
+    v = torch.full_like(ud, float("nan"))
+    plan.apply(Gd, Md, lam, ud, v, prec=pr, engine=eng)
+    torch.cuda.synchronize()
+    for k, p in enumerate(plan.p):
+        su, sg = _slices(plan, k)
+        D, _, _ = bk.bk5_matrices(p)
+        w = torch.full_like(ud[su], float("nan"))
+        bk.bk5_apply(p, plan.E[k], D, Gd[sg].clone(), ud[su].clone(), w, prec=pr, engine=eng,
+                     layout=bk.LAYOUT_COLUMN, mass=Md[su].clone(), lam=lam)
+        torch.cuda.synchronize()
+        assert oracle.rel_maxdiff(host(v[su]), host(w)) < tol, p
+        q, E = p + 1, min(plan.E[k], 64)
+        f = (lambda a: host(a)) if dt == torch.float64 else (lambda a: host(a).astype(np.float32).astype(np.float64))
+        ref = oracle.bk5(q, E, D, _col_to_interleaved(f(Gd[sg][: 6 * E * q ** 3]), E, q), f(ud[su][: E * q ** 3]),
+                         mass=f(Md[su][: E * q ** 3]), lam=lam)
+        assert oracle.rel_maxdiff(host(v[su][: E * q ** 3]), ref) < tol, p
+
+
+@pytest.mark.parametrize("prec", ["ff", "dfma", "mixed", "fp32"])
+@pytest.mark.parametrize("shape", ["many_tiles", "many_tiles_gstage", "looped_lines", "looped_lines_gstage"])
+def test_multi_apply_tile_shapes(bklib, prec, shape):
+    """Blocks that walk several tiles each (FP32 storage: the next tile's u
+    and mass staged into the second buffer while the current tile computes,
+    its G prefetched into L2 or staged after the pointwise stage; FP64: the
+    single stage refilled), and tiles with more lines than the block has
+    threads (bk_hplan_set_shape): the persistent apply equals the per-order
+    applies and the oracle."""
+    from omp_bk_gb300.helmholtz import HelmholtzPlan
+    gstage = int(shape.endswith("gstage"))
+    if shape.startswith("many_tiles"):
+        plan = HelmholtzPlan([(p, 700, 1) for p in range(2, 9)], gstage=gstage)
+        assert plan.ntiles > 3 * 1216   # more tiles than resident blocks
+    else:
+        # 180, 180 and 243 lines per tile, swept by 64 threads
+        plan = HelmholtzPlan([(2, 300, 20), (5, 90, 5), (8, 40, 3)], block=64, gstage=gstage)
+        assert plan.smem_bytes(fp64=True) <= 232448 and plan.block == 64
+    assert plan.gstage == gstage
+    try:
+        G, M = plan.geometry(seed=12)
+        u = bklib.fill_uniform(torch.empty(plan.n, dtype=torch.float64, device="cuda"), 13)
+        _check_per_order(bklib, plan, G, M, u, prec, lam=1.0 if prec != "dfma" else 0.5)
+    finally:
+        plan.close()
+
+
+def test_cg_with_shapes(bklib):
+    """The CG (its inner graph fuses p . Ap into the FP32 apply) on a plan
+    with a block smaller than its tiles and G staged."""
+    from omp_bk_gb300.helmholtz import HelmholtzPlan
+    plan = HelmholtzPlan([(2, 60, 20), (4, 30, 6), (7, 12, 2)], block=64, gstage=1)
+    try:
+        G, M = plan.geometry(seed=14)
+        ustar = bklib.fill_uniform(torch.empty(plan.n, dtype=torch.float64, device="cuda"), 15)
+        f = torch.empty_like(ustar)
+        plan.apply(G, M, 1.0, ustar, f, prec=bklib.PREC_FP64)
+        x = torch.zeros_like(ustar)
+        st = plan.cg(G, M, G.float(), M.float(), 1.0, f, x, rtol=1e-10)
+        torch.cuda.synchronize()
+        assert st["converged"] and st["relres"] <= 1e-10, st
+        assert float(torch.linalg.norm(x - ustar) / torch.linalg.norm(ustar)) < 1e-6
+    finally:
+        plan.close()
+
+
+def test_set_shape_arguments(bklib):
+    from omp_bk_gb300.helmholtz import HelmholtzPlan, _declare
+    L = _declare()
+    plan = HelmholtzPlan([(3, 10, 40)])   # 640 lines per tile: not for the column body
+    try:
+        for bad in ((32, 0), (48, 0), (100, 0), (288, 0), (64, 2), (0, -1)):
+            assert L.bk_hplan_set_shape(plan.h, *bad) == bklib.BK_ERR_ARG
+        for good in ((0, 0), (64, 1), (96, 0), (256, 1)):
+            assert L.bk_hplan_set_shape(plan.h, *good) == bklib.BK_OK
+        assert plan.block == 256 and plan.gstage == 1
+        assert L.bk_hplan_set_kernel(plan.h, bklib.KERNEL_COLUMN) == bklib.BK_ERR_ARG
+    finally:
+        plan.close()
 
 
 def test_operator_spd(bklib, small_plan):
