@@ -49,7 +49,7 @@ EXPORTS = [
     "bk_hplan_apply", "bk_hplan_cg",
     "bk_dot_noalloc",
     "bk_host_plan_create", "bk_host_plan_destroy", "bk1_apply_host", "bk3_apply_host", "bk5_apply_host",
-    "bk_g_to_ff", "bk5_make_g", "bk1_transpose_jxw",
+    "bk_g_to_ff", "bk5_make_g", "bk1_transpose_jxw", "bk_probe_contract",
 ]
 
 
@@ -113,6 +113,7 @@ def lib():
         "bk_g_to_ff": [_vp, _vp, _i64, _vp],
         "bk5_make_g": [C.c_int, _i64, _vp, _vp, C.c_int, C.c_int, C.c_int, _vp],
         "bk1_transpose_jxw": [C.c_int, _i64, _vp, _vp, C.c_int, _vp],
+        "bk_probe_contract": [C.c_int, C.c_longlong, _dp, _vp, _vp, _vp],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -241,6 +242,20 @@ def bk1_transpose_jxw(p, E, jxw, out=None, stream=None):
     prec = PREC_FP64 if jxw.dtype == torch.float64 else PREC_FP32
     check(lib().bk1_transpose_jxw(p, E, _ptr(jxw), _ptr(out), prec, _stream(stream)), "bk1_transpose_jxw")
     return out
+
+
+PROBE_COPY, PROBE_FF, PROBE_MMA = 0, 1, 2
+
+
+def probe_contract(method, D, x, y, stream=None):
+    """y(l, i) = sum_n D(i, n) x(l, n) over lines of 8 doubles by one route
+    (include/bk_probe.h): PROBE_COPY (split and join only), PROBE_FF (the
+    float-float route of the operator kernels) or PROBE_MMA (exact byte
+    slices on the tensor cores); a measurement entry point."""
+    Dh, Dp = _host(D)
+    check(lib().bk_probe_contract(int(method), x.numel() // 8, Dp, _ptr(x), _ptr(y), _stream(stream)),
+          "bk_probe_contract")
+    return y
 
 
 def g_to_ff(G, out=None, stream=None):

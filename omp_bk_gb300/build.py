@@ -45,7 +45,8 @@ def _units() -> list[tuple[str, list[str], str]]:
             for lay in range(3):
                 u.append(("bk_ops.cu", [f"-DBK_ENGINE_TU={eng}", f"-DBK_OP_TU={op}", f"-DBK_LAYOUT_TU={lay}"],
                           f"bk_ops_{eng}_{op}_{lay}.o"))
-    for src in ("bk_helmholtz.cu", "bk_api.cu", "bk_geom.cu", "bk_basis.cpp", "bk_vec.cu", "bk_noalloc.cu", "bk_host.cu"):
+    for src in ("bk_helmholtz.cu", "bk_api.cu", "bk_geom.cu", "bk_basis.cpp", "bk_vec.cu", "bk_noalloc.cu", "bk_host.cu",
+                "bk_probe.cu"):
         u.append((src, [], src.rsplit(".", 1)[0] + ".o"))
     return u
 
