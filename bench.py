@@ -623,6 +623,12 @@ def run_helmholtz(args):
             bk.bk5_apply(p, E, Dp[p], GG[sg], uu[su], vv[su], prec=prec, layout=bk.LAYOUT_COLUMN, mass=MM[su],
                          lam=1.0)
 
+    # the per-order launches take KERNEL_AUTO: the kernel shape per order
+    # measured by the tuner (sweep or column), FP32 storage and FP64
+    shapes = {name: tune.tune_apply(orders, prec=pr, layout=bk.LAYOUT_COLUMN, with_mass=True)
+              for name, pr in (("mixed", bk.PREC_MIXED), ("fp64", bk.PREC_FP64))}
+    shape_names = {name: {p: ("sweep" if r["kernel"] == bk.KERNEL_SWEEP else "column") for p, r in s.items()}
+                   for name, s in shapes.items()}
     aligned = all((o * 8) % 16 == 0 for o in plan.uoff) and all((o * 8) % 16 == 0 for o in plan.goff)
     m_per64 = _events_ms(lambda: per_order(bk.PREC_FP64, G, M, ustar, v64), max(3, steps // 4), 2, torch,
                          graph=True) if aligned else None
@@ -660,6 +666,7 @@ def run_helmholtz(args):
             "multi_mixed_column_gdofs": plan.n / m_col / 1e6, "tile_elems_column": tuned_col["tiles"],
             "per_order_mixed_gdofs": (plan.n / m_per32 / 1e6) if m_per32 else None,
             "per_order_fp64_gdofs": (plan.n / m_per64 / 1e6) if m_per64 else None,
+            "per_order_kernel_tuned": shape_names,
             "cg": st, "cg_seconds": solve_s, "solution_rel_err": err,
             "cpu_baseline": _cpu_line(units, sec, "BK5 + mass FP64 on the first 64 elements of every order, mean of "
                                                   "3 (oracle/bk_oracle.c, -O3, OpenMP)")}

@@ -209,6 +209,22 @@ int bk3_adjoint(int p, int64_t E, const double* B, const double* D, const void* 
                 const void* u, const void* res, void* dk, void* dG, const bk_options* opt,
                 bk_stream_t stream);
 
+/* BK5's BK_KERNEL_AUTO per order p, precision, engine, layout and mass term
+ * (with_mass 0/1: bk5_apply_ex with or without a mass array): kernel
+ * BK_KERNEL_SWEEP or BK_KERNEL_COLUMN fixes the shape AUTO uses there,
+ * BK_KERNEL_AUTO restores the built-in choice (the column kernel for FP32
+ * storage at p <= 5 with G in the column layout, the sweep kernel
+ * otherwise).  A tuner sets these from measurements (omp_bk_gb300.tune:
+ * tune_apply); the table is process-wide, so a process should set it before
+ * its applies run concurrently with the change.  G split ahead of time
+ * (BK_G_FF) always takes the sweep kernel.  No reference counterpart: it
+ * plays the part of the harnesses' per-order variant pick
+ * (openmp/offload/bk5_offload.cpp:750-772). */
+int bk5_set_auto_kernel(int p, int prec, int engine, int layout, int with_mass, int kernel);
+/* The kernel shape BK_KERNEL_AUTO takes for these arguments, or minus a
+ * bk_status code for invalid ones. */
+int bk5_auto_kernel(int p, int prec, int engine, int layout, int with_mass);
+
 /* make_bk5_G on the device (replaces include/bk_harness.h:220-244): G6i,
  * the six symmetric factors interleaved as BK5.cpp stores them,
  * G6i(e, i, j, s, k) (g6i_index, bk_harness.h:210), into G with nfactors = 6

@@ -49,7 +49,8 @@ EXPORTS = [
     "bk_hplan_apply", "bk_hplan_cg",
     "bk_dot_noalloc",
     "bk_host_plan_create", "bk_host_plan_destroy", "bk1_apply_host", "bk3_apply_host", "bk5_apply_host",
-    "bk_g_to_ff", "bk5_make_g", "bk1_transpose_jxw", "bk_probe_contract",
+    "bk_g_to_ff", "bk5_make_g", "bk1_transpose_jxw", "bk_probe_contract", "bk5_set_auto_kernel",
+    "bk5_auto_kernel",
 ]
 
 
@@ -114,6 +115,8 @@ def lib():
         "bk5_make_g": [C.c_int, _i64, _vp, _vp, C.c_int, C.c_int, C.c_int, _vp],
         "bk1_transpose_jxw": [C.c_int, _i64, _vp, _vp, C.c_int, _vp],
         "bk_probe_contract": [C.c_int, C.c_longlong, _dp, _vp, _vp, _vp],
+        "bk5_set_auto_kernel": [C.c_int] * 6,
+        "bk5_auto_kernel": [C.c_int] * 5,
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -256,6 +259,21 @@ def probe_contract(method, D, x, y, stream=None):
     check(lib().bk_probe_contract(int(method), x.numel() // 8, Dp, _ptr(x), _ptr(y), _stream(stream)),
           "bk_probe_contract")
     return y
+
+
+def bk5_set_auto_kernel(p, prec, layout, kernel, engine=ENGINE_AUTO, with_mass=False):
+    """Fix the shape BK5's KERNEL_AUTO takes for (p, prec, engine, layout,
+    mass term): KERNEL_SWEEP, KERNEL_COLUMN, or KERNEL_AUTO for the built-in
+    rule (the tuner's hook, process-wide)."""
+    check(lib().bk5_set_auto_kernel(p, prec, engine, layout, int(bool(with_mass)), kernel), "bk5_set_auto_kernel")
+
+
+def bk5_auto_kernel(p, prec, layout, engine=ENGINE_AUTO, with_mass=False) -> int:
+    """The shape BK5's KERNEL_AUTO takes for these arguments."""
+    r = lib().bk5_auto_kernel(p, prec, engine, layout, int(bool(with_mass)))
+    if r < 0:
+        raise BKError(-r, "bk5_auto_kernel")
+    return r
 
 
 def g_to_ff(G, out=None, stream=None):

@@ -26,6 +26,9 @@ constexpr long long kDefaultWaitLimit = 4000000000LL;   // SM cycles, ~2 s
 // address is that of this module's copy in the device's primary context; the
 // library is not meant to outlive a reset of that context (cudaDeviceReset).
 std::atomic<long long> g_wait_limit[kMaxDevices];
+// BK5's BK_KERNEL_AUTO as measured by a tuner, per order, engine, layout and
+// mass term (0: the built-in rule, bk5_builtin_auto); process-wide.
+std::atomic<int> g_auto_kernel[9][4][3][2];
 std::atomic<int*> g_status_ptr[kMaxDevices];
 std::atomic<int> g_sm_count[kMaxDevices];
 }  // namespace
@@ -172,16 +175,48 @@ int bk5_apply_ex(int p, int64_t E, const double* D, const void* G, const void* u
     if (E == 0) return BK_OK;
     if ((rc = status_or_null())) return rc;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    // AUTO: the tuned shape where a tuner set one, else the built-in rule
+    int kernel = o.kernel;
+    if (kernel == BK_KERNEL_AUTO) {
+        const int t = g_auto_kernel[p][eng][o.layout][mass != nullptr ? 1 : 0].load(std::memory_order_relaxed);
+        kernel = (o.gform == BK_G_STORAGE && t != 0) ? t : bk5_builtin_auto(p, eng, o.layout);
+        if (o.gform != BK_G_STORAGE) kernel = BK_KERNEL_SWEEP;
+    }
     switch (eng) {
-        case 0: return launch_bk5_dfma(p, E, D, G, u, mass, lambda, v, o.nfactors, o.layout, o.elems_per_block, o.kernel,
+        case 0: return launch_bk5_dfma(p, E, D, G, u, mass, lambda, v, o.nfactors, o.layout, o.elems_per_block, kernel,
                                       o.gform, s);
-        case 1: return launch_bk5_ff(p, E, D, G, u, mass, lambda, v, o.nfactors, o.layout, o.elems_per_block, o.kernel,
+        case 1: return launch_bk5_ff(p, E, D, G, u, mass, lambda, v, o.nfactors, o.layout, o.elems_per_block, kernel,
                                       o.gform, s);
-        case 2: return launch_bk5_f32(p, E, D, G, u, mass, lambda, v, o.nfactors, o.layout, o.elems_per_block, o.kernel,
+        case 2: return launch_bk5_f32(p, E, D, G, u, mass, lambda, v, o.nfactors, o.layout, o.elems_per_block, kernel,
                                       o.gform, s);
-        default: return launch_bk5_mixed(p, E, D, G, u, mass, lambda, v, o.nfactors, o.layout, o.elems_per_block, o.kernel,
+        default: return launch_bk5_mixed(p, E, D, G, u, mass, lambda, v, o.nfactors, o.layout, o.elems_per_block, kernel,
                                       o.gform, s);
     }
+}
+
+int bk5_set_auto_kernel(int p, int prec, int engine, int layout, int with_mass, int kernel)
+{
+    if (p < 1 || p > 8) return BK_ERR_ORDER;
+    bk_options o = bk_default_options();
+    o.prec = prec;
+    o.engine = engine;
+    const int eng = engine_of(o);
+    if (eng < 0 || layout < 0 || layout > 2 || (with_mass != 0 && with_mass != 1)) return BK_ERR_PREC;
+    if (kernel != BK_KERNEL_AUTO && kernel != BK_KERNEL_SWEEP && kernel != BK_KERNEL_COLUMN) return BK_ERR_ARG;
+    g_auto_kernel[p][eng][layout][with_mass].store(kernel, std::memory_order_relaxed);
+    return BK_OK;
+}
+
+int bk5_auto_kernel(int p, int prec, int engine, int layout, int with_mass)
+{
+    if (p < 1 || p > 8) return -BK_ERR_ORDER;
+    bk_options o = bk_default_options();
+    o.prec = prec;
+    o.engine = engine;
+    const int eng = engine_of(o);
+    if (eng < 0 || layout < 0 || layout > 2 || (with_mass != 0 && with_mass != 1)) return -BK_ERR_PREC;
+    const int t = g_auto_kernel[p][eng][layout][with_mass].load(std::memory_order_relaxed);
+    return t != 0 ? t : bk5_builtin_auto(p, eng, layout);
 }
 
 int bk5_apply_opt(int p, int64_t E, const double* D, const void* G, const void* u, void* v, const bk_options* opt,

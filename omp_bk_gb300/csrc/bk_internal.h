@@ -13,6 +13,14 @@ struct DevCtx;
 constexpr int kMaxDevices = 64;
 
 int current_device();          // cudaGetDevice, or -1
+
+// BK5's built-in choice for BK_KERNEL_AUTO (measured on GB300 at about 2^24
+// DoFs): the column kernel for the FP32-storage engines (2: FP32, 3: mixed)
+// at p <= 5 with G in the column layout, the sweep kernel otherwise.
+inline int bk5_builtin_auto(int p, int eng, int layout)
+{
+    return (eng >= 2 && p <= 5 && layout == 2) ? BK_KERNEL_COLUMN : BK_KERNEL_SWEEP;
+}
 int sm_count();                // SMs of the current device
 DevCtx dev_ctx();              // status word and wait limit of the current device
 

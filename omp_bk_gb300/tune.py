@@ -23,6 +23,11 @@ memory are skipped (the solver's FP64 residual runs on the same tiles).  The
 column body (one thread per column, tiles of at most 256 columns) keeps one
 line budget T for the plan, eb_p = max(1, T // (p+1)^2).
 
+tune_apply() does the same for the single-order BK5 applies: per order it
+times the two kernel shapes (one thread per line, one thread per k-column)
+and sets the faster as the library's KERNEL_AUTO choice for that order,
+precision, layout and mass term.
+
 Results are cached per GPU name, precision, body and order set in a JSON file
 (~/.cache/omp_bk_gb300/tune.json, or $BK_TUNE_CACHE)."""
 from __future__ import annotations
@@ -197,3 +202,71 @@ def make_plan(orders, tuned, kernel=0):
         plan.set_kernel(kernel)
     plan.set_shape(tuned.get("block", 0), tuned.get("gstage", 0))
     return plan
+
+
+# ---- single-order BK5 applies: the kernel shape per order ------------------------
+
+def tune_apply(orders, prec=PREC_MIXED, layout=2, with_mass=True, reps=10, max_elements=65536, use_cache=True,
+               verbose=False):
+    """BK5's kernel shape per order for bk5_apply(..., kernel=KERNEL_AUTO):
+    for every (p, E) of `orders` (E capped) the sweep kernel (one thread per
+    line) and the column kernel (one thread per k-column) are timed with
+    CUDA events on the same inputs, and the faster is set as AUTO's choice
+    for (p, prec, layout, mass term) in the library (bk5_set_auto_kernel).
+    Returns {p: {"kernel": KERNEL_SWEEP | KERNEL_COLUMN, "sweep_ms": ..,
+    "column_ms": ..}}; results cached like tune()."""
+    import torch
+
+    from . import KERNEL_SWEEP, bk5_apply, bk5_matrices, bk5_set_auto_kernel, fill_uniform
+    key = (f"{torch.cuda.get_device_name()}|apply|prec{prec}|layout{layout}|mass{int(bool(with_mass))}|"
+           + ",".join(f"{p}:{min(int(E), max_elements)}" for p, E in sorted(orders)))
+    cache = {}
+    if use_cache and os.path.exists(CACHE):
+        try:
+            cache = json.load(open(CACHE))
+        except (OSError, ValueError):
+            cache = {}
+    if key in cache:
+        res = {int(p): v for p, v in cache[key].items()}
+    else:
+        dt = torch.float64 if prec == 0 else torch.float32
+        res = {}
+        for p, E in sorted(orders):
+            E = max(1, min(int(E), max_elements))
+            q = p + 1
+            D = bk5_matrices(p)[0]
+            u = fill_uniform(torch.empty(E * q ** 3, dtype=dt, device="cuda"), 3)
+            G = fill_uniform(torch.empty(6 * E * q ** 3, dtype=dt, device="cuda"), 4, 0.5, 1.5)
+            M = fill_uniform(torch.empty(E * q ** 3, dtype=dt, device="cuda"), 5, 0.5, 1.5) if with_mass else None
+            v = torch.empty_like(u)
+            t = {}
+            for name, kern in (("sweep", KERNEL_SWEEP), ("column", KERNEL_COLUMN)):
+                def run():
+                    bk5_apply(p, E, D, G, u, v, prec=prec, layout=layout, mass=M, lam=1.0 if with_mass else 0.0,
+                              kernel=kern)
+                run()
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                for _ in range(reps):
+                    run()
+                e1.record()
+                torch.cuda.synchronize()
+                t[name] = e0.elapsed_time(e1) / reps
+            res[p] = {"kernel": KERNEL_SWEEP if t["sweep"] <= t["column"] else KERNEL_COLUMN,
+                      "sweep_ms": t["sweep"], "column_ms": t["column"]}
+            del u, G, M, v
+        if use_cache:
+            cache[key] = {str(p): v for p, v in res.items()}
+            try:
+                os.makedirs(os.path.dirname(CACHE), exist_ok=True)
+                json.dump(cache, open(CACHE, "w"), indent=1)
+            except OSError:
+                pass
+    for p, r in res.items():
+        bk5_set_auto_kernel(p, prec, layout, r["kernel"], with_mass=with_mass)
+    if verbose:
+        print("tune_apply: " + ", ".join(f"p={p}: {'sweep' if r['kernel'] == KERNEL_SWEEP else 'column'} "
+                                         f"({r['sweep_ms']:.3f} / {r['column_ms']:.3f} ms)"
+                                         for p, r in sorted(res.items())))
+    return res

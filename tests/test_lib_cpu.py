@@ -141,3 +141,24 @@ def test_interp_and_deriv_identities(bklib, p):
     assert np.allclose(D5 @ x, 1.0, atol=1e-12)
     if p >= 2:
         assert np.allclose(D5 @ x ** 2, 2 * x, atol=1e-11)
+
+
+def test_auto_kernel_table(bklib):
+    """BK5's KERNEL_AUTO table: the built-in rule by default, a tuned shape
+    once set, the rule again after a reset; argument checks (no GPU needed)."""
+    bk = bklib
+    L = bk.lib()
+    assert bk.bk5_auto_kernel(4, bk.PREC_MIXED, bk.LAYOUT_COLUMN) == bk.KERNEL_COLUMN
+    assert bk.bk5_auto_kernel(7, bk.PREC_MIXED, bk.LAYOUT_COLUMN) == bk.KERNEL_SWEEP
+    assert bk.bk5_auto_kernel(4, bk.PREC_FP64, bk.LAYOUT_COLUMN) == bk.KERNEL_SWEEP
+    assert bk.bk5_auto_kernel(4, bk.PREC_MIXED, bk.LAYOUT_INTERLEAVED) == bk.KERNEL_SWEEP
+    bk.bk5_set_auto_kernel(4, bk.PREC_MIXED, bk.LAYOUT_COLUMN, bk.KERNEL_SWEEP, with_mass=True)
+    assert bk.bk5_auto_kernel(4, bk.PREC_MIXED, bk.LAYOUT_COLUMN, with_mass=True) == bk.KERNEL_SWEEP
+    assert bk.bk5_auto_kernel(4, bk.PREC_MIXED, bk.LAYOUT_COLUMN, with_mass=False) == bk.KERNEL_COLUMN
+    bk.bk5_set_auto_kernel(4, bk.PREC_MIXED, bk.LAYOUT_COLUMN, bk.KERNEL_AUTO, with_mass=True)
+    assert bk.bk5_auto_kernel(4, bk.PREC_MIXED, bk.LAYOUT_COLUMN, with_mass=True) == bk.KERNEL_COLUMN
+    assert L.bk5_set_auto_kernel(9, 0, 0, 2, 0, 1) == bk.BK_ERR_ORDER
+    assert L.bk5_set_auto_kernel(3, 7, 0, 2, 0, 1) == bk.BK_ERR_PREC
+    assert L.bk5_set_auto_kernel(3, 0, 0, 3, 0, 1) == bk.BK_ERR_PREC
+    assert L.bk5_set_auto_kernel(3, 0, 0, 2, 0, 5) == bk.BK_ERR_ARG
+    assert L.bk5_auto_kernel(0, 0, 0, 2, 0) == -bk.BK_ERR_ORDER
