@@ -266,3 +266,33 @@ def test_operator_spd(bklib, small_plan):
         assert uMu > 0 and uAu >= lam * uMu * (1 - 1e-12)
         scale = float(torch.linalg.norm(u) * torch.linalg.norm(Aw))
         assert abs(float(torch.dot(u, Aw)) - float(torch.dot(w, Au))) <= 1e-12 * scale
+
+
+def test_tune_apply_sets_auto(bklib):
+    """The per-order tuner of the single-order BK5 applies times both kernel
+    shapes and sets KERNEL_AUTO to the faster; an AUTO apply is then bitwise
+    the apply with that shape.  The process-wide table is reset afterwards."""
+    from omp_bk_gb300 import tune
+    bk = bklib
+    orders = [(3, 300), (7, 40)]
+    res = tune.tune_apply(orders, prec=bk.PREC_MIXED, layout=bk.LAYOUT_COLUMN, with_mass=True, reps=2,
+                          use_cache=False)
+    try:
+        for p, E in orders:
+            r = res[p]
+            assert r["kernel"] in (bk.KERNEL_SWEEP, bk.KERNEL_COLUMN) and r["sweep_ms"] > 0 and r["column_ms"] > 0
+            assert bk.bk5_auto_kernel(p, bk.PREC_MIXED, bk.LAYOUT_COLUMN, with_mass=True) == r["kernel"]
+            q = p + 1
+            D = bk.bk5_matrices(p)[0]
+            u = bk.fill_uniform(torch.empty(E * q ** 3, dtype=torch.float32, device="cuda"), 1)
+            G = bk.fill_uniform(torch.empty(6 * E * q ** 3, dtype=torch.float32, device="cuda"), 2, 0.5, 1.5)
+            M = bk.fill_uniform(torch.empty(E * q ** 3, dtype=torch.float32, device="cuda"), 3, 0.5, 1.5)
+            v0, v1 = torch.empty_like(u), torch.empty_like(u)
+            bk.bk5_apply(p, E, D, G, u, v0, prec=bk.PREC_MIXED, layout=bk.LAYOUT_COLUMN, mass=M, lam=1.0)
+            bk.bk5_apply(p, E, D, G, u, v1, prec=bk.PREC_MIXED, layout=bk.LAYOUT_COLUMN, mass=M, lam=1.0,
+                         kernel=r["kernel"])
+            torch.cuda.synchronize()
+            assert torch.equal(v0, v1)
+    finally:
+        for p, _ in orders:
+            bk.bk5_set_auto_kernel(p, bk.PREC_MIXED, bk.LAYOUT_COLUMN, bk.KERNEL_AUTO, with_mass=True)
