@@ -67,11 +67,17 @@ int bk_hplan_set_shape(bk_hplan_t plan, int threads, int gstage);
 int bk_hplan_apply(bk_hplan_t plan, const void* G, const void* mass, double lambda, const void* u, void* v,
                    int prec, int engine, bk_stream_t stream);
 
+enum { BK_PRECOND_NONE = 0, BK_PRECOND_JACOBI = 1 };
+
 typedef struct bk_cg_options {
     double rtol;        /* stop at |f - A x| <= rtol |f| (FP64 residual); default 1e-10 */
     int max_outer;      /* refinement steps; default 8 */
-    double inner_rtol;  /* inner FP32 CG tolerance (relative); default 1e-5 */
+    double inner_rtol;  /* inner FP32 CG tolerance, relative, on r.z (the
+                           residual in the preconditioner's norm); default 1e-5 */
     int max_inner;      /* inner iterations per refinement step; default 10000 */
+    int precond;        /* inner CG preconditioner: BK_PRECOND_JACOBI (the
+                           default with opt NULL: z = r / diag(A)) or
+                           BK_PRECOND_NONE */
 } bk_cg_options;
 
 typedef struct bk_cg_stats {
@@ -79,6 +85,14 @@ typedef struct bk_cg_stats {
     int inner;          /* inner CG iterations, all steps */
     double relres;      /* final |f - A x| / |f| in FP64 */
 } bk_cg_stats;
+
+/* The diagonal of A = K + lambda M at every point (FP64; G, mass as for
+ * bk_hplan_apply in double, mass may be NULL): the sums of D(n,i)^2 times the
+ * diagonal factors along the three lines through the point and the mixed
+ * factors at the point (the element operators are independent, so this is
+ * the assembled diagonal too).  The inner CG's Jacobi preconditioner. */
+int bk_hplan_diagonal(bk_hplan_t plan, const void* G, const void* mass, double lambda, double* diag,
+                      bk_stream_t stream);
 
 /* Solves A x = f (x holds the initial guess; f, x FP64 device vectors).
  * The residual is formed in FP64 with G64/mass64 (double); the inner CG

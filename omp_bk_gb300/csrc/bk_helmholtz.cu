@@ -216,14 +216,61 @@ int smem_f32(const PMultiEO<float>& prm)
 
 // ---- CG kernels --------------------------------------------------------------
 
+// The diagonal of A = D^T G D + lambda M at the points of segment s (FP64
+// from the stored G and mass): with e_x the unit vector of point x = (i, j,
+// k), (D_r e_x)(y) = D(y_i, i) on the line through x along i and zero
+// elsewhere, so the three directions' own terms are sums along the lines
+// through x and the mixed terms meet only at x:
+//   A_xx = sum_n D(n,i)^2 G_rr(n,j,k) + D(n,j)^2 G_ss(i,n,k) + D(n,k)^2 G_tt(i,j,n)
+//        + 2 (D(i,i) D(j,j) G_rs + D(i,i) D(k,k) G_rt + D(j,j) D(k,k) G_st)(x)
+//        + lambda mass(x).
+// G in the column layout G(e, f, k, i, j).  out: A_xx (double) or its
+// inverse (float, the Jacobi preconditioner of the inner CG).
+template <class T, class O, bool INV>
+__global__ void diag_kernel(const __grid_constant__ PMulti<double> prm, int s, const T* __restrict__ G,
+                            const T* __restrict__ mass, double lambda, O* __restrict__ out)
+{
+    const MultiSeg sg = prm.seg[s];
+    const int q = sg.q, q2 = q * q, q3 = q2 * q;
+    const double* Dq = prm.D + multi_doff(q);   // D(a, b) = Dq[a*q + b]
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < sg.E * q3;
+         t += (long long)gridDim.x * blockDim.x) {
+        const long long e = t / q3;
+        const int x = int(t - e * q3);
+        const int i = x / q2, j = (x / q) % q, k = x % q;
+        const T* Ge = G + sg.goff + e * 6 * q3;
+        auto g = [&](int f, int a, int b, int c) { return double(Ge[((f * q + c) * q + a) * q + b]); };   // (i,j,k) = (a,b,c)
+        double acc = 0.0;
+        for (int n = 0; n < q; ++n) {
+            const double di = Dq[n * q + i], dj = Dq[n * q + j], dk = Dq[n * q + k];
+            acc += di * di * g(0, n, j, k) + dj * dj * g(3, i, n, k) + dk * dk * g(5, i, j, n);
+        }
+        const double dii = Dq[i * q + i], djj = Dq[j * q + j], dkk = Dq[k * q + k];
+        acc += 2.0 * (dii * djj * g(1, i, j, k) + dii * dkk * g(2, i, j, k) + djj * dkk * g(4, i, j, k));
+        if (mass != nullptr) acc += lambda * double(mass[sg.uoff + t]);
+        if constexpr (INV)
+            out[sg.uoff + t] = O(acc != 0.0 ? 1.0 / acc : 1.0);
+        else
+            out[sg.uoff + t] = O(acc);
+    }
+}
+
+__global__ void fill_ones_kernel(long long n, float* __restrict__ x)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        x[i] = 1.0f;
+}
+
+// r = r64 / |r|, d = 0, p = z = invd .* r (Jacobi; invd = 1 without it)
 __global__ void cg_start_kernel(long long n, const double* __restrict__ r64, const double* __restrict__ sc,
-                                float* __restrict__ r, float* __restrict__ p, float* __restrict__ d)
+                                const float* __restrict__ invd, float* __restrict__ r, float* __restrict__ p,
+                                float* __restrict__ d)
 {
     const double inv = sc[S_INV];
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const float x = float(r64[i] * inv);
         r[i] = x;
-        p[i] = x;
+        p[i] = invd[i] * x;
         d[i] = 0.0f;
     }
 }
@@ -299,11 +346,13 @@ __global__ void __launch_bounds__(kRedThreads) cg_pap_kernel(const double* __res
     if (threadIdx.x == 0) sc[S_PAP] = pap;
 }
 
-// d += alpha p, r -= alpha Ap and the partial sums of r.r
+// d += alpha p, r -= alpha Ap and the partial sums of r.z = r.(invd .* r)
+// (the preconditioned CG's r.z; r.r without the preconditioner, invd = 1)
 __global__ void __launch_bounds__(kRedThreads) cg_update_kernel(long long n, const double* __restrict__ sc,
                                                                 const float* __restrict__ p,
                                                                 const float* __restrict__ Ap, float* __restrict__ d,
-                                                                float* __restrict__ r, double* __restrict__ part)
+                                                                float* __restrict__ r, const float* __restrict__ invd,
+                                                                double* __restrict__ part)
 {
     const double pap = sc[S_PAP];
     const float alpha = float(pap != 0.0 ? sc[S_RR] / pap : 0.0);
@@ -325,16 +374,17 @@ __global__ void __launch_bounds__(kRedThreads) cg_update_kernel(long long n, con
         rr.w = fmaf(-alpha, aa.w, rr.w);
         reinterpret_cast<float4*>(d)[i] = dd;
         reinterpret_cast<float4*>(r)[i] = rr;
-        s = fma(double(rr.x), double(rr.x), s);
-        s = fma(double(rr.y), double(rr.y), s);
-        s = fma(double(rr.z), double(rr.z), s);
-        s = fma(double(rr.w), double(rr.w), s);
+        const float4 w = reinterpret_cast<const float4*>(invd)[i];
+        s = fma(double(rr.x), double(w.x * rr.x), s);
+        s = fma(double(rr.y), double(w.y * rr.y), s);
+        s = fma(double(rr.z), double(w.z * rr.z), s);
+        s = fma(double(rr.w), double(w.w * rr.w), s);
     }
     for (long long i = 4 * n4 + blockIdx.x * (long long)kRedThreads + threadIdx.x; i < n; i += stride) {
         d[i] = fmaf(alpha, p[i], d[i]);
         const float ri = fmaf(-alpha, Ap[i], r[i]);
         r[i] = ri;
-        s = fma(double(ri), double(ri), s);
+        s = fma(double(ri), double(invd[i] * ri), s);
     }
     const double t = block_reduce(s);
     if (threadIdx.x == 0) part[blockIdx.x] = t;
@@ -357,23 +407,25 @@ __global__ void __launch_bounds__(kRedThreads) cg_step_kernel(const double* __re
     }
 }
 
+// p = z + beta p, z = invd .* r
 __global__ void cg_dir_kernel(long long n, const double* __restrict__ beta_in, const float* __restrict__ r,
-                              float* __restrict__ p)
+                              const float* __restrict__ invd, float* __restrict__ p)
 {
     const float beta = float(beta_in[0]);
     const long long n4 = n / 4;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4; i += stride) {
         const float4 rr = reinterpret_cast<const float4*>(r)[i];
+        const float4 w = reinterpret_cast<const float4*>(invd)[i];
         float4 pp = reinterpret_cast<float4*>(p)[i];
-        pp.x = fmaf(beta, pp.x, rr.x);
-        pp.y = fmaf(beta, pp.y, rr.y);
-        pp.z = fmaf(beta, pp.z, rr.z);
-        pp.w = fmaf(beta, pp.w, rr.w);
+        pp.x = fmaf(beta, pp.x, w.x * rr.x);
+        pp.y = fmaf(beta, pp.y, w.y * rr.y);
+        pp.z = fmaf(beta, pp.z, w.z * rr.z);
+        pp.w = fmaf(beta, pp.w, w.w * rr.w);
         reinterpret_cast<float4*>(p)[i] = pp;
     }
     for (long long i = 4 * n4 + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride)
-        p[i] = fmaf(beta, p[i], r[i]);
+        p[i] = fmaf(beta, p[i], invd[i] * r[i]);
 }
 // x += |r| d (FP64), the norm from the scalars
 __global__ void cg_correct_kernel(long long n, const double* __restrict__ sc, const float* __restrict__ d,
@@ -475,6 +527,7 @@ struct bk_hplan {
     float* p32;
     float* Ap32;
     float* d32;
+    float* invd;        // the inner CG's Jacobi preconditioner (ones without it)
     double* part;
     double* sc;
     double* beta;
@@ -482,6 +535,7 @@ struct bk_hplan {
     cudaGraph_t inner_graph;
     const void* g_key[3];   // operator pointers the graph was built for
     double key_lambda;
+    int key_precond;
 };
 
 namespace {
@@ -560,7 +614,23 @@ void free_graph(bk_hplan* h)
 
 // The inner CG as a graph: start, r.r, then WHILE(cond) { A p, p.Ap, update,
 // step (sets cond), new direction }.
-int build_inner_graph(bk_hplan* h, const void* G32, const void* mass32, double lambda, cudaStream_t user)
+// invd = 1 / diag(A) from the FP32 operator (precond), or ones.
+int fill_precond(bk_hplan* h, const void* G32, const void* mass32, double lambda, int precond, cudaStream_t s)
+{
+    if (!precond) {
+        fill_ones_kernel<<<grid_n(h->n), 256, 0, s>>>(h->n, h->invd);
+        return ck(cudaGetLastError());
+    }
+    for (int sg = 0; sg < h->nseg; ++sg) {
+        const long long np = h->seg[sg].E * h->seg[sg].q * h->seg[sg].q * h->seg[sg].q;
+        if (np == 0) continue;
+        diag_kernel<float, float, true><<<grid_n(np), 256, 0, s>>>(h->p_dfma, sg, static_cast<const float*>(G32),
+                                                                   static_cast<const float*>(mass32), lambda, h->invd);
+    }
+    return ck(cudaGetLastError());
+}
+
+int build_inner_graph(bk_hplan* h, const void* G32, const void* mass32, double lambda, int precond, cudaStream_t user)
 {
     free_graph(h);
     {
@@ -604,8 +674,8 @@ int build_inner_graph(bk_hplan* h, const void* G32, const void* mass32, double l
         cudaGraphDestroy(g);
         return BK_ERR_CUDA;
     }
-    cg_start_kernel<<<gn, 256, 0, s>>>(n, h->r64, h->sc, h->r32, h->p32, h->d32);
-    red_dot_kernel<<<kRedBlocks, kRedThreads, 0, s>>>(n, h->r32, h->r32, h->part);
+    cg_start_kernel<<<gn, 256, 0, s>>>(n, h->r64, h->sc, h->invd, h->r32, h->p32, h->d32);
+    red_dot_kernel<<<kRedBlocks, kRedThreads, 0, s>>>(n, h->r32, h->p32, h->part);   // r.z
     cg_init_scalars_kernel<<<1, kRedThreads, 0, s>>>(h->part, kRedBlocks, h->sc);
     cudaGraph_t captured = nullptr;
     if (cudaStreamEndCapture(s, &captured) != cudaSuccess) rc = BK_ERR_CUDA;
@@ -648,9 +718,9 @@ int build_inner_graph(bk_hplan* h, const void* G32, const void* mass32, double l
                     cg_pap_kernel<<<1, kRedThreads, 0, s>>>(h->part, kRedBlocks, h->sc);
                 }
                 cg_update_kernel<<<kRedBlocks, kRedThreads, 0, s>>>(n, h->sc, h->p32, h->Ap32, h->d32, h->r32,
-                                                                    h->part);
+                                                                    h->invd, h->part);
                 cg_step_kernel<<<1, kRedThreads, 0, s>>>(h->part, kRedBlocks, h->sc, h->beta, handle);
-                cg_dir_kernel<<<gn, 256, 0, s>>>(n, h->beta, h->r32, h->p32);
+                cg_dir_kernel<<<gn, 256, 0, s>>>(n, h->beta, h->r32, h->invd, h->p32);
                 cudaGraph_t body_out = nullptr;
                 if (cudaStreamEndCapture(s, &body_out) != cudaSuccess || arc != BK_OK) rc = BK_ERR_CUDA;
             }
@@ -667,6 +737,7 @@ int build_inner_graph(bk_hplan* h, const void* G32, const void* mass32, double l
     h->g_key[0] = G32;
     h->g_key[1] = mass32;
     h->key_lambda = lambda;
+    h->key_precond = precond;
     return BK_OK;
 }
 
@@ -743,6 +814,7 @@ int bk_hplan_create(bk_hplan_t* out, int norders, const bk_order_range* orders, 
     rc |= ck(cudaMalloc(&h->p32, 4 * (nb + 4)));
     rc |= ck(cudaMalloc(&h->Ap32, 4 * (nb + 4)));
     rc |= ck(cudaMalloc(&h->d32, 4 * (nb + 4)));
+    rc |= ck(cudaMalloc(&h->invd, 4 * (nb + 4)));
     rc |= ck(cudaMalloc(&h->part, 8 * (kRedBlocks > kMaxDotParts ? kRedBlocks : kMaxDotParts)));
     rc |= ck(cudaMalloc(&h->sc, 8 * S_NSCAL));
     rc |= ck(cudaMalloc(&h->beta, 8 * 2));
@@ -767,6 +839,7 @@ int bk_hplan_destroy(bk_hplan_t h)
     cudaFree(h->p32);
     cudaFree(h->Ap32);
     cudaFree(h->d32);
+    cudaFree(h->invd);
     cudaFree(h->part);
     cudaFree(h->sc);
     cudaFree(h->beta);
@@ -840,6 +913,23 @@ int bk_hplan_apply(bk_hplan_t h, const void* G, const void* mass, double lambda,
     return apply_plan(h, eng, G, mass, lambda, u, v, reinterpret_cast<cudaStream_t>(stream));
 }
 
+int bk_hplan_diagonal(bk_hplan_t h, const void* G, const void* mass, double lambda, double* diag, bk_stream_t stream)
+{
+    if (!h) return BK_ERR_NULL;
+    if (h->n == 0) return BK_OK;
+    if (!G || !diag) return BK_ERR_NULL;
+    if ((reinterpret_cast<uintptr_t>(G) | reinterpret_cast<uintptr_t>(mass) | reinterpret_cast<uintptr_t>(diag)) & 15)
+        return BK_ERR_ALIGN;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    for (int sg = 0; sg < h->nseg; ++sg) {
+        const long long np = h->seg[sg].E * h->seg[sg].q * h->seg[sg].q * h->seg[sg].q;
+        if (np == 0) continue;
+        diag_kernel<double, double, false><<<grid_n(np), 256, 0, s>>>(h->p_dfma, sg, static_cast<const double*>(G),
+                                                                      static_cast<const double*>(mass), lambda, diag);
+    }
+    return ck(cudaGetLastError());
+}
+
 int bk_hplan_cg(bk_hplan_t h, const void* G64, const void* mass64, const void* G32, const void* mass32,
                 double lambda, const double* f, double* x, const bk_cg_options* opt, bk_cg_stats* stats,
                 bk_stream_t stream)
@@ -850,14 +940,18 @@ int bk_hplan_cg(bk_hplan_t h, const void* G64, const void* mass64, const void* G
     o.max_outer = 8;
     o.inner_rtol = 1e-5;
     o.max_inner = 10000;
+    o.precond = BK_PRECOND_JACOBI;
     if (opt) o = *opt;
     if (!(o.rtol > 0) || !(o.inner_rtol > 0) || o.max_outer < 1 || o.max_inner < 1) return BK_ERR_ARG;
+    if (o.precond != BK_PRECOND_NONE && o.precond != BK_PRECOND_JACOBI) return BK_ERR_ARG;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     const long long n = h->n;
     int rc;
     if (dev_ctx().status == nullptr) return BK_ERR_CUDA;
-    if (!h->inner_exec || h->g_key[0] != G32 || h->g_key[1] != mass32 || h->key_lambda != lambda) {
-        if ((rc = build_inner_graph(h, G32, mass32, lambda, s))) return rc;
+    if (!h->inner_exec || h->g_key[0] != G32 || h->g_key[1] != mass32 || h->key_lambda != lambda ||
+        h->key_precond != o.precond) {
+        if ((rc = fill_precond(h, G32, mass32, lambda, o.precond, s))) return rc;
+        if ((rc = build_inner_graph(h, G32, mass32, lambda, o.precond, s))) return rc;
     }
     const double sc_init[2] = {o.inner_rtol * o.inner_rtol, double(o.max_inner)};
     if ((rc = ck(cudaMemcpyAsync(h->sc + S_TOL2, sc_init, 2 * sizeof(double), cudaMemcpyHostToDevice, s)))) return rc;

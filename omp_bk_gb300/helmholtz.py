@@ -24,8 +24,12 @@ class OrderRange(C.Structure):
     _fields_ = [("p", C.c_int), ("E", C.c_int64), ("elems_per_tile", C.c_int)]
 
 
+PRECOND_NONE, PRECOND_JACOBI = 0, 1
+
+
 class CGOptions(C.Structure):
-    _fields_ = [("rtol", C.c_double), ("max_outer", C.c_int), ("inner_rtol", C.c_double), ("max_inner", C.c_int)]
+    _fields_ = [("rtol", C.c_double), ("max_outer", C.c_int), ("inner_rtol", C.c_double), ("max_inner", C.c_int),
+                ("precond", C.c_int)]
 
 
 class CGStats(C.Structure):
@@ -46,6 +50,8 @@ def _declare():
     L.bk_hplan_cg.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_void_p,
                               C.c_void_p, C.POINTER(CGOptions), C.POINTER(CGStats), C.c_void_p]
     L.bk_hplan_set_kernel.argtypes = [C.c_void_p, C.c_int]
+    L.bk_hplan_diagonal.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_void_p, C.c_void_p]
+    L.bk_hplan_diagonal.restype = C.c_int
     L.bk_hplan_set_shape.argtypes = [C.c_void_p, C.c_int, C.c_int]
     for f in ("bk_hplan_create", "bk_hplan_destroy", "bk_hplan_apply", "bk_hplan_cg", "bk_hplan_set_kernel",
               "bk_hplan_set_shape"):
@@ -128,9 +134,18 @@ class HelmholtzPlan:
         check(_declare().bk_hplan_apply(self.h, _ptr(G), _ptr(mass), float(lam), _ptr(u), _ptr(v), prec, engine,
                                         _stream(stream)), "bk_hplan_apply")
 
+    def diagonal(self, G, mass, lam, out=None, stream=None):
+        """diag(K + lam M) at every point (FP64 G and mass)."""
+        import torch
+        if out is None:
+            out = torch.empty(self.n, dtype=torch.float64, device="cuda")
+        check(_declare().bk_hplan_diagonal(self.h, _ptr(G), _ptr(mass), float(lam), _ptr(out), _stream(stream)),
+              "bk_hplan_diagonal")
+        return out
+
     def cg(self, G64, mass64, G32, mass32, lam, f, x, rtol=1e-10, max_outer=8, inner_rtol=1e-5, max_inner=10000,
-           stream=None, allow_noconv=False):
-        o = CGOptions(rtol, max_outer, inner_rtol, max_inner)
+           stream=None, allow_noconv=False, precond=PRECOND_JACOBI):
+        o = CGOptions(rtol, max_outer, inner_rtol, max_inner, precond)
         st = CGStats()
         rc = _declare().bk_hplan_cg(self.h, _ptr(G64), _ptr(mass64), _ptr(G32), _ptr(mass32), float(lam), _ptr(f),
                                     _ptr(x), C.byref(o), C.byref(st), _stream(stream))

@@ -296,3 +296,47 @@ def test_tune_apply_sets_auto(bklib):
     finally:
         for p, _ in orders:
             bk.bk5_set_auto_kernel(p, bk.PREC_MIXED, bk.LAYOUT_COLUMN, bk.KERNEL_AUTO, with_mass=True)
+
+
+def test_diagonal_matches_unit_applies(bklib, small_plan):
+    """bk_hplan_diagonal against the operator itself: one unit vector per
+    element (a different point in each; the element operators are
+    independent), so one FP64 apply gives A_xx at all those points."""
+    bk = bklib
+    plan, G, M, _ = small_plan
+    lam = 0.6
+    diag = plan.diagonal(G, M, lam)
+    u = torch.zeros(plan.n, dtype=torch.float64, device="cuda")
+    idx = []
+    for k, p in enumerate(plan.p):
+        q3 = (p + 1) ** 3
+        for e in range(plan.E[k]):
+            idx.append(plan.uoff[k] + e * q3 + (7 * e + 3 * k) % q3)
+    idx = torch.tensor(idx, device="cuda")
+    u[idx] = 1.0
+    v = torch.empty_like(u)
+    plan.apply(G, M, lam, u, v, prec=bk.PREC_FP64, engine=bk.ENGINE_DFMA)
+    torch.cuda.synchronize()
+    got, ref = diag[idx], v[idx]
+    assert float((got - ref).abs().max() / ref.abs().max()) < 1e-12
+    assert bool((diag > 0).all())   # SPD: a positive diagonal
+
+
+def test_cg_preconditioners(bklib, small_plan):
+    """The inner CG with and without the Jacobi preconditioner: both reach
+    the FP64 tolerance on the same system."""
+    bk = bklib
+    from omp_bk_gb300.helmholtz import PRECOND_JACOBI, PRECOND_NONE
+    plan, G, M, ustar = small_plan
+    f = torch.empty_like(ustar)
+    plan.apply(G, M, 1.0, ustar, f, prec=bk.PREC_FP64)
+    G32, M32 = G.float(), M.float()
+    its = {}
+    for pc in (PRECOND_NONE, PRECOND_JACOBI):
+        x = torch.zeros_like(ustar)
+        st = plan.cg(G, M, G32, M32, 1.0, f, x, rtol=1e-10, precond=pc)
+        torch.cuda.synchronize()
+        assert st["converged"] and st["relres"] <= 1e-10, (pc, st)
+        assert float(torch.linalg.norm(x - ustar) / torch.linalg.norm(ustar)) < 1e-6
+        its[pc] = st["inner"]
+    assert its[PRECOND_JACOBI] > 0 and its[PRECOND_NONE] > 0
