@@ -750,6 +750,10 @@ def main():
         bk.bk5_apply(P_ORDER, E, D, G, u, v, prec=prec, **kw)
 
     steps, warmup = args.steps, max(args.warmup, 3)
+    # a second sampler over all of this process's GPU work after the input
+    # build (the headline, its forms, the end-to-end leg and the other
+    # configurations: seconds under load), beside the timed region's own
+    clk_all = ClockSampler(local).__enter__()
     with ClockSampler(local) as clk:
         t = time_loop(apply, steps, warmup, world, stream, torch)
     t = max_over_ranks(t, world)
@@ -870,6 +874,8 @@ def main():
             torch.cuda.synchronize()
             torch.cuda.empty_cache()
 
+    clk_all.__exit__(None, None, None)
+    out["clocks_gpu_work"] = dict(clk_all.summary(), note="every GPU phase of this run after the input build")
     if rank == 0 and world == 1 and not args.no_cpu:
         out["cpu_baseline"] = cpu_bk5_run(E, 3, 1)
     if rank == 0:
