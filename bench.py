@@ -673,6 +673,12 @@ def run_helmholtz(args):
             "per_order_mixed_gdofs": (plan.n / m_per32 / 1e6) if m_per32 else None,
             "per_order_fp64_gdofs": (plan.n / m_per64 / 1e6) if m_per64 else None,
             "per_order_kernel_tuned": shape_names,
+            # the configuration's comparison: the persistent mixed-precision
+            # launch against the plain FP64 per-order launches; and like for
+            # like (same precision)
+            "speedup_vs_plain_fp64_per_order": ((plan.n / m_multi / 1e6) / (plan.n / m_per64 / 1e6)) if m_per64 else None,
+            "ratio_multi_vs_per_order_mixed": (m_per32 / m_multi) if m_per32 else None,
+            "ratio_multi_vs_per_order_fp64": (m_per64 / m_multi64) if m_per64 else None,
             "cg": st, "cg_seconds": solve_s, "solution_rel_err": err, "cg_preconditioner": "jacobi",
             "cg_unpreconditioned": cg_runs["none"],
             "cpu_baseline": _cpu_line(units, sec, "BK5 + mass FP64 on the first 64 elements of every order, mean of "
