@@ -687,6 +687,38 @@ __device__ __forceinline__ void load_box(const typename Eng::S* src, int estride
     }
 }
 
+// A pass over the points of `ne` (X, Y, Z) boxes by lines along the first
+// index: one thread per (e, j, k), f(e, j, k, d, b) called with the line's
+// first dense offset d (e*X*Y*Z + j*Z + k) and its first work-box offset b; the
+// callback walks the X points at the compile-time offsets d + i*Y*Z and
+// b + i*WB::PS.  Consecutive threads take consecutive (j, k), so at each i
+// a warp touches what the flat walk's warp touches, but the index arithmetic
+// is paid once per line instead of once per point (the flat walk divides
+// the point index by Q^3, Q^2 and Q at every point).
+template <class WB, int X, int Y, int Z, class F>
+__device__ __forceinline__ void ilines(int ne, int tid, int nt, F f)
+{
+    constexpr int YZ = Y * Z;
+    for (int l = tid; l < ne * YZ; l += nt) {
+        const int e = l / YZ;
+        const int r = l - e * YZ;
+        const int j = r / Z;
+        const int k = r - j * Z;
+        f(e, j, k, e * (X * YZ) + r, e * WB::size + WB::at(0, j, k));
+    }
+}
+
+// load_box by lines along i (ilines).
+template <class Eng, class WB, int X, int Y, int Z>
+__device__ __forceinline__ void load_box_lines(const typename Eng::S* src, typename Eng::V* dst, int ne, int tid,
+                                               int nt)
+{
+    ilines<WB, X, Y, Z>(ne, tid, nt, [&](int, int, int, int d, int b) {
+#pragma unroll
+        for (int i = 0; i < X; ++i) dst[b + i * WB::PS] = Eng::load(src[d + i * Y * Z]);
+    });
+}
+
 // Padded work box -> dense (X, Y, Z) S values.
 template <class Eng, class WB, int X, int Y, int Z>
 __device__ __forceinline__ void store_box(const typename Eng::V* src, typename Eng::S* dst, int estride, int ne,
@@ -846,8 +878,16 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
     const int grp = DPAR ? tid / ntd : 0;
     const int tg = tid - grp * ntd;
     V* QT = DPAR ? W3 : W2;   // qt, and the third transposed term
+    // The per-point passes (load, fluxes, last pass) go by lines, one thread
+    // per line of Q points at compile-time offsets, when the block has one
+    // thread per line of a direction; the direction-parallel blocks (three
+    // threads per line) walk the points flat.
+    constexpr bool LINES = DPAR == 0;
     // 2. u -> W2 (working type, padded)
-    load_box<Eng, WB, Q, Q, Q>(us, Q3, W2, ne, tid, nt);
+    if constexpr (LINES)
+        load_box_lines<Eng, WB, Q, Q, Q>(us, W2, ne, tid, nt);
+    else
+        load_box<Eng, WB, Q, Q, Q>(us, Q3, W2, ne, tid, nt);
     __syncthreads();
     // 3. gradient: qr -> W0 (along i), qs -> W1 (along j), qt (along k) ->
     //    QT (in place into W2 after the other two have read it unless DPAR)
@@ -870,23 +910,9 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
     }
     __syncthreads();
     // 4. fluxes with the symmetric (F = 6) or full (F = 9) factors
-    for (int w = tid; w < ne * Q3; w += nt) {
-        const int e = w / Q3;
-        const int x = w - e * Q3;
-        int i, j, k;
-        if (LAYOUT == 2) {   // walk points in G's (k, i, j) order
-            k = x / (Q * Q);
-            i = (x / Q) % Q;
-            j = x % Q;
-        } else {
-            i = x / (Q * Q);
-            j = (x / Q) % Q;
-            k = x % Q;
-        }
-        const int wi = e * WB::size + WB::at(i, j, k);
+    //    (point wi of the boxes, g(f) the point's factor f)
+    auto flux = [&](const int wi, auto g) {
         const V qr = W0[wi], qs = W1[wi], qt = QT[wi];
-        const GS* ge = gs + e * F * Q3;
-        auto g = [&](int f) { return Eng::load(ge[g_index<Eng, Q, F, LAYOUT>(i, j, f, k)]); };
         A r0, r1, r2;
         if (F == 6) {
             const V g0 = g(0), g1 = g(1), g2 = g(2), g3 = g(3), g4 = g(4), g5 = g(5);
@@ -901,6 +927,47 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
         W0[wi] = Eng::result(r0);
         W1[wi] = Eng::result(r1);
         QT[wi] = Eng::result(r2);
+    };
+    if constexpr (LINES && LAYOUT == 2) {
+        // lines along k, one thread per (e, i, j): G(e, f, k, i, j) of
+        // consecutive threads is consecutive
+        for (int l = tid; l < ne * Q * Q; l += nt) {
+            const int e = l / (Q * Q);
+            const int r = l - e * (Q * Q);   // i*Q + j
+            const int i = r / Q;
+            const int j = r - i * Q;
+            const int wb = e * WB::size + WB::at(i, j, 0);
+            const GS* ge = gs + e * F * Q3 + r;
+#pragma unroll
+            for (int k = 0; k < Q; ++k)
+                flux(wb + k, [&](int f) { return Eng::load(ge[(f * Q + k) * Q * Q]); });
+        }
+    } else if constexpr (LINES) {
+        // lines along i, one thread per (e, j, k)
+        ilines<WB, Q, Q, Q>(ne, tid, nt, [&](int e, int j, int k, int, int b) {
+            const GS* ge = gs + e * F * Q3;
+#pragma unroll
+            for (int i = 0; i < Q; ++i)
+                flux(b + i * WB::PS, [&](int f) { return Eng::load(ge[g_index<Eng, Q, F, LAYOUT>(i, j, f, k)]); });
+        });
+    } else {
+        for (int w = tid; w < ne * Q3; w += nt) {
+            const int e = w / Q3;
+            const int x = w - e * Q3;
+            int i, j, k;
+            if (LAYOUT == 2) {   // walk points in G's (k, i, j) order
+                k = x / (Q * Q);
+                i = (x / Q) % Q;
+                j = x % Q;
+            } else {
+                i = x / (Q * Q);
+                j = (x / Q) % Q;
+                k = x % Q;
+            }
+            const GS* ge = gs + e * F * Q3;
+            flux(e * WB::size + WB::at(i, j, k),
+                 [&](int f) { return Eng::load(ge[g_index<Eng, Q, F, LAYOUT>(i, j, f, k)]); });
+        }
     }
     __syncthreads();
     after_pw();   // the G stage (and u, without a mass term) is free from here
@@ -963,31 +1030,40 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
     //    arithmetic (double for the FP64 engines).  The loop is written twice
     //    (with and without the mass term) so that no point carries the
     //    predicated-off mass arithmetic.
-    auto last_pass = [&](auto with_mass) {
-        for (int w = tid; w < ne * Q3; w += nt) {
-            const int e = w / Q3;
-            const int x = w - e * Q3;
-            const int i = x / (Q * Q);
-            const int j = (x / Q) % Q;
-            const int k = x % Q;
-            const int wi = e * WB::size + WB::at(i, j, k);
-            V res;
-            if constexpr (EO) {
-                if constexpr (HasSum3<Eng>::value) {
-                    res = Eng::sum3(QT[wi], W0[wi], W1[wi]);
-                } else {
-                    A acc = Eng::from(QT[wi]);
-                    Eng::add(acc, W0[wi]);
-                    Eng::add(acc, W1[wi]);
-                    res = Eng::loose(acc);   // store() renormalises
-                }
+    auto last_point = [&](auto with_mass, const int w, const int wi) {
+        V res;
+        if constexpr (EO) {
+            if constexpr (HasSum3<Eng>::value) {
+                res = Eng::sum3(QT[wi], W0[wi], W1[wi]);
             } else {
-                res = W2[wi];
+                A acc = Eng::from(QT[wi]);
+                Eng::add(acc, W0[wi]);
+                Eng::add(acc, W1[wi]);
+                res = Eng::loose(acc);   // store() renormalises
             }
-            S out = Eng::store(res);
-            if constexpr (decltype(with_mass)::value) out += lam * mb[w] * us[w];
-            vb[w] = out;
-            if constexpr (DOT) acc_madd_f(*dot, us[w], out);   // u . A u for CG, compensated
+        } else {
+            res = W2[wi];
+        }
+        S out = Eng::store(res);
+        if constexpr (decltype(with_mass)::value) out += lam * mb[w] * us[w];
+        vb[w] = out;
+        if constexpr (DOT) acc_madd_f(*dot, us[w], out);   // u . A u for CG, compensated
+    };
+    auto last_pass = [&](auto with_mass) {
+        if constexpr (LINES) {
+            ilines<WB, Q, Q, Q>(ne, tid, nt, [&](int, int, int, int d, int b) {
+#pragma unroll
+                for (int i = 0; i < Q; ++i) last_point(with_mass, d + i * Q * Q, b + i * WB::PS);
+            });
+        } else {
+            for (int w = tid; w < ne * Q3; w += nt) {
+                const int e = w / Q3;
+                const int x = w - e * Q3;
+                const int i = x / (Q * Q);
+                const int j = (x / Q) % Q;
+                const int k = x % Q;
+                last_point(with_mass, w, e * WB::size + WB::at(i, j, k));
+            }
         }
     };
     // 7'. (KFUSE) one thread per k line: the transposed k-derivative of the
