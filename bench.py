@@ -586,7 +586,11 @@ def run_helmholtz(args):
     if args.elements:
         orders = [(p, max(1, (2 ** (8 - p)) * args.elements // 64)) for p, _ in orders]
     tuned = tune.tune(orders)
-    plan = tune.make_plan(orders, tuned)
+    # the FP64-storage launches (float-float: the solver's residual and the
+    # FP64 persistent apply) tuned apart: their arithmetic and shared memory
+    # per element differ from the FP32 forms'
+    tuned64 = tune.tune(orders, prec=bk.PREC_FP64)
+    plan = tune.make_plan(orders, tuned, fp64=tuned64)
     G, M = plan.geometry(seed=11)
     G32, M32 = G.float(), M.float()
     ustar = bk.fill_uniform(torch.empty(plan.n, dtype=torch.float64, device="cuda"), 5)
@@ -667,6 +671,7 @@ def run_helmholtz(args):
             "rel_max_err_vs_oracle_fp64_apply": errs, "oracle_elements_per_order": 64,
             "dofs": plan.n, "tiles": plan.ntiles,
             "tuned": {k: tuned.get(k) for k in ("block", "gstage", "tiles", "evaluated", "starts_ms")},
+            "tuned_fp64": {k: tuned64.get(k) for k in ("block", "tiles", "evaluated")},
             "kernel": {bk.KERNEL_SWEEP: "sweep (even-odd)", bk.KERNEL_COLUMN: "column"}[plan.kernel],
             "multi_mixed_gdofs": plan.n / m_multi / 1e6, "multi_fp64_gdofs": plan.n / m_multi64 / 1e6,
             "multi_mixed_column_gdofs": plan.n / m_col / 1e6, "tile_elems_column": tuned_col["tiles"],

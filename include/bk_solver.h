@@ -40,7 +40,8 @@ int bk_hplan_destroy(bk_hplan_t plan);
  * 3: the kernel shape of the applies (BK_KERNEL_SWEEP or BK_KERNEL_COLUMN);
  * 4, 5: shared memory per block of the sweep body's launch for FP64 / FP32
  * storage (a launch needs at most 232448 bytes); 6, 7: the threads and G
- * staging set by bk_hplan_set_shape. */
+ * staging set by bk_hplan_set_shape; 8, 9: the tiles and threads of the
+ * FP64-storage launches (bk_hplan_set_fp64_shape). */
 long long bk_hplan_size(bk_hplan_t plan, int what);
 
 /* The body of the persistent launch: BK_KERNEL_SWEEP (line sweeps in the
@@ -60,6 +61,17 @@ int bk_hplan_set_kernel(bk_hplan_t plan, int kernel);
  * from global memory, prefetched into L2 one tile ahead.  omp_bk_gb300.tune
  * chooses both by measurement.  BK_ERR_ARG for other values. */
 int bk_hplan_set_shape(bk_hplan_t plan, int threads, int gstage);
+
+/* The shape of the sweep body's FP64-storage launches (the float-float and
+ * DFMA applies, among them the solver's FP64 residual) apart from the FP32
+ * storage launches, whose arithmetic costs differ: elems_per_tile[r] for
+ * range r (elems_per_tile * q^2 <= 1024; 0 keeps the range's own) and
+ * threads as in bk_hplan_set_shape.  elems_per_tile NULL returns the FP64
+ * launches to the plan's tiles and threads.  Builds the FP64 tile list on
+ * the device (allocates; synchronizes `stream`, and the device when a list
+ * is replaced).  bk_hplan_set_shape sets the threads of both launches: call
+ * this after it.  BK_ERR_ARG for sizes out of range. */
+int bk_hplan_set_fp64_shape(bk_hplan_t plan, const int* elems_per_tile, int threads, bk_stream_t stream);
 
 /* v = A u for all orders in ONE persistent launch.  prec BK_PREC_FP64 (engine
  * AUTO/FF: float-float, DFMA: native), BK_PREC_MIXED or BK_PREC_FP32 (float

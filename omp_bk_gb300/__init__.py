@@ -46,6 +46,7 @@ EXPORTS = [
     "bk_fill_lognormal", "bk_geom_affine", "bk_coords_affine", "bk_geom_trilinear", "bk_convert",
     "bk3_adjoint", "bk_stream_kernel", "bk_dot_workspace_bytes", "bk_dot", "bk_axpby",
     "bk_hplan_create", "bk_hplan_destroy", "bk_hplan_size", "bk_hplan_set_kernel", "bk_hplan_set_shape",
+    "bk_hplan_set_fp64_shape",
     "bk_hplan_apply", "bk_hplan_cg", "bk_hplan_diagonal",
     "bk_dot_noalloc",
     "bk_host_plan_create", "bk_host_plan_destroy", "bk1_apply_host", "bk3_apply_host", "bk5_apply_host",

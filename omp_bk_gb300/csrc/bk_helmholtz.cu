@@ -510,6 +510,10 @@ struct bk_hplan {
     std::vector<MultiTile> htiles;
     MultiTile* tiles;   // device
     int ntiles;
+    // the FP64-storage sweep launches' own tiles (bk_hplan_set_fp64_shape;
+    // NULL: the plan's tiles)
+    MultiTile* tiles64;
+    int ntiles64;
     long long n;        // values of a vector
     long long ng;       // values of G
     PMulti<double> p_dfma;
@@ -569,6 +573,28 @@ bool fill_eo_params(PMultiEO<C>& P, const bk_hplan& h, const double* const* Dq, 
     return ok;
 }
 
+// The tile list of segments seg[0, nseg): tiles of seg[s].eb elements, the
+// most expensive order first.
+std::vector<MultiTile> make_tiles(const MultiSeg* seg, int nseg)
+{
+    std::vector<int> order(nseg);
+    for (int s = 0; s < nseg; ++s) order[s] = s;
+    for (int a = 0; a < nseg; ++a)
+        for (int b = a + 1; b < nseg; ++b)
+            if (seg[order[b]].q > seg[order[a]].q) std::swap(order[a], order[b]);
+    std::vector<MultiTile> t;
+    for (int s : order) {
+        for (long long e = 0; e < seg[s].E; e += seg[s].eb) {
+            MultiTile x;
+            x.seg = s;
+            x.ne = int((seg[s].E - e) < seg[s].eb ? (seg[s].E - e) : seg[s].eb);
+            x.e_first = e;
+            t.push_back(x);
+        }
+    }
+    return t;
+}
+
 double conv_d(double x) { return x; }
 float conv_f(double x) { return float(x); }
 ff conv_ff(double x) { return EngFF::coef(x); }
@@ -577,9 +603,11 @@ int apply_plan(bk_hplan* h, int eng, const void* G, const void* mass, double lam
                cudaStream_t s)
 {
     if (h->kernel == BK_KERNEL_SWEEP) {
+        const MultiTile* t64 = h->tiles64 ? h->tiles64 : h->tiles;
+        const int n64 = h->tiles64 ? h->ntiles64 : h->ntiles;
         switch (eng) {
-            case 0: return MultiEOLaunch<EngDfma, 256, 2>::run(h->e_dfma, h->tiles, h->ntiles, u, G, mass, lambda, v, s);
-            case 1: return MultiFF::run(h->e_ff, h->tiles, h->ntiles, u, G, mass, lambda, v, s);
+            case 0: return MultiEOLaunch<EngDfma, 256, 2>::run(h->e_dfma, t64, n64, u, G, mass, lambda, v, s);
+            case 1: return MultiFF::run(h->e_ff, t64, n64, u, G, mass, lambda, v, s);
             case 2: return run_f32<EngF32>(h->e_f32, h->tiles, h->ntiles, u, G, mass, lambda, v, s);
             default:
                 return run_f32<EngMixed>(h->e_f32, h->tiles, h->ntiles, u, G, mass, lambda, v, s);
@@ -779,21 +807,7 @@ int bk_hplan_create(bk_hplan_t* out, int norders, const bk_order_range* orders, 
     }
     h->n = uo;
     h->ng = go;
-    // tiles, most expensive order first
-    std::vector<int> order(norders);
-    for (int s = 0; s < norders; ++s) order[s] = s;
-    for (int a = 0; a < norders; ++a)
-        for (int b = a + 1; b < norders; ++b)
-            if (h->seg[order[b]].q > h->seg[order[a]].q) std::swap(order[a], order[b]);
-    for (int s : order) {
-        for (long long e = 0; e < h->seg[s].E; e += h->seg[s].eb) {
-            MultiTile t;
-            t.seg = s;
-            t.ne = int((h->seg[s].E - e) < h->seg[s].eb ? (h->seg[s].E - e) : h->seg[s].eb);
-            t.e_first = e;
-            h->htiles.push_back(t);
-        }
-    }
+    h->htiles = make_tiles(h->seg, norders);
     h->ntiles = int(h->htiles.size());
     fill_params(h->p_dfma, *h, D, conv_d);
     fill_params(h->p_ff, *h, D, conv_ff);
@@ -834,6 +848,7 @@ int bk_hplan_destroy(bk_hplan_t h)
     if (!h) return BK_OK;
     free_graph(h);
     cudaFree(h->tiles);
+    cudaFree(h->tiles64);
     cudaFree(h->r64);
     cudaFree(h->r32);
     cudaFree(h->p32);
@@ -861,7 +876,53 @@ long long bk_hplan_size(bk_hplan_t h, int what)
     if (what == 5) return smem_f32<EngMixed>(h->e_f32);
     if (what == 6) return h->e_f32.block;
     if (what == 7) return h->e_f32.gstage;
+    if (what == 8) return h->tiles64 ? h->ntiles64 : h->ntiles;
+    if (what == 9) return h->e_ff.block;
     return -1;
+}
+
+int bk_hplan_set_fp64_shape(bk_hplan_t h, const int* elems_per_tile, int threads, bk_stream_t stream)
+{
+    if (!h) return BK_ERR_NULL;
+    if (threads != 0 && (threads < 64 || threads > kNT || threads % 32 != 0)) return BK_ERR_ARG;
+    MultiSeg seg[kMultiNQ];
+    for (int s = 0; s < h->nseg; ++s) {
+        seg[s] = h->seg[s];
+        if (elems_per_tile && elems_per_tile[s] != 0) {
+            const int q = seg[s].q;
+            if (elems_per_tile[s] < 0 || elems_per_tile[s] * q * q > kMaxTileLines) return BK_ERR_ARG;
+            seg[s].eb = elems_per_tile[s];
+        }
+    }
+    MultiTile* dev = nullptr;
+    int ntiles = 0;
+    if (elems_per_tile) {
+        const std::vector<MultiTile> t = make_tiles(seg, h->nseg);
+        ntiles = int(t.size());
+        cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+        if (ck(cudaMalloc(&dev, sizeof(MultiTile) * (ntiles > 0 ? ntiles : 1)))) return BK_ERR_CUDA;
+        int rc = BK_OK;
+        if (ntiles > 0)
+            rc = ck(cudaMemcpyAsync(dev, t.data(), sizeof(MultiTile) * ntiles, cudaMemcpyHostToDevice, s));
+        if (rc == BK_OK) rc = ck(cudaStreamSynchronize(s));
+        if (rc != BK_OK) {
+            cudaFree(dev);
+            return rc;
+        }
+    }
+    // the old list may still be read by FP64 applies queued on any stream
+    if (h->tiles64) {
+        if (ck(cudaDeviceSynchronize())) {
+            cudaFree(dev);
+            return BK_ERR_CUDA;
+        }
+        cudaFree(h->tiles64);
+    }
+    h->tiles64 = dev;
+    h->ntiles64 = ntiles;
+    for (int s = 0; s < h->nseg; ++s) h->e_dfma.seg[s].eb = h->e_ff.seg[s].eb = seg[s].eb;
+    h->e_dfma.block = h->e_ff.block = elems_per_tile ? threads : h->e_f32.block;
+    return BK_OK;
 }
 
 int bk_hplan_set_shape(bk_hplan_t h, int threads, int gstage)

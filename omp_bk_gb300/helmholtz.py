@@ -53,8 +53,9 @@ def _declare():
     L.bk_hplan_diagonal.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_void_p, C.c_void_p]
     L.bk_hplan_diagonal.restype = C.c_int
     L.bk_hplan_set_shape.argtypes = [C.c_void_p, C.c_int, C.c_int]
+    L.bk_hplan_set_fp64_shape.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.c_int, C.c_void_p]
     for f in ("bk_hplan_create", "bk_hplan_destroy", "bk_hplan_apply", "bk_hplan_cg", "bk_hplan_set_kernel",
-              "bk_hplan_set_shape"):
+              "bk_hplan_set_shape", "bk_hplan_set_fp64_shape"):
         getattr(L, f).restype = C.c_int
     L._hplan_declared = True
     return L
@@ -107,9 +108,32 @@ class HelmholtzPlan:
         storage, whether G is staged in shared memory (bk_hplan_set_shape)."""
         check(_declare().bk_hplan_set_shape(self.h, int(block), int(gstage)), "bk_hplan_set_shape")
 
+    def set_fp64_shape(self, tiles=None, block: int = 0, stream=None):
+        """Tiles and threads of the FP64-storage launches apart from the FP32
+        ones (bk_hplan_set_fp64_shape): tiles {p: elements per tile} or a list
+        per range (0 keeps the range's own); None returns them to the plan's."""
+        if tiles is None:
+            arr = None
+        else:
+            eb = [int(tiles.get(p, 0)) for p in self.p] if isinstance(tiles, dict) else [int(t) for t in tiles]
+            if len(eb) != len(self.p):
+                raise ValueError("one tile size per range")
+            arr = (C.c_int * len(eb))(*eb)
+        check(_declare().bk_hplan_set_fp64_shape(self.h, arr, int(block), _stream(stream)),
+              "bk_hplan_set_fp64_shape")
+
     @property
     def block(self) -> int:
         return int(_declare().bk_hplan_size(self.h, 6))
+
+    @property
+    def fp64_block(self) -> int:
+        """Threads (per direction group) of the FP64-storage launches."""
+        return int(_declare().bk_hplan_size(self.h, 9))
+
+    @property
+    def fp64_ntiles(self) -> int:
+        return int(_declare().bk_hplan_size(self.h, 8))
 
     @property
     def gstage(self) -> int:

@@ -97,9 +97,13 @@ class _Bench:
         try:
             plan.set_kernel(self.kernel)
             plan.set_shape(block, gstage)
-            # the FP64 apply (the solver's residual) runs on the same tiles:
-            # both forms' stages must fit a block's shared memory
-            if max(plan.smem_bytes(fp64=True), plan.smem_bytes(fp64=False)) > MAX_SMEM:
+            # FP32 storage: the plan's FP64 applies (the solver's residual)
+            # run on the same tiles unless given their own (make_plan's
+            # fp64), so both forms' stages must fit a block's shared memory
+            need = plan.smem_bytes(fp64=True)
+            if self.prec != 0:
+                need = max(need, plan.smem_bytes(fp64=False))
+            if need > MAX_SMEM:
                 ms = float("inf")
             else:
                 if self.data is None:
@@ -195,12 +199,16 @@ def tune(orders, prec=PREC_MIXED, max_elements=65536, reps=5, use_cache=True, ve
     return res
 
 
-def make_plan(orders, tuned, kernel=0):
-    """A HelmholtzPlan over the (p, E) orders in the tuned shape."""
+def make_plan(orders, tuned, kernel=0, fp64=None):
+    """A HelmholtzPlan over the (p, E) orders in the tuned shape; fp64: the
+    shape tuned for FP64 storage (tune(prec=PREC_FP64)), given to the plan's
+    FP64 launches (the solver's residual) apart from the FP32 ones."""
     plan = HelmholtzPlan([(p, E, tuned["tiles"][p]) for p, E in orders])
     if kernel:
         plan.set_kernel(kernel)
     plan.set_shape(tuned.get("block", 0), tuned.get("gstage", 0))
+    if fp64 is not None and plan.kernel != KERNEL_COLUMN:
+        plan.set_fp64_shape(fp64["tiles"], fp64.get("block", 0))
     return plan
 
 

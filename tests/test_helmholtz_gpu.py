@@ -7,6 +7,8 @@ orders p = 2..8) and its mixed-precision CG with FP64 refinement.
   - CG reaches |f - A x| <= 1e-10 |f| (FP64 residual), checked again with the
     oracle's FP64 operator on the host.
 """
+import ctypes as C
+
 import numpy as np
 import pytest
 import torch
@@ -150,9 +152,16 @@ def test_tuner(bklib):
     assert col["block"] == 0
     for p in (2, 5, 8):
         assert col["tiles"][p] in tune.candidates(p) and col["tiles"][p] * (p + 1) ** 2 <= 256
-    plan = tune.make_plan(orders, best)
+    # the FP64-storage launches tuned apart, and given to the plan
+    b64 = tune.tune(orders, prec=bklib.PREC_FP64, max_elements=512, reps=2, use_cache=False)
+    assert b64["block"] in tune.BLOCKS and b64["gstage"] == 0
+    for p in (2, 5, 8):
+        assert b64["tiles"][p] in tune.candidates(p, b64["block"])
+    plan = tune.make_plan(orders, best, fp64=b64)
     try:
         assert plan.block == best["block"] and plan.gstage == best["gstage"]
+        assert plan.fp64_block == b64["block"]
+        assert plan.fp64_ntiles == sum(-(-E // b64["tiles"][p]) for p, E in orders)
         G, M = plan.geometry(seed=8)
         u = bklib.fill_uniform(torch.empty(plan.n, dtype=torch.float64, device="cuda"), 9)
         _check_per_order(bklib, plan, G, M, u, "ff")
@@ -244,6 +253,55 @@ def test_set_shape_arguments(bklib):
             assert L.bk_hplan_set_shape(plan.h, *good) == bklib.BK_OK
         assert plan.block == 256 and plan.gstage == 1
         assert L.bk_hplan_set_kernel(plan.h, bklib.KERNEL_COLUMN) == bklib.BK_ERR_ARG
+    finally:
+        plan.close()
+
+
+def test_fp64_shape(bklib):
+    """The FP64-storage launches on their own tiles and threads
+    (bk_hplan_set_fp64_shape): the same results bit for bit (an element's
+    arithmetic does not depend on its tile), the FP32 launches untouched,
+    the CG (FP64 residual on the FP64 tiles) still converging, and the
+    arguments checked."""
+    from omp_bk_gb300.helmholtz import HelmholtzPlan, _declare
+    L = _declare()
+    plan = HelmholtzPlan([(2, 200, 20), (5, 40, 3), (8, 9, 1)], block=128)
+    try:
+        G, M = plan.geometry(seed=16)
+        u = bklib.fill_uniform(torch.empty(plan.n, dtype=torch.float64, device="cuda"), 17)
+        G32, M32, u32 = G.float(), M.float(), u.float()
+        outs = {}
+        for name in ("plain", "own", "back"):
+            if name == "own":
+                plan.set_fp64_shape({2: 7, 5: 0, 8: 2}, 96)
+                assert plan.fp64_block == 96 and plan.block == 128
+                assert plan.fp64_ntiles == 29 + 14 + 5 and plan.ntiles == 10 + 14 + 9
+            elif name == "back":
+                plan.set_fp64_shape(None)
+                assert plan.fp64_block == 128 and plan.fp64_ntiles == plan.ntiles
+            r = {}
+            for key, prec, eng, GG, MM, uu in (("ff", bklib.PREC_FP64, bklib.ENGINE_FF, G, M, u),
+                                              ("dfma", bklib.PREC_FP64, bklib.ENGINE_DFMA, G, M, u),
+                                              ("mixed", bklib.PREC_MIXED, bklib.ENGINE_AUTO, G32, M32, u32)):
+                v = torch.full_like(uu, float("nan"))
+                plan.apply(GG, MM, 1.0, uu, v, prec=prec, engine=eng)
+                torch.cuda.synchronize()
+                r[key] = v
+            outs[name] = r
+        for key in ("ff", "dfma", "mixed"):
+            assert torch.equal(outs["plain"][key], outs["own"][key]), key
+            assert torch.equal(outs["plain"][key], outs["back"][key]), key
+        plan.set_fp64_shape({2: 7, 5: 2, 8: 2}, 64)
+        f = torch.empty_like(u)
+        plan.apply(G, M, 1.0, u, f, prec=bklib.PREC_FP64)
+        x = torch.zeros_like(u)
+        st = plan.cg(G, M, G32, M32, 1.0, f, x, rtol=1e-10)
+        torch.cuda.synchronize()
+        assert st["converged"] and st["relres"] <= 1e-10, st
+        for bad_tiles, bad_block in (([0, 0, 13], 0), ([-1, 0, 0], 0), ([0, 0, 0], 32), ([0, 0, 0], 100)):
+            arr = (C.c_int * 3)(*bad_tiles)
+            assert L.bk_hplan_set_fp64_shape(plan.h, arr, bad_block, None) == bklib.BK_ERR_ARG
+        assert plan.fp64_block == 64   # a refused shape changes nothing
     finally:
         plan.close()
 
