@@ -10,7 +10,12 @@ the box in a few fixed ways, 32 consecutive work items per warp:
   pointwise  G's (k, i, j) order (BK5 layout 2) or the dense order (BK3);
   sweeps     one thread per line of a direction, all lines of the block's
              elements in turn; each reads its NI inputs and writes its NO
-             outputs at base + n * stride.
+             outputs at base + n * stride;
+  line passes  (BK5 without direction groups, op 52) the load of u and the
+             last pass by i lines (thread per (e, j, k), one access per i)
+             and the pointwise stage by k lines (thread per (e, i, j), one
+             access per k): a warp's 32 lines span elements where the flat
+             walks' 32 points span planes.
 
 A warp instruction on 4-byte values costs the largest number of distinct
 words any of the 32 banks is asked for; on 8-byte values each half warp is
@@ -97,6 +102,20 @@ def _sweep(X, Y, Z, d, NO, eb, zp, ps, es, reads=True, writes=True, nread=None):
     return out
 
 
+def _lines(Q, eb, zp, ps, es, along):
+    """A pass by lines along i (along = 0: thread per (e, j, k)) or along k
+    (along = 2: thread per (e, i, j)), one warp access per point of the
+    line."""
+    out = []
+    for n in range(Q):
+        def f(w, n=n):
+            e, r = divmod(w, Q * Q)
+            a, b = divmod(r, Q)
+            return e * es + (n * ps + a * zp + b if along == 0 else a * ps + b * zp + n)
+        out += _warps(eb * Q * Q, f)
+    return out
+
+
 def walks(op: int, Q: int, eb: int, zp: int, ps: int, es: int):
     """(weight, warps) of one batch of eb elements.  op 5: BK5 (Q points);
     op 3: BK3 (P = Q - 1 nodes, Q points); op 31: BK3's flow fused along k
@@ -120,6 +139,21 @@ def walks(op: int, Q: int, eb: int, zp: int, ps: int, es: int):
         for d in (0, 1):                                 # transposed i, j
             yield 1, _sweep(Q, Q, Q, d, Q, eb, zp, ps, es)
         yield 3, _sweep(Q, Q, Q, 2, Q, eb, zp, ps, es, writes=False)   # last pass: three k lines read
+        return
+    if op == 52:
+        # BK5 FP32 storage (no direction groups): the per-point passes by
+        # lines; the k-direction last pass fused (KFUSE) except at Q = 8
+        kfuse = Q != 8
+        yield 1, _lines(Q, eb, zp, ps, es, 0)           # load u
+        yield 6, _lines(Q, eb, zp, ps, es, 2)           # pointwise
+        for d in range(3):                              # gradient
+            yield 1, _sweep(Q, Q, Q, d, Q, eb, zp, ps, es)
+        for d in ((0, 1) if kfuse else (0, 1, 2)):      # transposed
+            yield 1, _sweep(Q, Q, Q, d, Q, eb, zp, ps, es)
+        if kfuse:                                       # last pass: three k lines read
+            yield 3, _sweep(Q, Q, Q, 2, Q, eb, zp, ps, es, writes=False)
+        else:                                           # last pass by i lines
+            yield 3, _lines(Q, eb, zp, ps, es, 0)
         return
     P = Q - 1
     if op == 3:
@@ -258,6 +292,9 @@ EBS = {
     (3, 8): {3: [12], 4: [8], 5: [8], 6: [3], 7: [3], 8: [1], 9: [3], 10: [1]},
     (31, 4): {3: [16], 4: [8], 5: [6], 6: [4], 7: [3], 8: [1], 9: [1], 10: [1]},
     (51, 4): {2: [12], 3: [12, 14], 4: [8, 8], 5: [4, 5], 6: [3, 3], 7: [2, 2], 9: [1, 1]},
+    # the single-order sweep kernels' batches and the Helmholtz launch's
+    # tuned tiles (q = 3..9: 42, 16, 10, 3, 2, 2, 1 elements)
+    (52, 4): {2: [12], 3: [12, 42], 4: [8, 16], 5: [4, 10], 6: [3], 7: [2], 8: [1, 2], 9: [1]},
 }
 
 
@@ -281,7 +318,7 @@ def search(op: int, Q: int, vbytes: int):
 
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
-    ap.add_argument("--op", type=int, choices=(3, 5, 31, 32, 51), default=5)
+    ap.add_argument("--op", type=int, choices=(3, 5, 31, 32, 51, 52), default=5)
     ap.add_argument("--vbytes", type=int, choices=(4, 8), default=4)
     args = ap.parse_args(argv)
     if args.op == 32:

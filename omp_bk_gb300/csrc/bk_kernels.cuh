@@ -59,21 +59,23 @@ constexpr int box_ps(int q, int vbytes)
 // The BK5 work box (the sweep kernel and the mixed-order Helmholtz kernel):
 // row stride, plane stride and element stride (values) per Q and value size,
 // each the minimum of a model of the warps' shared-memory wavefronts over
-// the box's access patterns (the dense walk of the load and last passes, the
-// pointwise walk in G's (k, i, j) order, and the thread-per-line sweeps of
-// the three directions, reads and writes), averaged over the elements per
-// block that occur (omp_bk_gb300/box_model.py, --op 5).  For small Q a warp
-// spans several elements, so the element stride matters as much as the row
-// and plane strides.  Model wavefronts per access (1 = conflict-free)
-// against the first strides (box_zp, box_ps):
-//   4-byte values, Q = 2..9: 1.21 1.57 1.54 1.56 1.65 1.53 1.36 1.22
-//                   (first:  2.62 2.27 2.00 1.90 1.92 1.70 1.36 1.75)
+// the box's access patterns, averaged over the elements per block that occur
+// (omp_bk_gb300/box_model.py).  For small Q a warp spans several elements,
+// so the element stride matters as much as the row and plane strides.
+// 4-byte values (FP32 storage, no direction groups: the load and last
+// passes by i lines, the pointwise stage by k lines, the thread-per-line
+// sweeps of the three directions; --op 52) and 8-byte values (the dense
+// walks of the direction-parallel blocks and the pointwise walk in G's
+// (k, i, j) order; --op 5).  Model wavefronts per access (1 =
+// conflict-free) against the first strides (box_zp, box_ps):
+//   4-byte values, Q = 2..9: 1.10 1.39 1.20 1.38 1.34 1.36 1.36 1.13
+//                   (first:  3.00 2.53 2.00 1.88 1.75 1.62 1.36 1.75)
 //   8-byte values, Q = 2..9: 1.36 1.62 1.18 1.41 1.44 1.43 1.36 1.23
 //                   (first:  3.09 2.55 2.00 1.80 1.96 1.65 1.36 1.62)
 constexpr int bk5_box(int q, int vbytes, int what)   // what: 0 ZP, 1 PS, 2 element stride
 {
     // {ZP, PS, element stride} for q = 2..9
-    constexpr int t4[8][3] = {{2, 16, 36}, {3, 9, 27}, {6, 24, 97}, {5, 25, 125},
+    constexpr int t4[8][3] = {{2, 15, 36}, {3, 9, 27}, {4, 19, 80}, {5, 25, 125},
                               {7, 42, 252}, {7, 49, 343}, {9, 72, 576}, {9, 81, 729}};
     constexpr int t8[8][3] = {{4, 8, 18}, {3, 9, 27}, {4, 19, 76}, {5, 25, 125},
                               {9, 54, 324}, {7, 49, 343}, {9, 72, 576}, {9, 81, 737}};

@@ -162,7 +162,7 @@ def _search_column(bench, orders, verbose):
             "ms": times[best_lines]}
 
 
-def tune(orders, prec=PREC_MIXED, max_elements=65536, reps=5, use_cache=True, verbose=False, kernel=0):
+def tune(orders, prec=PREC_MIXED, max_elements=65536, reps=15, use_cache=True, verbose=False, kernel=0):
     """The plan shape for the (p, E) orders and the plan body `kernel`
     (KERNEL_AUTO: the plan's default, the even-odd sweep body for GLL):
     {"block": threads per block (0: the largest tile's lines), "gstage": FP32
@@ -170,7 +170,7 @@ def tune(orders, prec=PREC_MIXED, max_elements=65536, reps=5, use_cache=True, ve
     tile}, "ms": the tuned plan's time on the capped orders}."""
     import torch
     ps = sorted(p for p, _ in orders)
-    key = f"{torch.cuda.get_device_name()}|prec{prec}|kernel{kernel}|p{','.join(map(str, ps))}|v2"
+    key = f"{torch.cuda.get_device_name()}|prec{prec}|kernel{kernel}|p{','.join(map(str, ps))}|v3"
     cache = {}
     if use_cache and os.path.exists(CACHE):
         try:

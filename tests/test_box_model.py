@@ -20,7 +20,7 @@ def _table(name):
     return [tuple(int(x) for x in t) for t in re.findall(r"\{\s*(\d+),\s*(\d+),\s*(\d+)\s*\}", m.group(1))]
 
 
-@pytest.mark.parametrize("op,name,vb,q0", [(5, "t4", 4, 2), (5, "t8", 8, 2), (3, "b4", 4, 3), (3, "b8", 8, 3)])
+@pytest.mark.parametrize("op,name,vb,q0", [(52, "t4", 4, 2), (5, "t8", 8, 2), (3, "b4", 4, 3), (3, "b8", 8, 3)])
 def test_tables_valid_and_no_worse(op, name, vb, q0):
     rows = _table(name)
     qs = sorted(box_model.EBS[(op, vb)])
