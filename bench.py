@@ -793,8 +793,12 @@ def main():
     # into 16 chunks whose copies in and out (two copy streams) overlap the
     # applies of the neighbouring chunks
     if not args.no_e2e:
+        # both host arrays pinned (empty_like would not pin the second: its
+        # copies out would then be synchronous, the host in lockstep with the
+        # device, and every host hiccup a gap in the device's work)
         uh = torch.empty(u.numel(), dtype=u.dtype, pin_memory=True)
-        vh = torch.empty_like(uh)
+        vh = torch.empty(u.numel(), dtype=u.dtype, pin_memory=True)
+        assert uh.is_pinned() and vh.is_pinned()
         uh.copy_(u)
         hp = bk.HostPlan(5, P_ORDER, E, prec=prec)
 
