@@ -806,11 +806,9 @@ def main():
             hp.apply(uh, vh, G=G, D=D, engine=engine, layout=args.layout, kernel=kernel, stream=stream)
 
         # the mean per call (the statistic of `value` and of the reference
-        # arm) over at least 50 timed calls after the warm-up, every call's
-        # own time recorded too: the host link is shared with the machine's
-        # other work, and a call now and then takes 40-130 ms instead of
-        # 7.1 (measured in isolation too), which over K = 20 calls would
-        # weigh up to twice as much; no call is left out
+        # arm) over at least 50 timed calls after the warm-up, no call left
+        # out, every call's own time recorded too (the host link is shared
+        # with the machine's other work and stalls a call now and then)
         ncalls = max(steps, 50)
         for _ in range(warmup):
             step_e2e()
