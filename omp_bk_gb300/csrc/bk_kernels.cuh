@@ -710,15 +710,22 @@ __device__ __forceinline__ void ilines(int ne, int tid, int nt, F f)
     }
 }
 
-// load_box by lines along i (ilines).
-template <class Eng, class WB, int X, int Y, int Z>
-__device__ __forceinline__ void load_box_lines(const typename Eng::S* src, typename Eng::V* dst, int ne, int tid,
-                                               int nt)
+// The points n0, n0 + NS, n0 + 2 NS, ... (< Q) of one line, f(n) for each:
+// NS = 1 walks the whole line at compile-time n; with NS > 1 (a line split
+// among NS thread groups, n0 the group) the offsets n * stride are the
+// per-line n0 * stride plus compile-time multiples.
+template <int Q, int NS, class F>
+__device__ __forceinline__ void line_points(const int n0, F f)
 {
-    ilines<WB, X, Y, Z>(ne, tid, nt, [&](int, int, int, int d, int b) {
 #pragma unroll
-        for (int i = 0; i < X; ++i) dst[b + i * WB::PS] = Eng::load(src[d + i * Y * Z]);
-    });
+    for (int m = 0; m < (Q + NS - 1) / NS; ++m) {
+        if (NS == 1) {
+            f(m);
+        } else {
+            const int n = n0 + m * NS;
+            if (n < Q) f(n);
+        }
+    }
 }
 
 // Padded work box -> dense (X, Y, Z) S values.
@@ -880,16 +887,28 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
     const int grp = DPAR ? tid / ntd : 0;
     const int tg = tid - grp * ntd;
     V* QT = DPAR ? W3 : W2;   // qt, and the third transposed term
-    // The per-point passes (load, fluxes, last pass) go by lines, one thread
-    // per line of Q points at compile-time offsets, when the block has one
-    // thread per line of a direction; the direction-parallel blocks (three
-    // threads per line) walk the points flat.
-    constexpr bool LINES = DPAR == 0;
+    // The per-point passes (load, fluxes, last pass) go by lines, the points
+    // of a line at compile-time offsets from its base (ilines, line_points):
+    // one thread per line, or in the direction-parallel blocks each line
+    // split among the three groups (group g takes the points g, g + 3, ..).
+    // A split of Q = 3m + 1 points gives one group a point more than the
+    // others (float-float p = 6, q = 7: 32.6 -> 31.2 GDoF/s when tried), so
+    // those blocks walk the points flat (point w of the batch, its indices
+    // by division), which spreads them evenly over all threads.
+    constexpr bool FLAT = DPAR != 0 && Q % 3 == 1;
+    constexpr int LS = DPAR ? 3 : 1;
+    const int lt = DPAR ? tg : tid;     // the thread's first line
+    const int lnt = DPAR ? ntd : nt;    // threads per line set
+    const int ln0 = DPAR ? grp : 0;     // the thread's first point of a line
+    const bool lact = !DPAR || grp < 3;
     // 2. u -> W2 (working type, padded)
-    if constexpr (LINES)
-        load_box_lines<Eng, WB, Q, Q, Q>(us, W2, ne, tid, nt);
-    else
+    if constexpr (FLAT) {
         load_box<Eng, WB, Q, Q, Q>(us, Q3, W2, ne, tid, nt);
+    } else if (lact) {
+        ilines<WB, Q, Q, Q>(ne, lt, lnt, [&](int, int, int, int d, int b) {
+            line_points<Q, LS>(ln0, [&](int i) { W2[b + i * WB::PS] = Eng::load(us[d + i * Q * Q]); });
+        });
+    }
     __syncthreads();
     // 3. gradient: qr -> W0 (along i), qs -> W1 (along j), qt (along k) ->
     //    QT (in place into W2 after the other two have read it unless DPAR)
@@ -930,29 +949,7 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
         W1[wi] = Eng::result(r1);
         QT[wi] = Eng::result(r2);
     };
-    if constexpr (LINES && LAYOUT == 2) {
-        // lines along k, one thread per (e, i, j): G(e, f, k, i, j) of
-        // consecutive threads is consecutive
-        for (int l = tid; l < ne * Q * Q; l += nt) {
-            const int e = l / (Q * Q);
-            const int r = l - e * (Q * Q);   // i*Q + j
-            const int i = r / Q;
-            const int j = r - i * Q;
-            const int wb = e * WB::size + WB::at(i, j, 0);
-            const GS* ge = gs + e * F * Q3 + r;
-#pragma unroll
-            for (int k = 0; k < Q; ++k)
-                flux(wb + k, [&](int f) { return Eng::load(ge[(f * Q + k) * Q * Q]); });
-        }
-    } else if constexpr (LINES) {
-        // lines along i, one thread per (e, j, k)
-        ilines<WB, Q, Q, Q>(ne, tid, nt, [&](int e, int j, int k, int, int b) {
-            const GS* ge = gs + e * F * Q3;
-#pragma unroll
-            for (int i = 0; i < Q; ++i)
-                flux(b + i * WB::PS, [&](int f) { return Eng::load(ge[g_index<Eng, Q, F, LAYOUT>(i, j, f, k)]); });
-        });
-    } else {
+    if constexpr (FLAT) {
         for (int w = tid; w < ne * Q3; w += nt) {
             const int e = w / Q3;
             const int x = w - e * Q3;
@@ -969,6 +966,31 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
             const GS* ge = gs + e * F * Q3;
             flux(e * WB::size + WB::at(i, j, k),
                  [&](int f) { return Eng::load(ge[g_index<Eng, Q, F, LAYOUT>(i, j, f, k)]); });
+        }
+    } else if (lact) {
+        if constexpr (LAYOUT == 2) {
+            // lines along k, one per (e, i, j): G(e, f, k, i, j) of
+            // consecutive threads is consecutive
+            for (int l = lt; l < ne * Q * Q; l += lnt) {
+                const int e = l / (Q * Q);
+                const int r = l - e * (Q * Q);   // i*Q + j
+                const int i = r / Q;
+                const int j = r - i * Q;
+                const int wb = e * WB::size + WB::at(i, j, 0);
+                const GS* ge = gs + e * F * Q3 + r;
+                line_points<Q, LS>(ln0, [&](int k) {
+                    flux(wb + k, [&](int f) { return Eng::load(ge[(f * Q + k) * Q * Q]); });
+                });
+            }
+        } else {
+            // lines along i, one per (e, j, k)
+            ilines<WB, Q, Q, Q>(ne, lt, lnt, [&](int e, int j, int k, int, int b) {
+                const GS* ge = gs + e * F * Q3;
+                line_points<Q, LS>(ln0, [&](int i) {
+                    flux(b + i * WB::PS,
+                         [&](int f) { return Eng::load(ge[g_index<Eng, Q, F, LAYOUT>(i, j, f, k)]); });
+                });
+            });
         }
     }
     __syncthreads();
@@ -1052,12 +1074,7 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
         if constexpr (DOT) acc_madd_f(*dot, us[w], out);   // u . A u for CG, compensated
     };
     auto last_pass = [&](auto with_mass) {
-        if constexpr (LINES) {
-            ilines<WB, Q, Q, Q>(ne, tid, nt, [&](int, int, int, int d, int b) {
-#pragma unroll
-                for (int i = 0; i < Q; ++i) last_point(with_mass, d + i * Q * Q, b + i * WB::PS);
-            });
-        } else {
+        if constexpr (FLAT) {
             for (int w = tid; w < ne * Q3; w += nt) {
                 const int e = w / Q3;
                 const int x = w - e * Q3;
@@ -1066,6 +1083,10 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
                 const int k = x % Q;
                 last_point(with_mass, w, e * WB::size + WB::at(i, j, k));
             }
+        } else if (lact) {
+            ilines<WB, Q, Q, Q>(ne, lt, lnt, [&](int, int, int, int d, int b) {
+                line_points<Q, LS>(ln0, [&](int i) { last_point(with_mass, d + i * Q * Q, b + i * WB::PS); });
+            });
         }
     };
     // 7'. (KFUSE) one thread per k line: the transposed k-derivative of the
