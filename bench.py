@@ -585,11 +585,15 @@ def run_helmholtz(args):
     orders = hz.config_orders()
     if args.elements:
         orders = [(p, max(1, (2 ** (8 - p)) * args.elements // 64)) for p, _ in orders]
-    tuned = tune.tune(orders)
+    # tuned on the configuration itself (no cap on the elements per order:
+    # a full apply takes a third of a millisecond), so that the tiles fit
+    # its balance of orders
+    emax = max(E for _, E in orders)
+    tuned = tune.tune(orders, max_elements=emax)
     # the FP64-storage launches (float-float: the solver's residual and the
     # FP64 persistent apply) tuned apart: their arithmetic and shared memory
     # per element differ from the FP32 forms'
-    tuned64 = tune.tune(orders, prec=bk.PREC_FP64)
+    tuned64 = tune.tune(orders, prec=bk.PREC_FP64, max_elements=emax)
     plan = tune.make_plan(orders, tuned, fp64=tuned64)
     G, M = plan.geometry(seed=11)
     G32, M32 = G.float(), M.float()

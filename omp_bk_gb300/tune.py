@@ -28,7 +28,7 @@ times the two kernel shapes (one thread per line, one thread per k-column)
 and sets the faster as the library's KERNEL_AUTO choice for that order,
 precision, layout and mass term.
 
-Results are cached per GPU name, precision, body and order set in a JSON file
+Results are cached per GPU name, precision, body and (capped) orders in a JSON file
 (~/.cache/omp_bk_gb300/tune.json, or $BK_TUNE_CACHE)."""
 from __future__ import annotations
 
@@ -169,8 +169,11 @@ def tune(orders, prec=PREC_MIXED, max_elements=65536, reps=15, use_cache=True, v
     G staged (1) or read from global memory (0), "tiles": {p: elements per
     tile}, "ms": the tuned plan's time on the capped orders}."""
     import torch
-    ps = sorted(p for p, _ in orders)
-    key = f"{torch.cuda.get_device_name()}|prec{prec}|kernel{kernel}|p{','.join(map(str, ps))}|v3"
+    capped = [(p, max(1, min(int(E), max_elements))) for p, E in orders]
+    # the key holds the (capped) element counts: the best tiles depend on
+    # the balance of the orders' work
+    sig = ",".join(f"{p}:{E}" for p, E in sorted(capped))
+    key = f"{torch.cuda.get_device_name()}|prec{prec}|kernel{kernel}|{sig}|v4"
     cache = {}
     if use_cache and os.path.exists(CACHE):
         try:
@@ -181,7 +184,6 @@ def tune(orders, prec=PREC_MIXED, max_elements=65536, reps=15, use_cache=True, v
         c = cache[key]
         return {"block": int(c["block"]), "gstage": int(c["gstage"]),
                 "tiles": {int(p): int(e) for p, e in c["tiles"].items()}, "ms": c.get("ms")}
-    capped = [(p, max(1, min(int(E), max_elements))) for p, E in orders]
     bench = _Bench(capped, prec, kernel, reps, torch)
     if kernel == KERNEL_COLUMN:
         res = _search_column(bench, capped, verbose)
