@@ -810,10 +810,12 @@ def main():
             hp.apply(uh, vh, G=G, D=D, engine=engine, layout=args.layout, kernel=kernel, stream=stream)
 
         # the mean per call (the statistic of `value` and of the reference
-        # arm) over at least 50 timed calls after the warm-up, no call left
-        # out, every call's own time recorded too (the host link is shared
-        # with the machine's other work and stalls a call now and then)
-        ncalls = max(steps, 50)
+        # arm) over at least 200 timed calls after the warm-up (1.4 s), no
+        # call left out, every call's own time recorded too: the host link
+        # is shared with the machine's other work and stalls one or two calls
+        # in most sets of 50 by 20-70 ms, so a short window makes the mean
+        # swing between 14 and 19.5 GDoF/s with where the stalls fall
+        ncalls = max(steps, 200)
         for _ in range(warmup):
             step_e2e()
         torch.cuda.synchronize()
