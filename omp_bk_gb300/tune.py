@@ -17,9 +17,11 @@ choices that shape it are timed here with CUDA events on the plan itself
 
 Search: every (B, staging) starts from the tiles whose lines fill B best (at
 most B lines); the best start is then improved one order at a time over the
-counts whose lines fill 1..4 sweeps of B threads (coordinate descent, two
-passes).  Shapes whose FP64 or FP32 launch would not fit a block's shared
-memory are skipped (the solver's FP64 residual runs on the same tiles).  The
+counts whose lines fill 1..8 sweeps of B threads (coordinate descent, two
+passes, each shape timed over 15 applies).  Shapes whose launch would not
+fit a block's shared memory are skipped (tuning FP32 storage, the FP64
+launch on the same tiles too: it runs the solver's residual unless given
+its own shape).  The
 column body (one thread per column, tiles of at most 256 columns) keeps one
 line budget T for the plan, eb_p = max(1, T // (p+1)^2).
 
@@ -44,6 +46,7 @@ BLOCKS = (128, 192, 256)      # threads per block of the sweep body
 GSTAGE = (0, 1)               # FP32 G read from global memory / staged
 LINE_BUDGETS = (64, 96, 128, 160, 192, 256)   # column body
 MAX_TILE_LINES = 1024         # bk_order_range: elems_per_tile * q^2 <= 1024
+SWEEPS = 8                    # sweep-body tiles: lines for 1..SWEEPS sweeps of the block
 MAX_SMEM = 232448             # shared memory of one block, bytes
 
 
@@ -54,13 +57,15 @@ def tiles_for(p: int, lines: int) -> int:
 
 def candidates(p: int, block: int = 0):
     """Elements per tile the tuner tries for order p: with a block of
-    `block` threads, the counts whose lines fill 1..4 sweeps of the block
-    best; without, the column body's line budgets."""
+    `block` threads, the counts whose lines fill 1..SWEEPS sweeps of the
+    block best (a tile's fixed costs, its staging and barriers, spread over
+    more points per thread as it grows); without, the column body's line
+    budgets."""
     if not block:
         return sorted({tiles_for(p, t) for t in LINE_BUDGETS})
     q2 = (p + 1) ** 2
     out = set()
-    for k in range(1, 5):
+    for k in range(1, SWEEPS + 1):
         eb = max(1, (k * block) // q2)
         if eb * q2 <= MAX_TILE_LINES:
             out.add(eb)
