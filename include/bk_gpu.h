@@ -131,9 +131,9 @@ enum bk_gform {
 /* BK5 kernel shapes. */
 enum bk_kernel_shape {
     BK_KERNEL_AUTO = 0,   /* the faster of the two as measured on GB300: the
-                             column kernel for the FP32-storage forms at
-                             p <= 5 with G in the column layout, the sweep
-                             kernel otherwise */
+                             column kernel for the FP32-storage forms with G
+                             in the column layout at p <= 3 and at p = 5
+                             with a mass term, the sweep kernel otherwise */
     BK_KERNEL_SWEEP = 1,  /* one thread per line of the box per 1-D contraction,
                              all intermediates in shared memory */
     BK_KERNEL_COLUMN = 2  /* one thread per k-column of an element, the
@@ -213,8 +213,8 @@ int bk3_adjoint(int p, int64_t E, const double* B, const double* D, const void* 
  * (with_mass 0/1: bk5_apply_ex with or without a mass array): kernel
  * BK_KERNEL_SWEEP or BK_KERNEL_COLUMN fixes the shape AUTO uses there,
  * BK_KERNEL_AUTO restores the built-in choice (the column kernel for FP32
- * storage at p <= 5 with G in the column layout, the sweep kernel
- * otherwise).  A tuner sets these from measurements (omp_bk_gb300.tune:
+ * storage with G in the column layout at p <= 3 and at p = 5 with a mass
+ * term, the sweep kernel otherwise).  A tuner sets these from measurements (omp_bk_gb300.tune:
  * tune_apply); the table is process-wide, so a process should set it before
  * its applies run concurrently with the change.  G split ahead of time
  * (BK_G_FF) always takes the sweep kernel.  No reference counterpart: it

@@ -179,7 +179,7 @@ int bk5_apply_ex(int p, int64_t E, const double* D, const void* G, const void* u
     int kernel = o.kernel;
     if (kernel == BK_KERNEL_AUTO) {
         const int t = g_auto_kernel[p][eng][o.layout][mass != nullptr ? 1 : 0].load(std::memory_order_relaxed);
-        kernel = (o.gform == BK_G_STORAGE && t != 0) ? t : bk5_builtin_auto(p, eng, o.layout);
+        kernel = (o.gform == BK_G_STORAGE && t != 0) ? t : bk5_builtin_auto(p, eng, o.layout, mass != nullptr);
         if (o.gform != BK_G_STORAGE) kernel = BK_KERNEL_SWEEP;
     }
     switch (eng) {
@@ -216,7 +216,7 @@ int bk5_auto_kernel(int p, int prec, int engine, int layout, int with_mass)
     const int eng = engine_of(o);
     if (eng < 0 || layout < 0 || layout > 2 || (with_mass != 0 && with_mass != 1)) return -BK_ERR_PREC;
     const int t = g_auto_kernel[p][eng][layout][with_mass].load(std::memory_order_relaxed);
-    return t != 0 ? t : bk5_builtin_auto(p, eng, layout);
+    return t != 0 ? t : bk5_builtin_auto(p, eng, layout, with_mass != 0);
 }
 
 int bk5_apply_opt(int p, int64_t E, const double* D, const void* G, const void* u, void* v, const bk_options* opt,

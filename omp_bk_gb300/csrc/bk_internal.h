@@ -15,11 +15,14 @@ constexpr int kMaxDevices = 64;
 int current_device();          // cudaGetDevice, or -1
 
 // BK5's built-in choice for BK_KERNEL_AUTO (measured on GB300 at about 2^24
-// DoFs): the column kernel for the FP32-storage engines (2: FP32, 3: mixed)
-// at p <= 5 with G in the column layout, the sweep kernel otherwise.
-inline int bk5_builtin_auto(int p, int eng, int layout)
+// DoFs, mixed form, GDoF/s sweep / column): the column kernel for the
+// FP32-storage engines (2: FP32, 3: mixed) with G in the column layout at
+// p <= 3 (p = 1..3: 100 / 129, 116 / 126, 167 / 174) and at p = 5 with the
+// mass term (131 / 135), the sweep kernel otherwise (p = 4 141 / 138, p = 5
+// without the mass term 147 / 144, p >= 6 by 19-83 %).
+inline int bk5_builtin_auto(int p, int eng, int layout, bool with_mass)
 {
-    return (eng >= 2 && p <= 5 && layout == 2) ? BK_KERNEL_COLUMN : BK_KERNEL_SWEEP;
+    return (eng >= 2 && layout == 2 && (p <= 3 || (p == 5 && with_mass))) ? BK_KERNEL_COLUMN : BK_KERNEL_SWEEP;
 }
 int sm_count();                // SMs of the current device
 DevCtx dev_ctx();              // status word and wait limit of the current device

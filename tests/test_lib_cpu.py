@@ -148,15 +148,20 @@ def test_auto_kernel_table(bklib):
     once set, the rule again after a reset; argument checks (no GPU needed)."""
     bk = bklib
     L = bk.lib()
-    assert bk.bk5_auto_kernel(4, bk.PREC_MIXED, bk.LAYOUT_COLUMN) == bk.KERNEL_COLUMN
-    assert bk.bk5_auto_kernel(7, bk.PREC_MIXED, bk.LAYOUT_COLUMN) == bk.KERNEL_SWEEP
-    assert bk.bk5_auto_kernel(4, bk.PREC_FP64, bk.LAYOUT_COLUMN) == bk.KERNEL_SWEEP
-    assert bk.bk5_auto_kernel(4, bk.PREC_MIXED, bk.LAYOUT_INTERLEAVED) == bk.KERNEL_SWEEP
-    bk.bk5_set_auto_kernel(4, bk.PREC_MIXED, bk.LAYOUT_COLUMN, bk.KERNEL_SWEEP, with_mass=True)
-    assert bk.bk5_auto_kernel(4, bk.PREC_MIXED, bk.LAYOUT_COLUMN, with_mass=True) == bk.KERNEL_SWEEP
-    assert bk.bk5_auto_kernel(4, bk.PREC_MIXED, bk.LAYOUT_COLUMN, with_mass=False) == bk.KERNEL_COLUMN
-    bk.bk5_set_auto_kernel(4, bk.PREC_MIXED, bk.LAYOUT_COLUMN, bk.KERNEL_AUTO, with_mass=True)
-    assert bk.bk5_auto_kernel(4, bk.PREC_MIXED, bk.LAYOUT_COLUMN, with_mass=True) == bk.KERNEL_COLUMN
+    # the built-in rule: column kernel for FP32 storage, column layout, at
+    # p <= 3 and at p = 5 with a mass term
+    for p, mass, want in ((1, False, bk.KERNEL_COLUMN), (3, True, bk.KERNEL_COLUMN), (4, False, bk.KERNEL_SWEEP),
+                          (4, True, bk.KERNEL_SWEEP), (5, False, bk.KERNEL_SWEEP), (5, True, bk.KERNEL_COLUMN),
+                          (7, True, bk.KERNEL_SWEEP)):
+        assert bk.bk5_auto_kernel(p, bk.PREC_MIXED, bk.LAYOUT_COLUMN, with_mass=mass) == want, (p, mass)
+        assert bk.bk5_auto_kernel(p, bk.PREC_FP32, bk.LAYOUT_COLUMN, with_mass=mass) == want, (p, mass)
+    assert bk.bk5_auto_kernel(3, bk.PREC_FP64, bk.LAYOUT_COLUMN) == bk.KERNEL_SWEEP
+    assert bk.bk5_auto_kernel(3, bk.PREC_MIXED, bk.LAYOUT_INTERLEAVED) == bk.KERNEL_SWEEP
+    bk.bk5_set_auto_kernel(3, bk.PREC_MIXED, bk.LAYOUT_COLUMN, bk.KERNEL_SWEEP, with_mass=True)
+    assert bk.bk5_auto_kernel(3, bk.PREC_MIXED, bk.LAYOUT_COLUMN, with_mass=True) == bk.KERNEL_SWEEP
+    assert bk.bk5_auto_kernel(3, bk.PREC_MIXED, bk.LAYOUT_COLUMN, with_mass=False) == bk.KERNEL_COLUMN
+    bk.bk5_set_auto_kernel(3, bk.PREC_MIXED, bk.LAYOUT_COLUMN, bk.KERNEL_AUTO, with_mass=True)
+    assert bk.bk5_auto_kernel(3, bk.PREC_MIXED, bk.LAYOUT_COLUMN, with_mass=True) == bk.KERNEL_COLUMN
     assert L.bk5_set_auto_kernel(9, 0, 0, 2, 0, 1) == bk.BK_ERR_ORDER
     assert L.bk5_set_auto_kernel(3, 7, 0, 2, 0, 1) == bk.BK_ERR_PREC
     assert L.bk5_set_auto_kernel(3, 0, 0, 3, 0, 1) == bk.BK_ERR_PREC
