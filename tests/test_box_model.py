@@ -97,3 +97,21 @@ def test_two_base_line_addressing():
                 la = line(2, e, i, j)
                 for c in (0, 4):
                     assert la(c) % 4 == 0 and [la(c) + q for q in range(4)] == [at(e, i, j, c + q) for q in range(4)]
+
+
+def test_line_walks_table():
+    """The 4-byte BK5 box serves the line walks of the FP32-storage sweep
+    body (op 52): the entries re-searched for them (q = 2, 4) score below
+    the boxes they replaced, and a line pass touches every point of a batch
+    exactly once."""
+    t4 = dict(zip(sorted(box_model.EBS[(52, 4)]), _table("t4")))
+    assert t4[4] == (4, 19, 80) and t4[2] == (2, 15, 36)
+    assert box_model.mean_score(52, 4, 4, *t4[4]) < box_model.mean_score(52, 4, 4, 6, 24, 97)
+    assert box_model.mean_score(52, 2, 4, *t4[2]) < box_model.mean_score(52, 2, 4, 2, 16, 36)
+    for Q, eb in ((3, 12), (4, 8), (8, 2)):
+        zp, ps, es = t4[Q]
+        for along in (0, 2):
+            seen = [a for ws in box_model._lines(Q, eb, zp, ps, es, along) for a in ws if a is not None]
+            want = {e * es + i * ps + j * zp + k for e in range(eb) for i in range(Q) for j in range(Q)
+                    for k in range(Q)}
+            assert len(seen) == eb * Q ** 3 and set(seen) == want, (Q, along)

@@ -167,3 +167,21 @@ def test_auto_kernel_table(bklib):
     assert L.bk5_set_auto_kernel(3, 0, 0, 3, 0, 1) == bk.BK_ERR_PREC
     assert L.bk5_set_auto_kernel(3, 0, 0, 2, 0, 5) == bk.BK_ERR_ARG
     assert L.bk5_auto_kernel(0, 0, 0, 2, 0) == -bk.BK_ERR_ORDER
+
+
+def test_tuner_candidates():
+    """The tile sizes the Helmholtz tuner tries (no GPU): for the sweep body
+    the counts whose lines fill 1..SWEEPS sweeps of the block, each within
+    the plan's line limit; for the column body the line budgets."""
+    from omp_bk_gb300 import tune
+    for p in range(2, 9):
+        q2 = (p + 1) ** 2
+        for block in tune.BLOCKS:
+            c = tune.candidates(p, block)
+            assert c == sorted(set(c)) and c
+            assert all(eb >= 1 and eb * q2 <= tune.MAX_TILE_LINES for eb in c)
+            assert max(1, block // q2) in c
+            full = [max(1, k * block // q2) for k in range(1, tune.SWEEPS + 1)
+                    if max(1, k * block // q2) * q2 <= tune.MAX_TILE_LINES]
+            assert set(full) == set(c)
+        assert tune.candidates(p) == sorted({tune.tiles_for(p, t) for t in tune.LINE_BUDGETS})
