@@ -45,6 +45,7 @@ struct EngDfma {
         s = a + b;
         d = b - a;
     }
+    __device__ static __forceinline__ void sum_diff_loose(const A& a, const A& b, V& s, V& d) { sum_diff(a, b, s, d); }
     static C coef(double d) { return d; }
 };
 
@@ -77,6 +78,11 @@ struct EngFF {
     __device__ static __forceinline__ V vsub_in(V a, V b) { return ff_add_loose(a, ff{-b.hi, -b.lo}); }
     // a + b and b - a of two accumulators
     __device__ static __forceinline__ void sum_diff(const A& a, const A& b, V& s, V& d) { acc_sum_diff(a, b, s, d); }
+    // the same as unevaluated pairs, for outputs that are only summed next
+    __device__ static __forceinline__ void sum_diff_loose(const A& a, const A& b, V& s, V& d)
+    {
+        acc_sum_diff_loose(a, b, s, d);
+    }
     static C coef(double d)
     {
         C c;
@@ -113,6 +119,7 @@ struct EngF32 {
         s = a + b;
         d = b - a;
     }
+    __device__ static __forceinline__ void sum_diff_loose(const A& a, const A& b, V& s, V& d) { sum_diff(a, b, s, d); }
     static C coef(double d) { return static_cast<float>(d); }
 };
 

@@ -173,6 +173,18 @@ __device__ __forceinline__ void acc_sum_diff(const ffacc& a, const ffacc& b, ff&
     two_sum(t, cd, diff.hi, diff.lo);
 }
 
+// a + b and b - a from two compensated accumulators as unevaluated pairs,
+// not renormalised (16 flops for the pair instead of 28): for values that
+// are only summed or stored next, never multiplied (see acc_loose).
+__device__ __forceinline__ void acc_sum_diff_loose(const ffacc& a, const ffacc& b, ff& sum, ff& diff)
+{
+    float e, f;
+    two_sum(a.s, b.s, sum.hi, e);
+    two_sum(b.s, -a.s, diff.hi, f);
+    sum.lo = __fadd_rn(e, __fadd_rn(a.c, b.c));
+    diff.lo = __fadd_rn(f, __fsub_rn(b.c, a.c));
+}
+
 // a + b, both float-float, normalised (TwoSum of the hi parts, lo parts added).
 __device__ __forceinline__ ff ff_add(const ff a, const ff b)
 {

@@ -425,8 +425,9 @@ __device__ __forceinline__ void sweep_eo(const typename Eng::V* in, typename Eng
 
 // sweep_eo with the direction dir (0, 1, 2) given at run time: the line's
 // strides are computed, not constants, so that one code body serves all
-// three directions.
-template <class Eng, class WB, int Q, class EM>
+// three directions.  LOOSE: the outputs as unevaluated pairs (sum_diff_loose),
+// for sweeps whose outputs are only summed next (the transposed derivatives).
+template <class Eng, class WB, int Q, bool LOOSE = false, class EM>
 __device__ __forceinline__ void sweep_eo_dyn(const typename Eng::V* in, typename Eng::V* out, int ne, const EM& m,
                                              int tid, int nt, int dir)
 {
@@ -464,7 +465,10 @@ __device__ __forceinline__ void sweep_eo_dyn(const typename Eng::V* in, typename
             }
             if (Q & 1) Eng::madd(aa, m.c[o], x[H]);
             V s, d;
-            Eng::sum_diff(aa, bb, s, d);   // a + b, b - a
+            if constexpr (LOOSE)
+                Eng::sum_diff_loose(aa, bb, s, d);   // a + b, b - a
+            else
+                Eng::sum_diff(aa, bb, s, d);
             po[o * SD] = s;
             po[(Q - 1 - o) * SD] = d;
         }
@@ -999,8 +1003,9 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
     //    (even-odd) along k on QT
     if constexpr (DPAR == 2) {
         if (grp < 3) {
+            // summed in the last pass, never multiplied: loose pairs
             V* Wg = grp == 0 ? W0 : (grp == 1 ? W1 : W3);
-            sweep_eo_dyn<Eng, WB, Q>(Wg, Wg, ne, eot, tg, ntd, grp);
+            sweep_eo_dyn<Eng, WB, Q, true>(Wg, Wg, ne, eot, tg, ntd, grp);
         }
     } else if constexpr (DPAR == 1) {
         if (grp == 0) sweep_eo<Eng, WB, 0, Q>(W0, W0, ne, eot, tg, ntd);
@@ -1548,7 +1553,8 @@ __global__ void __launch_bounds__(BK3Cfg<Eng, Q, EB, DPAR>::NT)
                 const int grp = tid / Cfg::LINES;
                 if (grp < 3) {
                     V* Wg = grp == 0 ? W0 : (grp == 1 ? W1 : W3);
-                    sweep_eo_dyn<Eng, WB, Q>(Wg, Wg, ne, prm.dtr, tid - grp * Cfg::LINES, Cfg::LINES, grp);
+                    // summed along k next, never multiplied: loose pairs
+                    sweep_eo_dyn<Eng, WB, Q, true>(Wg, Wg, ne, prm.dtr, tid - grp * Cfg::LINES, Cfg::LINES, grp);
                 }
                 __syncthreads();
                 // the three terms summed into W2, then back along k
