@@ -367,7 +367,7 @@ inline bool make_eo(const double* m, bool trans, EOMat<C, Q>& out, Conv conv)
 // direction 2 (BK5's last transposed derivative plus the other two terms).
 // The Q outputs y of one line x through the square even-odd form m (see
 // EOMat); x and y are register arrays of the caller.
-template <class Eng, int Q, class EM>
+template <class Eng, int Q, bool LOOSE = false, class EM>
 __device__ __forceinline__ void eo_line(const typename Eng::V (&x)[Q], typename Eng::V (&y)[Q], const EM& m)
 {
     using V = typename Eng::V;
@@ -388,17 +388,20 @@ __device__ __forceinline__ void eo_line(const typename Eng::V (&x)[Q], typename 
             Eng::madd(bb, m.B[o * H + n], dv[n]);
         }
         if (Q & 1) Eng::madd(aa, m.c[o], x[H]);
-        Eng::sum_diff(aa, bb, y[o], y[Q - 1 - o]);   // a + b, b - a
+        if constexpr (LOOSE)
+            Eng::sum_diff_loose(aa, bb, y[o], y[Q - 1 - o]);   // a + b, b - a
+        else
+            Eng::sum_diff(aa, bb, y[o], y[Q - 1 - o]);
     }
     if constexpr ((Q & 1) != 0) {
         A t = Eng::first(m.r[0], dv[0]);
 #pragma unroll
         for (int n = 1; n < H; ++n) Eng::madd(t, m.r[n], dv[n]);
-        y[H] = Eng::result(t);
+        y[H] = LOOSE ? Eng::loose(t) : Eng::result(t);
     }
 }
 
-template <class Eng, class WB, int DIR, int Q, class EM>
+template <class Eng, class WB, int DIR, int Q, bool LOOSE = false, class EM>
 __device__ __forceinline__ void sweep_eo(const typename Eng::V* in, typename Eng::V* out, int ne, const EM& m,
                                          int tid, int nt)
 {
@@ -417,7 +420,7 @@ __device__ __forceinline__ void sweep_eo(const typename Eng::V* in, typename Eng
         V x[Q], y[Q];
 #pragma unroll
         for (int n = 0; n < Q; ++n) x[n] = in[base + n * SD];
-        eo_line<Eng, Q>(x, y, m);
+        eo_line<Eng, Q, LOOSE>(x, y, m);
 #pragma unroll
         for (int o = 0; o < Q; ++o) out[base + o * SD] = y[o];
     }
@@ -530,7 +533,7 @@ inline bool make_eor(const double* m, int ld, bool trans, int sign, EORMat<C, NO
 
 // The NO outputs y of one line of NI inputs x through the even-odd form m
 // (see EORMat); x and y are register arrays of the caller.
-template <class Eng, int NI, int NO, int SIGN, class EM>
+template <class Eng, int NI, int NO, int SIGN, bool LOOSE = false, class EM>
 __device__ __forceinline__ void eor_line(const typename Eng::V (&x)[NI], typename Eng::V (&y)[NO], const EM& m)
 {
     using V = typename Eng::V;
@@ -547,7 +550,7 @@ __device__ __forceinline__ void eor_line(const typename Eng::V (&x)[NI], typenam
 #pragma unroll
         for (int n = 1; n < HI; ++n) Eng::madd(t, m.r[n], SIGN > 0 ? ev[n] : dv[n]);
         if constexpr (SIGN > 0 && (NI & 1) != 0) Eng::madd(t, m.rm, x[HI]);
-        y[HO] = Eng::result(t);
+        y[HO] = LOOSE ? Eng::loose(t) : Eng::result(t);
     }
 #pragma unroll
     for (int o = 0; o < HO; ++o) {
@@ -558,17 +561,21 @@ __device__ __forceinline__ void eor_line(const typename Eng::V (&x)[NI], typenam
             Eng::madd(bb, m.B[o * HI + n], dv[n]);
         }
         if constexpr ((NI & 1) != 0) Eng::madd(aa, m.c[o], x[HI]);
-        if constexpr (SIGN > 0) {
-            Eng::sum_diff(bb, aa, y[o], y[NO - 1 - o]);   // b + a, a - b
+        if constexpr (SIGN > 0 && LOOSE) {
+            Eng::sum_diff_loose(bb, aa, y[o], y[NO - 1 - o]);   // b + a, a - b
+        } else if constexpr (SIGN > 0) {
+            Eng::sum_diff(bb, aa, y[o], y[NO - 1 - o]);
+        } else if constexpr (LOOSE) {
+            Eng::sum_diff_loose(aa, bb, y[o], y[NO - 1 - o]);   // a + b, b - a
         } else {
-            Eng::sum_diff(aa, bb, y[o], y[NO - 1 - o]);   // a + b, b - a
+            Eng::sum_diff(aa, bb, y[o], y[NO - 1 - o]);
         }
     }
 }
 
 // Even-odd sweep of direction DIR of the (X, Y, Z) box into extent NO along
 // DIR (see EORMat; in == out allowed).
-template <class Eng, class WB, int DIR, int X, int Y, int Z, int NO, int SIGN, class EM>
+template <class Eng, class WB, int DIR, int X, int Y, int Z, int NO, int SIGN, bool LOOSE = false, class EM>
 __device__ __forceinline__ void sweep_eor(const typename Eng::V* in, typename Eng::V* out, int ne, const EM& m,
                                           int tid, int nt)
 {
@@ -589,7 +596,7 @@ __device__ __forceinline__ void sweep_eor(const typename Eng::V* in, typename En
 #pragma unroll
             for (int n = 0; n < NI; ++n) x[n] = in[la(n)];
         }
-        eor_line<Eng, NI, NO, SIGN>(x, y, m);
+        eor_line<Eng, NI, NO, SIGN, LOOSE>(x, y, m);
         if constexpr (DIR == 2) {
             line_store<WB, NO>(out, la, y);
         } else {
@@ -1008,15 +1015,16 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
             sweep_eo_dyn<Eng, WB, Q, true>(Wg, Wg, ne, eot, tg, ntd, grp);
         }
     } else if constexpr (DPAR == 1) {
-        if (grp == 0) sweep_eo<Eng, WB, 0, Q>(W0, W0, ne, eot, tg, ntd);
-        else if (grp == 1) sweep_eo<Eng, WB, 1, Q>(W1, W1, ne, eot, tg, ntd);
-        else if (grp == 2) sweep_eo<Eng, WB, 2, Q>(W3, W3, ne, eot, tg, ntd);
+        if (grp == 0) sweep_eo<Eng, WB, 0, Q, true>(W0, W0, ne, eot, tg, ntd);
+        else if (grp == 1) sweep_eo<Eng, WB, 1, Q, true>(W1, W1, ne, eot, tg, ntd);
+        else if (grp == 2) sweep_eo<Eng, WB, 2, Q, true>(W3, W3, ne, eot, tg, ntd);
     } else if constexpr (EO) {
-        sweep_eo<Eng, WB, 0, Q>(W0, W0, ne, eot, tid, nt);
-        sweep_eo<Eng, WB, 1, Q>(W1, W1, ne, eot, tid, nt);
+        // summed in the last pass, never multiplied: loose pairs
+        sweep_eo<Eng, WB, 0, Q, true>(W0, W0, ne, eot, tid, nt);
+        sweep_eo<Eng, WB, 1, Q, true>(W1, W1, ne, eot, tid, nt);
         // the k direction: in registers in the last pass (KFUSE, below), or
         // here
-        if constexpr (!KFUSE) sweep_eo<Eng, WB, 2, Q>(W2, W2, ne, eot, tid, nt);
+        if constexpr (!KFUSE) sweep_eo<Eng, WB, 2, Q, true>(W2, W2, ne, eot, tid, nt);
     } else {
         sweep<Eng, WB, 0, Q, Q, Q, Q>(W0, W0, ne, Dt, tid, nt);
         sweep<Eng, WB, 1, Q, Q, Q, Q>(W1, W1, ne, Dt, tid, nt);
@@ -1100,7 +1108,7 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
     auto kline_last = [&](auto with_mass) {
         kline_pass<Eng, WB, Q, Q>(QT, ne, tid, nt, [&](int e, int i, int j, const V (&x)[Q], const BoxLine<WB, 2>& la) {
             V t[Q];
-            eo_line<Eng, Q>(x, t, eot);
+            eo_line<Eng, Q, true>(x, t, eot);   // summed next: loose pairs
             const int w0 = e * Q3 + (i * Q + j) * Q;
 #pragma unroll
             for (int o = 0; o < Q; ++o) {
@@ -1325,7 +1333,7 @@ __global__ void __launch_bounds__(BK1Cfg<Eng, Q, EB>::NT)
             if constexpr (kDirectIO) {
                 interp0_to_dense<Eng, WB, P, Q>(W1, v + e0 * P3, ne, prm.bb, tid, nt);  // -> v
             } else {
-                sweep_eor<Eng, WB, 0, Q, P, P, P, +1>(W1, W0, ne, prm.bb, tid, nt);   // (P,P,P)
+                sweep_eor<Eng, WB, 0, Q, P, P, P, +1, true>(W1, W0, ne, prm.bb, tid, nt);   // (P,P,P), stored next
                 __syncthreads();
                 store_box<Eng, WB, P, P, P>(W0, v + e0 * P3, P3, ne, tid, nt);
             }
@@ -1566,15 +1574,16 @@ __global__ void __launch_bounds__(BK3Cfg<Eng, Q, EB, DPAR>::NT)
                 __syncthreads();
                 sweep_eor<Eng, WB, 2, Q, Q, Q, P, +1>(W2, W0, ne, prm.bb, tid, nt);   // (Q,Q,P)
             } else {
-                sweep_eor<Eng, WB, 0, Q, Q, Q, Q, -1>(W0, W0, ne, prm.dtr, tid, nt);
-                sweep_eor<Eng, WB, 1, Q, Q, Q, Q, -1>(W1, W1, ne, prm.dtr, tid, nt);
+                // summed along k next, never multiplied: loose pairs
+                sweep_eor<Eng, WB, 0, Q, Q, Q, Q, -1, true>(W0, W0, ne, prm.dtr, tid, nt);
+                sweep_eor<Eng, WB, 1, Q, Q, Q, Q, -1, true>(W1, W1, ne, prm.dtr, tid, nt);
                 __syncthreads();
                 // along k in registers: the transposed derivative of the
                 // third flux, plus the other two terms, back to the nodes;
                 // (Q,Q,P) into W0 (each line reads its own W0 values first)
                 kline_pass<Eng, WB, Q, Q>(W3, ne, tid, nt, [&](int, int, int, const V (&x)[Q], const BoxLine<WB, 2>& la) {
                     V t[Q], sv[Q], z[P];
-                    eor_line<Eng, Q, Q, -1>(x, t, prm.dtr);
+                    eor_line<Eng, Q, Q, -1, true>(x, t, prm.dtr);   // summed next: loose pairs
                     sum_line(t, sv, la);
                     eor_line<Eng, Q, P, +1>(sv, z, prm.bb);
                     line_store<WB, P>(W0, la, z);
@@ -1586,7 +1595,7 @@ __global__ void __launch_bounds__(BK3Cfg<Eng, Q, EB, DPAR>::NT)
             if constexpr (kDirectIO) {
                 interp0_to_dense<Eng, WB, P, Q>(W1, v + e0 * P3, ne, prm.bb, tid, nt);  // -> v
             } else {
-                sweep_eor<Eng, WB, 0, Q, P, P, P, +1>(W1, W0, ne, prm.bb, tid, nt);   // (P,P,P)
+                sweep_eor<Eng, WB, 0, Q, P, P, P, +1, true>(W1, W0, ne, prm.bb, tid, nt);   // (P,P,P), stored next
                 __syncthreads();
                 store_box<Eng, WB, P, P, P>(W0, v + e0 * P3, P3, ne, tid, nt);
             }
