@@ -366,7 +366,9 @@ inline bool make_eo(const double* m, bool trans, EOMat<C, Q>& out, Conv conv)
 // see EOMat.  When ADD is set, out(o) = M x + X(o) + Y(o) for the lines of
 // direction 2 (BK5's last transposed derivative plus the other two terms).
 // The Q outputs y of one line x through the square even-odd form m (see
-// EOMat); x and y are register arrays of the caller.
+// EOMat); x and y are register arrays of the caller.  LOOSE: the outputs
+// as unevaluated pairs (Eng::sum_diff_loose), for outputs that are only
+// summed or stored next, never multiplied.
 template <class Eng, int Q, bool LOOSE = false, class EM>
 __device__ __forceinline__ void eo_line(const typename Eng::V (&x)[Q], typename Eng::V (&y)[Q], const EM& m)
 {
@@ -532,7 +534,8 @@ inline bool make_eor(const double* m, int ld, bool trans, int sign, EORMat<C, NO
 }
 
 // The NO outputs y of one line of NI inputs x through the even-odd form m
-// (see EORMat); x and y are register arrays of the caller.
+// (see EORMat); x and y are register arrays of the caller.  LOOSE as for
+// eo_line.
 template <class Eng, int NI, int NO, int SIGN, bool LOOSE = false, class EM>
 __device__ __forceinline__ void eor_line(const typename Eng::V (&x)[NI], typename Eng::V (&y)[NO], const EM& m)
 {
