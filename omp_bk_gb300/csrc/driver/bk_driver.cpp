@@ -1,6 +1,7 @@
 // bk_driver.cpp -- the reference drivers' command line on the GB300 kernels.
 //
 //   bk_cuda BK1|BK3|BK5 <p> [nelmt] [ntests]
+//   bk_cuda BK1_ff <p> [nelmt] [ntests]      (openmp/BK1_ff.cpp: run_bk1_ff)
 //
 // Keeps the surface of openmp/BK1.cpp, BK3.cpp and BK5.cpp and of the variant
 // harnesses: the positional arguments and defaults of bk::parse_args
@@ -222,18 +223,141 @@ const Variant kVariants[] = {
         }                                                                                      \
     } while (0)
 
+// ||x - ref|| / ||ref|| in double (the reference's relative_error,
+// openmp/BK1_ff.cpp:751-764)
+double rel_l2(const std::vector<double>& x, const std::vector<double>& ref)
+{
+    double num = 0, den = 0;
+    for (size_t i = 0; i < ref.size(); ++i) {
+        const double d = x[i] - ref[i];
+        num += d * d;
+        den += ref[i] * ref[i];
+    }
+    return std::sqrt(num) / std::sqrt(den);
+}
+
+// BK1_ff <p> [nelmt] [ntests]: the precision harness of openmp/BK1_ff.cpp
+// (run_test :799-845, main :847-862) on the GPU kernels.  The same data (the
+// double test basis, in = 3, JxW = 1, or BK_RANDOM's LCG) through BK1 in
+// double (the DFMA engine), float (FP32 storage, the double data rounded)
+// and float-float (the FF engine); one row per precision with GDoF/s, GB/s
+// and the norm; the float and float-float relative L2 errors against the
+// double result; ok or FAIL at BK_TOL (default 1e-10) for the float-float
+// result, and the exit code 0 or 1.  The reference's ff-teams and ff-plane
+// rows are loop organisations of the same float-float arithmetic on the
+// host; the GPU has one float-float kernel, reported once.
+int run_bk1_ff(int argc, char** argv)
+{
+    const int p = (argc > 2) ? std::atoi(argv[2]) : 2;
+    const size_t nelmt = (argc > 3) ? size_t(std::atoll(argv[3])) : (size_t(1) << 19);
+    const int ntests = (argc > 4) ? std::atoi(argv[4]) : 5;
+    if (p < 1 || p > 8) {
+        std::fprintf(stderr, "unsupported polynomial order p = %d (supported: 1..8)\n", p);
+        return 1;
+    }
+    const bool random_data = env_set("BK_RANDOM");
+    const double tol = std::atof(env_str("BK_TOL", "1e-10").c_str());
+    const int nq = p + 2, nm = nq - 1;
+    const size_t n_in = nelmt * size_t(nm) * nm * nm, n_geo = nelmt * size_t(nq) * nq * nq;
+    const std::vector<double> B = test_basis(nm, nq, false);
+    std::vector<double> in(n_in, 3.0), jxw(n_geo, 1.0);
+    if (random_data) fill_random(in, jxw);
+    std::printf("SumFactorization -> nelmt = %zu nq = %d data = %s fma = hardware\n", nelmt, nq,
+                random_data ? "random" : "constant");
+    void *d_in = nullptr, *d_geo = nullptr, *d_out = nullptr;
+    CK(cudaMalloc(&d_in, n_in * 8));
+    CK(cudaMalloc(&d_geo, n_geo * 8));
+    CK(cudaMalloc(&d_out, n_in * 8));
+    cudaStream_t s;
+    CK(cudaStreamCreate(&s));
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    const Variant rows[] = {{"double", BK_PREC_FP64, BK_ENGINE_DFMA},
+                            {"float", BK_PREC_FP32, BK_ENGINE_AUTO},
+                            {"float-float", BK_PREC_FP64, BK_ENGINE_FF}};
+    std::vector<double> out[3];
+    int status = BK_OK;
+    for (int r = 0; r < 3; ++r) {
+        const Variant& v = rows[r];
+        const bool f32 = v.prec == BK_PREC_FP32;
+        const size_t vb = f32 ? 4 : 8;
+        auto upload = [&](void* dst, const std::vector<double>& h) {
+            if (f32) {
+                std::vector<float> t(h.begin(), h.end());
+                CK(cudaMemcpy(dst, t.data(), t.size() * 4, cudaMemcpyHostToDevice));
+            } else {
+                CK(cudaMemcpy(dst, h.data(), h.size() * 8, cudaMemcpyHostToDevice));
+            }
+        };
+        upload(d_in, in);
+        upload(d_geo, jxw);
+        bk_options o = bk_default_options();
+        o.prec = v.prec;
+        o.engine = v.engine;
+        // float: the double basis rounded, as the reference's float row sees it
+        std::vector<double> Bv = B;
+        if (f32)
+            for (double& b : Bv) b = double(float(b));
+        auto run = [&]() { return bk1_apply_opt(p, int64_t(nelmt), Bv.data(), d_geo, d_in, d_out, &o, s); };
+        int rc = run();
+        if (rc != BK_OK) {
+            std::fprintf(stderr, "%s: status %d\n", v.name, rc);
+            status = rc;
+            break;
+        }
+        float best = 1e30f;
+        for (int t = 0; t < ntests; ++t) {
+            CK(cudaEventRecord(e0, s));
+            run();
+            CK(cudaEventRecord(e1, s));
+            CK(cudaEventSynchronize(e1));
+            float ms = 0;
+            CK(cudaEventElapsedTime(&ms, e0, e1));
+            best = std::min(best, ms);
+        }
+        int st = 0;
+        bk_device_status(&st, 1, s);
+        if (st != BK_OK) status = st;
+        out[r].resize(n_in);
+        if (f32) {
+            std::vector<float> t(n_in);
+            CK(cudaMemcpy(t.data(), d_out, n_in * 4, cudaMemcpyDeviceToHost));
+            std::copy(t.begin(), t.end(), out[r].begin());
+        } else {
+            CK(cudaMemcpy(out[r].data(), d_out, n_in * 8, cudaMemcpyDeviceToHost));
+        }
+        const double sec = best * 1e-3;
+        double nrm = 0;
+        for (double x : out[r]) nrm += x * x;
+        std::printf("%-12s GDoF/s = %9.4g GB/s = %9.4g norm = %.10g\n", v.name, 1e-9 * n_in / sec,
+                    1e-9 * double(vb) * (2.0 * n_in + n_geo) / sec, std::sqrt(nrm));
+    }
+    cudaFree(d_in);
+    cudaFree(d_geo);
+    cudaFree(d_out);
+    if (status != BK_OK) return 1;
+    const double err_float = rel_l2(out[1], out[0]);
+    const double err_ff = rel_l2(out[2], out[0]);
+    const bool ok = err_ff <= tol;
+    std::printf("float        rel. error vs double = %g\n", err_float);
+    std::printf("%s: float-float rel. error vs double = %g (tol = %g)\n", ok ? "ok" : "FAIL", err_ff, tol);
+    return ok ? 0 : 1;
+}
+
 }  // namespace
 
 int main(int argc, char** argv)
 {
     if (argc < 2) {
-        std::fprintf(stderr, "usage: %s BK1|BK3|BK5 <p> [nelmt] [ntests]\n", argv[0]);
+        std::fprintf(stderr, "usage: %s BK1|BK3|BK5|BK1_ff <p> [nelmt] [ntests]\n", argv[0]);
         return 1;
     }
     const std::string op = argv[1];
+    if (op == "BK1_ff") return run_bk1_ff(argc, argv);
     const int bk = (op == "BK1") ? 1 : (op == "BK3") ? 3 : (op == "BK5") ? 5 : 0;
     if (bk == 0) {
-        std::fprintf(stderr, "unknown operator %s (BK1, BK3 or BK5)\n", op.c_str());
+        std::fprintf(stderr, "unknown operator %s (BK1, BK3, BK5 or BK1_ff)\n", op.c_str());
         return 1;
     }
     // bk::parse_args: <order> [nelmt] [ntests], defaults 2 (3 for BK5), 2^19, 5

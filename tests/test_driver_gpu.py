@@ -52,3 +52,44 @@ def test_driver_random_data_check():
     r = subprocess.run([DRIVER, "BK3", "6", "37", "2"], env=env, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0 and "FAIL" not in r.stdout, r.stdout + r.stderr
     assert len(re.findall(r"relerr = (\S+)", r.stdout)) == 2
+
+
+def _run_ff(p, nelmt, extra=None):
+    env = dict(os.environ)
+    env.pop("BK_RANDOM", None)
+    env.update(extra or {})
+    r = subprocess.run([DRIVER, "BK1_ff", str(p), str(nelmt), "2"], env=env, capture_output=True, text=True,
+                       timeout=300)
+    return r.returncode, r.stdout + r.stderr
+
+
+@pytest.mark.parametrize("p", [2, 5, 7])
+def test_bk1_ff_harness(golden, p):
+    """BK1_ff mode (openmp/BK1_ff.cpp): double, float and float-float rows on
+    the same data, the double and float-float norms equal to the reference's
+    FP64 known answer, the float-float error against double below BK_TOL
+    (default 1e-10) with "ok" and exit code 0."""
+    _, meta = golden
+    E = meta["E_const"]
+    rc, out = _run_ff(p, E)
+    assert rc == 0, out
+    assert re.search(rf"^SumFactorization -> nelmt = {E} nq = {p + 2} data = constant", out, re.M), out
+    rows = dict((n, (float(g), float(nrm))) for n, g, nrm in
+                re.findall(r"^(double|float-float|float)\s+GDoF/s =\s*(\S+) GB/s =\s*\S+ norm = (\S+)", out, re.M))
+    assert set(rows) == {"double", "float", "float-float"}, out
+    ref = meta["norms"][f"bk1_p{p}_const_f64"]
+    assert abs(rows["double"][1] - ref) <= 1e-9 * abs(ref)
+    assert abs(rows["float-float"][1] - ref) <= 1e-9 * abs(ref)
+    assert abs(rows["float"][1] - ref) <= 1e-5 * abs(ref)
+    m = re.search(r"^ok: float-float rel\. error vs double = (\S+) \(tol = 1e-10\)", out, re.M)
+    assert m and float(m.group(1)) <= 1e-10, out
+    assert float(re.search(r"^float\s+rel\. error vs double = (\S+)", out, re.M).group(1)) < 1e-5
+
+
+def test_bk1_ff_random_and_tolerance():
+    """BK_RANDOM data passes; a tolerance below the float-float error (set on
+    the host, nothing faults) prints FAIL and exits 1."""
+    rc, out = _run_ff(3, 300, {"BK_RANDOM": "1"})
+    assert rc == 0 and "data = random" in out and re.search(r"^ok: ", out, re.M), out
+    rc, out = _run_ff(3, 300, {"BK_RANDOM": "1", "BK_TOL": "1e-30"})
+    assert rc == 1 and re.search(r"^FAIL: float-float rel\. error vs double = \S+ \(tol = 1e-30\)", out, re.M), out
