@@ -448,3 +448,28 @@ def test_bk1_transposed_jxw_apply(bklib, p, prec, basis):
     assert torch.equal(v0, v1)
     tol = TOL64 if prec == bklib.PREC_FP64 else 1e-5
     assert oracle.rel_maxdiff(host(v1), oracle.bk1(q, E, B, jxw, u)) < tol
+
+
+@pytest.mark.parametrize("p", [4, 7])
+@pytest.mark.parametrize("h", [1.0 / 64, 1.0 / 16])
+def test_bk5_fp64_smooth_field(bklib, p, h):
+    """The FP64 forms on a smooth field, u = sin(pi x) sin(pi y) sin(pi z)
+    at the nodes of the jittered trilinear mesh: the operator's image
+    cancels (v is a second difference, |v| ~ h^2 |u| ... h |u|), which
+    amplifies the float-float engine's 2^-48 rounding of the terms; measured
+    3e-13 to 4e-13 at p = 7 (DFMA 1e-14), still inside the 1e-12 bound."""
+    import math
+    Q, E, n = p + 1, 1024, 256
+    D, x, w = bklib.bk5_matrices(p)
+    G = torch.empty(E * 6 * Q ** 3, dtype=torch.float64, device="cuda")
+    X = torch.empty(E * Q ** 3 * 3, dtype=torch.float64, device="cuda")
+    bklib.geom_trilinear(Q, E, 16, 16, x, w, 2, h, 0.15, G=G, layout=bklib.LAYOUT_COLUMN, coords=X)
+    xyz = X.view(-1, 3)
+    u = (torch.sin(math.pi * xyz[:, 0]) * torch.sin(math.pi * xyz[:, 1]) * torch.sin(math.pi * xyz[:, 2])).contiguous()
+    g = host(G[: n * 6 * Q ** 3]).reshape(n, 6, Q, Q, Q).transpose(0, 3, 4, 1, 2).copy().ravel()
+    ref = oracle.bk5(Q, n, np.asarray(D), g, host(u[: n * Q ** 3]))
+    for eng in (bklib.ENGINE_FF, bklib.ENGINE_DFMA):
+        v = torch.full_like(u, float("nan"))
+        bklib.bk5_apply(p, E, D, G, u, v, prec=bklib.PREC_FP64, engine=eng, layout=bklib.LAYOUT_COLUMN)
+        torch.cuda.synchronize()
+        assert oracle.rel_maxdiff(host(v[: n * Q ** 3]), ref) < TOL64, (eng, p, h)
