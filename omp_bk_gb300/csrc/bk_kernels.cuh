@@ -848,8 +848,9 @@ struct BK5Cfg {
 // the sum compensated (float-float: about 44 bits).  after_pw: called by every
 // thread after the pointwise stage, when the G stage is no longer read (nor
 // u, unless the mass term or dot reads it at the end).  Ends with a block
-// barrier (after which the stages may be reused).  GS: the type G is stored
-// in (the storage type, or float-float pairs split ahead of time).
+// barrier (after which the stages may be reused) unless end_sync is false.
+// GS: the type G is stored in (the storage type, or float-float pairs split
+// ahead of time).
 //
 // Stages: load u into a box; gradient (three sweeps); pointwise fluxes;
 // transposed sweeps; last pass (sum of the three terms, mass term, store).
@@ -877,7 +878,8 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
                                                 typename Eng::V* W2, typename Eng::V* W3, int ne, int tid, int nt,
                                                 typename Eng::S* __restrict__ vb,
                                                 const typename Eng::S* __restrict__ mb, double lambda,
-                                                ffacc* dot = nullptr, AfterPw after_pw = AfterPw())
+                                                ffacc* dot = nullptr, AfterPw after_pw = AfterPw(),
+                                                const bool end_sync = true)
 {
     static_assert(!DOT || sizeof(typename Eng::S) == 4, "the fused dot product is for FP32 storage");
     static_assert(!DPAR || EO, "direction-parallel sweeps need the even-odd form");
@@ -1142,7 +1144,9 @@ __device__ __forceinline__ void bk5_sweep_batch(const typename Eng::C* __restric
         else
             last_pass(std::false_type{});
     }
-    __syncthreads();
+    // end_sync (uniform): false when the caller's next step is a block
+    // barrier anyway and nothing before it writes what the last pass read
+    if (end_sync) __syncthreads();
 }
 
 // The block walks batches bt = blockIdx.x, + gridDim.x, ...  One stage buffer:
@@ -1222,8 +1226,12 @@ __global__ void __launch_bounds__(BK5Cfg<Eng, Q, EB, F, LAYOUT, DPAR>::NT)
                 if (mass == nullptr) issue_u(next);
             }
         };
+        // the next batch's wait ends with a block barrier before anything
+        // writes the boxes or the stage again, except the copy of u that
+        // follows a batch with the mass term (its last pass reads u): only
+        // that batch ends with its own barrier
         bk5_sweep_batch<Eng, Q, F, LAYOUT, EO, DPAR>(prm.D, prm.eo, prm.eot, ub, gb, W0, W1, W2, W3, ne, tid, nt,
-                                                     v + e0 * Q3, mb, lambda, nullptr, early);
+                                                     v + e0 * Q3, mb, lambda, nullptr, early, mass != nullptr);
         if (mass != nullptr && next < nbatch) issue_u(next);
     }
 }
