@@ -284,11 +284,13 @@ inline void multi_eo_smem(const MultiSeg* seg, int nseg, int& u_bytes, int& g_by
 // tuner picks the faster for a plan.
 //
 // Staging, by mode:
-//   FP32, G direct:  u and mass double-buffered; at the top of tile t the
-//                    next tile's u and mass go into the other buffer (its
-//                    barrier gets the bytes and the arrival) and its G is
-//                    prefetched into L2 (one bulk prefetch), so the pointwise
-//                    stage's loads wait on L2 rather than HBM.
+//   FP32, G direct:  u and mass double-buffered; right after tile t's wait
+//                    (whose block barrier also ends tile t-1's last pass, so
+//                    a tile needs no barrier of its own at its end) the next
+//                    tile's u and mass go into the other buffer (its barrier
+//                    gets the bytes and the arrival) and its G is prefetched
+//                    into L2 (one bulk prefetch), so the pointwise stage's
+//                    loads wait on L2 rather than HBM.
 //   FP32, G staged:  the same, but the arrival on the other buffer's barrier
 //                    comes with the next tile's G, issued into the single G
 //                    stage after tile t's pointwise stage.
@@ -388,24 +390,17 @@ __global__ void __launch_bounds__(NT, MINB)
         const int b = (NB == 2) ? (it & 1) : 0;
         const uint32_t parity = (NB == 2) ? uint32_t((it >> 1) & 1) : uint32_t(it & 1);
         const int tn = t + gridDim.x;
+        // nothing of the next tile is in flight yet: a failed wait just leaves
+        if (batch_wait_failed(&bars[b], parity, ctx, tid)) return;
         if constexpr (NB == 2) {
-            // the other buffer was last read by the previous tile, which
-            // ended with a block barrier: the next tile's u and mass go there
-            // now, so that they land while this tile computes
+            // the other buffer was last read by the previous tile, whose last
+            // pass every thread finished before the wait's barrier: the next
+            // tile's u and mass go there now, so that they land while this
+            // tile computes
             if (tn < ntiles) {
                 if constexpr (GD) prefetch_g(tn);
                 issue_um(tn, b ^ 1, GD);
             }
-        }
-        if (batch_wait_failed(&bars[b], parity, ctx, tid)) {
-            if (NB == 2 && tn < ntiles) {
-                // the next tile's copies into the other buffer may be in
-                // flight: complete its phase's arrival (G staged: still owed)
-                // and wait for them before the block leaves
-                if (GS2 && tid == 0) mbar_arrive(&bars[b ^ 1]);
-                mbar_wait_bounded(&bars[b ^ 1], uint32_t(((it + 1) >> 1) & 1), ctx.wait_limit);
-            }
-            return;
         }
         const MultiTile tl = tiles[t];
         const MultiSeg& sg = prm.seg[tl.seg];
@@ -427,7 +422,7 @@ __global__ void __launch_bounds__(NT, MINB)
     case QQ:                                                                                                    \
         bk5_sweep_batch<Eng, QQ, 6, 2, true, DPAR, decltype(early), DOT>(                                      \
             nullptr, prm.eo.template at<QQ>().eo, prm.eo.template at<QQ>().eot, ub, gb, W0, W1, W2, W3,         \
-            tl.ne, tid, nt, vb, mb, lambda, &dacc, early);                                                      \
+            tl.ne, tid, nt, vb, mb, lambda, &dacc, early, NB == 1);                                             \
         break;
             BK_MULTI_EO_CASE(3)
             BK_MULTI_EO_CASE(4)
@@ -440,7 +435,10 @@ __global__ void __launch_bounds__(NT, MINB)
             default:
                 break;
         }
-        // FP64: the single buffer is free after the tile's last pass
+        // FP64: the single buffer is free after the tile's last pass (the
+        // batch ended with a barrier); FP32 storage: the next tile's wait
+        // has the barrier that separates this tile's last pass from the
+        // next writes of the boxes and of this tile's buffer
         if (NB == 1 && tn < ntiles) issue_um(tn, 0, true);
     }
     if constexpr (DOT) {
@@ -448,6 +446,7 @@ __global__ void __launch_bounds__(NT, MINB)
         // (the work boxes are free after the last tile; no static shared
         // memory, which would shrink the dynamic limit)
         double* wsum = reinterpret_cast<double*>(W0);
+        __syncthreads();   // the last tile's last pass may still read W0
         double s = double(dacc.s) + double(dacc.c);
         for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
         if ((tid & 31) == 0) wsum[tid >> 5] = s;
